@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Reconstruction benchmark: 10M-point cloud, normals + signed distance + PMC.
+
+Workload (the lvr2 plain GPU configuration at scale): 10,000,000 float32
+points uniform on the surfaces of 200 random spheres (r in [0.02, 0.2]) and
+100 tori in the unit cube, noise sigma 1e-3 (seeded, lvr2_gb300.synthetic);
+kn = ki = kd = 20, PCA normals (nem 3) with lvr2's adaptive k (2kn .. 32kn),
+flip point = bounding-box centroid, voxel size 0.005, PMC decomposition.
+
+One step = the whole hot path on the resident cloud: LBVH build, normal
+estimation, normal interpolation, grid build, signed distance at every grid
+vertex, culling and marching cubes.  `value` = points / step time (every point
+gets its normal and the surface is extracted); the per-stage rates (normals/s,
+SDF evals/s, MC cells/s) are reported beside it.  `e2e` runs the same steps
+through the C ABI with host buffers (points in, normals and mesh out).
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement in oracle/ (kd-tree, AdaptiveKSearchSurface, PointsetGrid,
+FastReconstruction), on a spatial crop of the same cloud (same density).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "normals/s, SDF evals/s @10M pts; plain vs batched/adjoint form, ≤0.5° error"
+KN = KI = KD = 20
+VOXELSIZE = 0.005
+NEM = 3
+CPU_SAMPLE_FRACTION = 0.02
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--points", type=int, default=10_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(n):
+    from lvr2_gb300 import synthetic
+    return synthetic.spheres_tori(n, seed=2)
+
+
+def config(n, extra=None):
+    c = {"workload": "spheres_tori_%dM" % (n // 1_000_000) if n >= 1_000_000 else "spheres_tori_%d" % n,
+         "points": n, "kn": KN, "ki": KI, "kd": KD, "nem": NEM, "adaptive_k": True, "voxelsize": VOXELSIZE,
+         "decomposition": "PMC", "flip_point": "bbox centroid",
+         "l2": "inputs and per-step working set (>1 GB) larger than L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def normal_bytes(stats, kn):
+    """Algorithmic bytes of the normal stage (gather model: 16 B per point record
+    read, per neighbour per search round, + 16 B query + 12 B normal written)."""
+    total = 0
+    for r in range(5):
+        searched = sum(16 + 16 * kn * (2 ** (j + 1)) for j in range(r + 1))
+        total += int(stats[r]) * (searched + 12)
+    return total
+
+
+def sdf_bytes(n_vertices, kd):
+    return n_vertices * (12 + 32 * kd + 4 + 1)
+
+
+def cpu_reference_step(points, threads=0, canonical=False):
+    """One pass of the reference algorithm on the host (oracle/)."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    s = O.OracleSurface(points, leaf_size=20, threads=threads)
+    lo, hi, c = s.bbox()
+    n = s.normals(KN, nem=NEM, adaptive=True, flip=c, canonical=canonical)
+    n = s.interpolate(n, KI, canonical=canonical)
+    r = s.reconstruct(n, voxelsize=VOXELSIZE, kd=KD, decomposition="PMC", canonical=canonical)
+    dt = time.perf_counter() - t0
+    return dt, r
+
+
+def cpu_sample(points):
+    from lvr2_gb300 import synthetic
+    return np.ascontiguousarray(synthetic.crop(points, CPU_SAMPLE_FRACTION, center=np.array([0.5, 0.5, 0.5])))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    pts = workload(args.points)
+    sample = cpu_sample(pts)
+    for _ in range(args.warmup):
+        cpu_reference_step(sample)
+    times = []
+    for _ in range(args.steps):
+        dt, r = cpu_reference_step(sample)
+        times.append(dt)
+    value = len(sample) * len(times) / sum(times)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "normals/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config(args.points, {"sample_points": len(sample)}),
+        "cpu_baseline": {"value": value, "unit": "normals/s", "cores": cores, "kind": "port",
+                         "sample": "spatial crop of the 10M cloud (%d points, same density); full pipeline: "
+                                   "kd-tree (leaf 20), adaptive-k PCA normals, ki interpolation, grid + "
+                                   "signed distance + culling, PMC marching cubes" % len(sample)},
+        "e2e": {"value": value, "unit": "normals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import build as B
+    from lvr2_gb300.surface import kernel_launches
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    B.build()
+    pts = workload(args.points)
+    n = len(pts)
+    d_pts = torch.from_numpy(pts).to(f"cuda:{local}")
+    s = lvr2_gb300.Surface(d_pts, kn=KN, ki=KI, kd=KD, nem=NEM, adaptive=True, flip_point=None, device=local)
+
+    def step():
+        s.set_points(d_pts)
+        s.calculate_normals()
+        return s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    l0 = kernel_launches()
+    stage = np.zeros(7)
+    stats_acc = np.zeros(8)
+    infos = []
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record()
+        for _ in range(args.steps):
+            info = step()
+            stage += s.timings()
+            stats_acc += s.normal_stats()
+            infos.append((info.grid_vertices, info.cells_valid, info.faces, info.vertices))
+        t_end.record()
+        torch.cuda.synchronize()
+    launches = (kernel_launches() - l0) // max(args.steps, 1)
+    ms = t_start.elapsed_time(t_end) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    stage /= args.steps
+    stats = stats_acc / args.steps
+    nq, ncv, nf, nv = infos[-1]
+    value = world * n / (ms / 1000.0)
+
+    # ---- end to end through the C ABI with host buffers -----------------------
+    e2e = None
+    if not args.no_e2e:
+        h_norm = np.empty((n, 3), np.float32)
+        for _ in range(1):
+            s.set_points(pts)
+            s.calculate_normals()
+            s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+            h_norm = s.normals()
+            s.mesh(with_edges=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(args.steps):
+            s.set_points(pts)
+            s.calculate_normals()
+            info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+            h_norm = s.normals()
+            v, f, _ = s.mesh(with_edges=False)
+            d2h = h_norm.nbytes + v.nbytes + f.nbytes
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": world * n / e2e_s, "unit": "normals/s", "h2d_bytes_per_step": int(pts.nbytes),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = peaks()
+    nb = normal_bytes(stats, KN)
+    sb = sdf_bytes(nq, KD)
+    normals_ms, sdf_ms = float(stage[1]), float(stage[4])
+    if normals_ms >= sdf_ms:
+        dom = {"kernel": "normals_kernel<3> (fused kNN + PCA + flip, all adaptive rounds)",
+               "bytes": nb, "ms": normals_ms}
+    else:
+        dom = {"kernel": "sdf_kernel (kd-nearest signed distance)", "bytes": sb, "ms": sdf_ms}
+    achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "normals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(n, {"parallelism": "replicas" if world > 1 else "single"}),
+        "stages_ms": {"lbvh_build": float(stage[0]), "normals": normals_ms, "interpolation": float(stage[2]),
+                      "grid_build": float(stage[3]), "signed_distance": sdf_ms, "culling": float(stage[5]),
+                      "marching_cubes": float(stage[6])},
+        "rates": {"normals_per_s_stage": n / ((stage[0] + stage[1] + stage[2]) / 1000.0),
+                  "sdf_evals_per_s_stage": nq / (sdf_ms / 1000.0),
+                  "mc_cells_per_s_stage": ncv / (stage[6] / 1000.0) if stage[6] > 0 else None},
+        "counts": {"grid_vertices": int(nq), "cells_valid": int(ncv), "faces": int(nf), "vertices": int(nv),
+                   "fitted_per_round": [int(x) for x in stats[:5]], "fp64_eigensolves": int(stats[5])},
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes": int(dom["bytes"]), "traffic": None},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+    }
+    if not args.no_cpu_baseline:
+        sample = cpu_sample(pts)
+        dt, _ = cpu_reference_step(sample)
+        line["cpu_baseline"] = {"value": len(sample) / dt, "unit": "normals/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": "spatial crop of the cloud (%d points, same density), one pass of "
+                                          "the full CPU pipeline (oracle/ restatement of the reference)"
+                                          % len(sample)}
+    print(json.dumps(line))
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+/*
+ * lvrgb.h -- C ABI of liblvrgb.so, the GB300 (sm_103a) implementation of the
+ * lvr2 surface-reconstruction hot path: LBVH kNN, point normals, normal
+ * interpolation, signed distance at grid vertices and marching cubes.
+ *
+ * Each entry point replaces one piece of the lvr2 interface; the citation in
+ * its comment names the lvr2 declaration (path inside the lvr2 source tree).
+ *
+ * Conventions
+ *  - Point, normal and query arrays are float32 x,y,z triples (AoS), in the
+ *    caller's order, like PointBuffer's "points" / "normals" channels.
+ *  - on_device = 0: pointers are host memory; the call copies through pinned
+ *    staging and returns when the result is in host memory.
+ *    on_device = 1: pointers are device memory of the handle's GPU; the call
+ *    is asynchronous on `stream` unless stated otherwise.
+ *  - stream: a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - No exception crosses the ABI.  Every call returns an lvrgb_status; the
+ *    message of the last failure on the calling thread is lvrgb_last_error().
+ *  - A handle is not thread-safe: use one handle per host thread (lvr2 calls
+ *    PointsetSurface::distance from OpenMP threads; route those through
+ *    lvrgb_distance in one batched call instead).
+ *  - Neighbour order: k nearest = the k smallest keys (d2, index), where
+ *    d2 = fl(fl(fl(dx*dx) + fl(dy*dy)) + fl(dz*dz)), dx = fl(qx - px) in
+ *    float32 without fused multiply-add, and index is the point's position in
+ *    the input array.  lvr2's kd-tree ranks by double-precision d2 with
+ *    traversal-order tie handling; both agree except on float32 near-ties.
+ */
+#ifndef LVRGB_H
+#define LVRGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lvrgb_status {
+    LVRGB_OK = 0,
+    LVRGB_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, k, voxel size or method */
+    LVRGB_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+    LVRGB_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed (lvr2 retries smaller chunks) */
+    LVRGB_ERR_UNSUPPORTED = 4,      /* e.g. nem 1 (RANSAC) */
+    LVRGB_ERR_STATE = 5,            /* call order: no normals yet, no mesh yet */
+    LVRGB_ERR_KERNEL = 6            /* a kernel reported an internal limit (traversal depth) */
+} lvrgb_status;
+
+typedef struct lvrgb_surface_s* lvrgb_surface;
+
+/* Construction parameters of a surface.
+ * Replaces AdaptiveKSearchSurface(PointBufferPtr, string searchTreeName,
+ * int kn, int ki, int kd, int calcMethod, string posefile)
+ * (include/lvr2/reconstruction/AdaptiveKSearchSurface.hpp:99-107) and
+ * CudaSurface(floatArr& points, size_t num_points, int device)
+ * (include/lvr2/reconstruction/cuda/CudaSurface.hpp:80). */
+typedef struct lvrgb_surface_config {
+    int32_t kn;            /* normal estimation neighbourhood (first search uses 2*kn) */
+    int32_t ki;            /* interpolation neighbourhood, 0 = no interpolation */
+    int32_t kd;            /* signed-distance neighbourhood */
+    int32_t nem;           /* plane fit: 0 least squares (lvr2 default), 2 iterative, 3 PCA */
+    int32_t adaptive;      /* 1: k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed */
+    int32_t flip_set;      /* 0: flip point = bounding-box centroid (AdaptiveKSearchSurface::init) */
+    float flip[3];         /* flip point when flip_set != 0 */
+    int32_t bucket;        /* LBVH bucket size 1..32 (0 = 32) */
+    float gap_threshold;   /* relative eigengap below which PCA solves in FP64 (0 = 1e-3) */
+    int32_t device;        /* CUDA device ordinal */
+} lvrgb_surface_config;
+
+/* Fills the lvr2_reconstruct defaults: kn 10, ki 10, kd 5, nem 0, adaptive,
+ * flip point (0,0,0) (src/tools/lvr2_reconstruct/Options.cpp:69-118,
+ * Main.cpp:335-349). */
+void lvrgb_surface_config_default(lvrgb_surface_config* cfg);
+
+/* Builds the search structure over n points.  Replaces the search-tree
+ * construction of AdaptiveKSearchSurface (getSearchTree,
+ * include/lvr2/util/Factories.tcc:44-83; SearchKDTree ctor,
+ * include/lvr2/algorithm/KDTree.tcc:317-329), PointsetSurface's bounding box
+ * (include/lvr2/reconstruction/PointsetSurface.tcc:39-58) and
+ * LBVHIndex::build (include/lvr2/reconstruction/cuda/LBVHIndex.hpp:114). */
+lvrgb_status lvrgb_surface_create(const lvrgb_surface_config* cfg, const float* xyz, int64_t n,
+                                  int32_t on_device, void* stream, lvrgb_surface* out);
+
+/* Frees the handle and its device memory (CudaSurface::freeGPU,
+ * include/lvr2/reconstruction/cuda/CudaSurface.hpp:158). */
+lvrgb_status lvrgb_surface_destroy(lvrgb_surface s);
+
+/* PointsetSurface::setKn/setKi/setKd (PointsetSurface.hpp:112-126),
+ * CudaSurface::setKn/setKi/setKd (CudaSurface.hpp:108-126).  A value < 0
+ * leaves that parameter unchanged. */
+lvrgb_status lvrgb_surface_set_k(lvrgb_surface s, int32_t kn, int32_t ki, int32_t kd);
+
+/* PointsetSurface::setFlipPoint (PointsetSurface.hpp:128-131),
+ * CudaSurface::setFlippoint (CudaSurface.hpp:136). */
+lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, float z);
+
+/* Plane-fit method: AdaptiveKSearchSurface calcMethod / CudaSurface::setMethod
+ * (CudaSurface.hpp:144).  nem 1 (RANSAC) returns LVRGB_ERR_UNSUPPORTED. */
+lvrgb_status lvrgb_surface_set_method(lvrgb_surface s, int32_t nem);
+
+/* PointsetSurface::getBoundingBox (PointsetSurface.hpp:106): out9 = min xyz,
+ * max xyz, centroid xyz (BoundingBox.tcc:198-215 arithmetic). */
+lvrgb_status lvrgb_surface_bounding_box(lvrgb_surface s, float out9[9]);
+lvrgb_status lvrgb_surface_num_points(lvrgb_surface s, int64_t* n);
+
+/* AdaptiveKSearchSurface::calculateSurfaceNormals
+ * (include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:158-290) followed,
+ * when ki > 0, by interpolateSurfaceNormals (:293-335).  Replaces
+ * CudaSurface::calculateNormals (CudaSurface.hpp:88) and
+ * LBVHIndex::knn_normals (LBVHIndex.hpp:301).  Synchronous. */
+lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream);
+
+/* AdaptiveKSearchSurface::interpolateSurfaceNormals
+ * (include/lvr2/reconstruction/AdaptiveKSearchSurface.hpp:188, .tcc:293-335),
+ * CudaSurface::interpolateNormals (CudaSurface.hpp:93): replaces the current
+ * normals (estimated or set) by their ki-neighbourhood interpolation.
+ * Synchronous. */
+lvrgb_status lvrgb_interpolate_normals(lvrgb_surface s, void* stream);
+
+/* Normals in input order (n x 3).  CudaSurface::getNormals(floatArr)
+ * (CudaSurface.hpp:99); PointBuffer "normals" channel. */
+lvrgb_status lvrgb_get_normals(lvrgb_surface s, float* normals, int32_t on_device, void* stream);
+
+/* Normals before interpolation (n x 3), and the k of the search whose
+ * neighbourhood fitted each plane (may be NULL). */
+lvrgb_status lvrgb_get_raw_normals(lvrgb_surface s, float* normals, int32_t* k_used, int32_t on_device,
+                                   void* stream);
+
+/* Use given normals instead of estimating them (lvr2_reconstruct without
+ * --recalcNormals on a cloud with normals, Main.cpp:380-383). */
+lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on_device, void* stream);
+
+/* Counters of the last lvrgb_calculate_normals: out[0..4] planes fitted in
+ * search round 1..5, out[5] PCA eigensolves done in FP64. */
+lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[8]);
+
+/* Batched k-nearest-neighbour search: SearchTree::kSearch / kSearchParallel
+ * (include/lvr2/reconstruction/SearchTree.hpp:71, 101-125),
+ * LBVHIndex::kSearch (LBVHIndex.hpp:135).  Rows of k, ascending; idx =
+ * input indices (0xffffffff padding), dist = Euclidean distance (+inf
+ * padding), count (may be NULL) = neighbours found.  Synchronous for host
+ * pointers. */
+lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, uint32_t* idx, float* dist,
+                       int32_t* count, int32_t on_device, void* stream);
+
+/* AdaptiveKSearchSurface::distance for nq positions
+ * (AdaptiveKSearchSurface.tcc:414-457, PointsetSurface.hpp:74-75): projected
+ * and Euclidean distance to the mean of the kd nearest points along their
+ * normalised mean normal. */
+lvrgb_status lvrgb_distance(lvrgb_surface s, const float* q, int64_t nq, float* projected, float* euclidean,
+                            int32_t on_device, void* stream);
+
+/* CudaSurface::distances(std::vector<QueryPoint<Vec>>&, float voxel_size)
+ * (CudaSurface.hpp:156): projected distance and the invalid flag of
+ * PointsetGrid::calcDistanceValues (euclidean > 1.75 * voxel_size,
+ * PointsetGrid.tcc:133-140). */
+lvrgb_status lvrgb_grid_distances(lvrgb_surface s, const float* q, int64_t nq, float voxel_size, float* distance,
+                                  uint8_t* invalid, int32_t on_device, void* stream);
+
+/* PointsetSurface::getInterpolatedNormal (PointsetSurface.tcc:61-74) for nq
+ * positions (n x 3 out). */
+lvrgb_status lvrgb_interpolated_normal(lvrgb_surface s, const float* q, int64_t nq, float* out,
+                                       int32_t on_device, void* stream);
+
+/* Grid and marching-cubes parameters: the lvr2_reconstruct flags --voxelsize,
+ * --intersections, --noExtrusion, --decomposition (Options.cpp:69-74). */
+typedef struct lvrgb_grid_config {
+    float resolution;       /* voxel size, or intersections when is_voxelsize == 0 */
+    int32_t is_voxelsize;
+    int32_t extrude;        /* 0 = --noExtrusion */
+    int32_t decomposition;  /* 0 = MC (FastBox), 1 = PMC (BilinearFastBox, lvr2 default) */
+} lvrgb_grid_config;
+
+typedef struct lvrgb_mesh_info {
+    int64_t cells_all;      /* grid cells before culling */
+    int64_t grid_vertices;  /* query points */
+    int64_t cells_valid;    /* cells after culling ("Grid Cells" log line) */
+    int64_t vertices;       /* mesh vertices */
+    int64_t faces;          /* mesh faces */
+    float voxelsize;
+    float stage_ms[4];      /* device time: grid build, signed distance, culling, marching cubes */
+} lvrgb_mesh_info;
+
+/* PointsetGrid construction (include/lvr2/reconstruction/PointsetGrid.tcc:41-109),
+ * calcDistanceValues (:111-185) and FastReconstruction::getMesh
+ * (include/lvr2/reconstruction/FastReconstruction.tcc:47-66) with FastBox /
+ * BilinearFastBox::getSurface (FastBox.tcc:205-269, BilinearFastBox.tcc:55-138),
+ * as called by createGridAndReconstruction (src/tools/lvr2_reconstruct/Main.cpp:404-453).
+ * Needs normals (lvrgb_calculate_normals or lvrgb_set_normals).  The mesh
+ * stays on the handle until the next call.  Synchronous. */
+lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrgb_mesh_info* info, void* stream);
+
+/* The last mesh: vertices (V x 3), faces (F x 3 vertex indices, MC-table
+ * orientation) and, optionally, each vertex's grid edge (V x 4: lattice x, y,
+ * z of the edge's lower corner and the edge axis 0/1/2).  Replaces the
+ * BaseMesh::addVertex / addFace calls of FastBox::getSurface
+ * (include/lvr2/geometry/BaseMesh.hpp:115, 131). */
+lvrgb_status lvrgb_get_mesh(lvrgb_surface s, float* vertices, uint32_t* faces, int32_t* vertex_edges,
+                            int32_t on_device, void* stream);
+
+/* The last grid, sorted by lattice key: each grid vertex's lattice index
+ * (Q x 3), position (Q x 3), projected distance and invalid flag; any
+ * pointer may be NULL.  Same content as HashGrid::getQueryPoints
+ * (include/lvr2/reconstruction/HashGrid.hpp:179). */
+lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, float* distance,
+                            uint8_t* invalid, int32_t on_device, void* stream);
+
+/* Cells of the last grid as lattice indices (x, y, z of the cell's lowest
+ * corner): all cells before culling and the valid cells (either may be NULL).
+ * HashGrid::getCells (HashGrid.hpp:182). */
+lvrgb_status lvrgb_get_cells(lvrgb_surface s, int32_t* cells_all, int32_t* cells_valid, int32_t on_device,
+                             void* stream);
+
+/* Replaces the points of an existing handle and rebuilds its search
+ * structure, reusing its device memory (LBVHIndex::build on an existing
+ * index, include/lvr2/reconstruction/cuda/LBVHIndex.hpp:114).  Normals and
+ * the mesh of the previous points are dropped. */
+lvrgb_status lvrgb_surface_set_points(lvrgb_surface s, const float* xyz, int64_t n, int32_t on_device,
+                                      void* stream);
+
+/* Device time in ms of the handle's last calls: out[0] search-structure
+ * build, [1] normal estimation, [2] interpolation, [3] grid build, [4]
+ * signed distance, [5] culling, [6] marching cubes; [7] unused.  These are the
+ * stage boundaries of lvr2_reconstruct's log lines (README.md:118-124).  No
+ * lvr2 counterpart beyond those log lines. */
+lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]);
+
+/* Number of kernels this library has launched in the process (diagnostics;
+ * no lvr2 counterpart). */
+lvrgb_status lvrgb_kernel_launches(uint64_t* out);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lvrgb_last_error(void);
+
+/* Library version string. */
+const char* lvrgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LVRGB_H */

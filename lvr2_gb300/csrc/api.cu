@@ -1,0 +1,720 @@
+// api.cu -- the C ABI (include/lvrgb.h): handle, input staging, call
+// sequencing and error translation.  No exception crosses this file's
+// extern "C" functions.
+#include <atomic>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/lvrgb.h"
+#include "grid.h"
+#include "lbvh_build.h"
+#include "surface.h"
+
+using namespace lvrgb;
+
+struct lvrgb_surface_s {
+    lvrgb_surface_config cfg;
+    int device = 0;
+    Workspace ws;
+    Lbvh T;
+    float bb[9] = {0};
+    float* d_box = nullptr;
+    int* d_err = nullptr;
+    uint32_t* d_stats = nullptr;
+    float4* normals = nullptr;      // final normals, Morton order
+    float4* raw_normals = nullptr;  // before interpolation
+    int32_t* kused = nullptr;
+    bool has_normals = false;
+    bool has_raw = false;
+    GridResult grid;
+    bool has_grid = false;
+    // device-time events: LBVH build, normal estimation, interpolation
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool ev_used[3] = {false, false, false};
+    float grid_ms[4] = {0, 0, 0, 0};
+    ~lvrgb_surface_s() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+namespace lvrgb {
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace lvrgb
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct ApiError {
+    lvrgb_status st;
+    std::string msg;
+};
+
+lvrgb_status fail(lvrgb_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+template <typename F>
+lvrgb_status guarded(F&& f) {
+    try {
+        f();
+        return LVRGB_OK;
+    } catch (const ApiError& e) {
+        return fail(e.st, e.msg);
+    } catch (const CudaError& e) {
+        std::string m = std::string(cudaGetErrorString(e.err)) + " at " + e.file + ":" + std::to_string(e.line);
+        cudaGetLastError();  // clear a sticky launch error where possible
+        if (e.err == cudaErrorMemoryAllocation) return fail(LVRGB_ERR_OUT_OF_MEMORY, m);
+        return fail(LVRGB_ERR_CUDA, m);
+    } catch (const std::invalid_argument& e) {
+        return fail(LVRGB_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(LVRGB_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(LVRGB_ERR_CUDA, e.what());
+    } catch (...) {
+        return fail(LVRGB_ERR_CUDA, "unknown error");
+    }
+}
+
+void require(bool ok, lvrgb_status st, const char* msg) {
+    if (!ok) throw ApiError{st, msg};
+}
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        LVRGB_CUDA(cudaGetDevice(&prev));
+        if (prev != dev) LVRGB_CUDA(cudaSetDevice(dev));
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != prev && prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// Device view of an input array: device pointers pass through, host arrays
+// are copied into a workspace buffer.
+template <typename T>
+const T* stage_in(Workspace& ws, const char* name, const T* p, size_t count, int on_device, cudaStream_t s) {
+    if (on_device) return p;
+    T* d = ws.get<T>(name, count);
+    if (count) LVRGB_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * count, cudaMemcpyHostToDevice, s));
+    return d;
+}
+// Device destination for an output array; finish_out copies it to the host.
+template <typename T>
+T* stage_out(Workspace& ws, const char* name, T* p, size_t count, int on_device) {
+    return on_device ? p : ws.get<T>(name, count);
+}
+template <typename T>
+void finish_out(T* host, const T* dev, size_t count, int on_device, cudaStream_t s) {
+    if (on_device || !host) return;
+    if (count) LVRGB_CUDA(cudaMemcpyAsync(host, dev, sizeof(T) * count, cudaMemcpyDeviceToHost, s));
+}
+
+void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
+    int* h = reinterpret_cast<int*>(s->ws.pinned());
+    h[0] = 0;
+    LVRGB_CUDA(cudaMemcpyAsync(h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LVRGB_CUDA(cudaStreamSynchronize(st));
+    if (h[0]) {
+        LVRGB_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int), st));
+        throw ApiError{LVRGB_ERR_KERNEL, "kNN traversal exceeded its stack depth"};
+    }
+}
+
+__global__ void morton_to_aos_kernel(const float4* __restrict__ v, const float4* __restrict__ pts, int n,
+                                     float* __restrict__ out) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    size_t o = __float_as_uint(pts[j].w);
+    float4 a = v[j];
+    out[3 * o] = a.x;
+    out[3 * o + 1] = a.y;
+    out[3 * o + 2] = a.z;
+}
+__global__ void aos_to_morton_kernel(const float* __restrict__ in, const float4* __restrict__ pts, int n,
+                                     float4* __restrict__ v) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    size_t o = __float_as_uint(pts[j].w);
+    v[j] = make_float4(in[3 * o], in[3 * o + 1], in[3 * o + 2], 0.0f);
+}
+__global__ void morton_to_orig_i32_kernel(const int32_t* __restrict__ v, const float4* __restrict__ pts, int n,
+                                          int32_t* __restrict__ out) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    out[__float_as_uint(pts[j].w)] = v[j];
+}
+__global__ void decode_lattice_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ sel, int n,
+                                      int bx, int by, int bz, int32_t* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t x, y, z;
+    lattice_decode(keys[sel ? sel[i] : uint32_t(i)], x, y, z);
+    out[3 * size_t(i)] = int(x) + bx;
+    out[3 * size_t(i) + 1] = int(y) + by;
+    out[3 * size_t(i) + 2] = int(z) + bz;
+}
+__global__ void decode_edges_kernel(const uint64_t* __restrict__ keys, int n, int bx, int by, int bz,
+                                    int32_t* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t k = keys[i];
+    uint32_t x, y, z;
+    lattice_decode(k >> 2, x, y, z);
+    out[4 * size_t(i)] = int(x) + bx;
+    out[4 * size_t(i) + 1] = int(y) + by;
+    out[4 * size_t(i) + 2] = int(z) + bz;
+    out[4 * size_t(i) + 3] = int(k & 3);
+}
+__global__ void pos3_kernel(const float4* __restrict__ p, int n, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = p[i];
+    out[3 * size_t(i)] = a.x;
+    out[3 * size_t(i) + 1] = a.y;
+    out[3 * size_t(i) + 2] = a.z;
+}
+
+NormalsConfig normals_config(const lvrgb_surface_s* s) {
+    NormalsConfig c;
+    c.kn = s->cfg.kn;
+    c.nem = s->cfg.nem;
+    c.adaptive = s->cfg.adaptive;
+    if (s->cfg.flip_set) {
+        c.flip[0] = s->cfg.flip[0]; c.flip[1] = s->cfg.flip[1]; c.flip[2] = s->cfg.flip[2];
+    } else {
+        c.flip[0] = s->bb[6]; c.flip[1] = s->bb[7]; c.flip[2] = s->bb[8];
+    }
+    c.gap_threshold = s->cfg.gap_threshold > 0 ? s->cfg.gap_threshold : 1e-3f;
+    return c;
+}
+
+void check_nem(int nem) {
+    require(nem != 1, LVRGB_ERR_UNSUPPORTED, "nem 1 (RANSAC plane fit) is not supported");
+    require(nem == 0 || nem == 2 || nem == 3, LVRGB_ERR_INVALID_ARGUMENT, "nem must be 0, 2 or 3");
+}
+
+// Sorts host/device query positions into Morton order on the device.
+const float4* prepare_queries(lvrgb_surface s, const float* q, int64_t nq, int on_device, cudaStream_t st) {
+    const float* dq = stage_in(s->ws, "api.q", q, size_t(nq) * 3, on_device, st);
+    float4* qs = s->ws.get<float4>("api.qs", size_t(nq));
+    sort_queries(dq, int(nq), s->d_box, qs, s->ws, st);
+    return qs;
+}
+
+void record(lvrgb_surface s, int i, cudaStream_t st) {
+    if (!s->ev[i]) LVRGB_CUDA(cudaEventCreate(&s->ev[i]));
+    LVRGB_CUDA(cudaEventRecord(s->ev[i], st));
+}
+
+// (Re)builds the search structure and bounding box of a handle.
+void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, cudaStream_t st) {
+    require(n >= 0 && n < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "point count must be in [0, 2^31)");
+    require(n == 0 || xyz != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "xyz is NULL");
+    s->has_normals = s->has_raw = s->has_grid = false;
+    const float* dx = stage_in(s->ws, "api.xyz", xyz, size_t(n) * 3, on_device, st);
+    record(s, 0, st);
+    lbvh_build(dx, int(n), s->cfg.bucket, s->ws, "tree", s->T, s->d_box, st);
+    record(s, 1, st);
+    s->ev_used[0] = true;
+    float h[6] = {0, 0, 0, 0, 0, 0};
+    if (n > 0) {
+        LVRGB_CUDA(cudaMemcpyAsync(h, s->d_box, 6 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+    } else {
+        // empty BoundingBox: min = FLT_MAX, max = lowest (BoundingBox.tcc:45-53)
+        h[0] = h[1] = h[2] = FLT_MAX;
+        h[3] = h[4] = h[5] = -FLT_MAX;
+    }
+    for (int i = 0; i < 6; i++) s->bb[i] = h[i];
+    // BoundingBox centroid (BoundingBox.tcc:210-214)
+    for (int a = 0; a < 3; a++) s->bb[6 + a] = h[a] + 0.5f * (h[3 + a] - h[a]);
+    s->normals = s->ws.get<float4>("api.normals", size_t(n));
+    s->raw_normals = s->ws.get<float4>("api.raw_normals", size_t(n));
+    s->kused = s->ws.get<int32_t>("api.kused", size_t(n));
+}
+
+}  // namespace
+
+extern "C" {
+
+void lvrgb_surface_config_default(lvrgb_surface_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->kn = 10;
+    cfg->ki = 10;
+    cfg->kd = 5;
+    cfg->nem = 0;
+    cfg->adaptive = 1;
+    cfg->flip_set = 1;
+    cfg->bucket = 32;
+    cfg->gap_threshold = 1e-3f;
+    cfg->device = 0;
+}
+
+lvrgb_status lvrgb_surface_create(const lvrgb_surface_config* cfg, const float* xyz, int64_t n, int32_t on_device,
+                                  void* stream, lvrgb_surface* out) {
+    if (!out) return fail(LVRGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    lvrgb_surface s = nullptr;
+    lvrgb_status st = guarded([&] {
+        require(cfg != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "cfg is NULL");
+        require(n >= 0 && n < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "point count must be in [0, 2^31)");
+        require(n == 0 || xyz != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "xyz is NULL");
+        require(cfg->kn > 0 && cfg->ki >= 0 && cfg->kd > 0, LVRGB_ERR_INVALID_ARGUMENT, "kn, kd must be > 0, ki >= 0");
+        check_nem(cfg->nem);
+        require(cfg->bucket >= 0 && cfg->bucket <= 32, LVRGB_ERR_INVALID_ARGUMENT, "bucket must be in 0..32");
+        DeviceScope dev(cfg->device);
+        cudaStream_t st = as_stream(stream);
+        s = new lvrgb_surface_s();
+        s->cfg = *cfg;
+        if (s->cfg.bucket == 0) s->cfg.bucket = 32;
+        s->device = cfg->device;
+        s->d_box = s->ws.get<float>("api.box", 8);
+        s->d_err = s->ws.get<int>("api.err", 4);
+        s->d_stats = s->ws.get<uint32_t>("api.stats", kNormalStats);
+        LVRGB_CUDA(cudaMemsetAsync(s->d_err, 0, 4 * sizeof(int), st));
+        LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
+        build_points(s, xyz, n, on_device, st);
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+    if (st != LVRGB_OK) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return LVRGB_OK;
+}
+
+lvrgb_status lvrgb_surface_destroy(lvrgb_surface s) {
+    if (!s) return LVRGB_OK;
+    return guarded([&] {
+        DeviceScope dev(s->device);
+        delete s;
+    });
+}
+
+lvrgb_status lvrgb_surface_set_k(lvrgb_surface s, int32_t kn, int32_t ki, int32_t kd) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(kn != 0 && kd != 0, LVRGB_ERR_INVALID_ARGUMENT, "kn and kd must be > 0");
+        if (kn > 0) s->cfg.kn = kn;
+        if (ki >= 0) s->cfg.ki = ki;
+        if (kd > 0) s->cfg.kd = kd;
+    });
+}
+
+lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, float z) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        s->cfg.flip_set = 1;
+        s->cfg.flip[0] = x; s->cfg.flip[1] = y; s->cfg.flip[2] = z;
+    });
+}
+
+lvrgb_status lvrgb_surface_set_method(lvrgb_surface s, int32_t nem) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        check_nem(nem);
+        s->cfg.nem = nem;
+    });
+}
+
+lvrgb_status lvrgb_surface_bounding_box(lvrgb_surface s, float out9[9]) {
+    return guarded([&] {
+        require(s != nullptr && out9 != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        std::memcpy(out9, s->bb, sizeof(s->bb));
+    });
+}
+
+lvrgb_status lvrgb_surface_num_points(lvrgb_surface s, int64_t* n) {
+    return guarded([&] {
+        require(s != nullptr && n != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        *n = s->T.n;
+    });
+}
+
+lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
+        NormalsConfig c = normals_config(s);
+        record(s, 2, st);
+        compute_normals(s->T, c, s->raw_normals, s->kused, s->ws, s->d_err, s->d_stats, st);
+        record(s, 3, st);
+        s->ev_used[1] = true;
+        s->has_raw = true;
+        record(s, 4, st);
+        if (s->cfg.ki > 0)
+            interpolate_normals(s->T, s->cfg.ki, s->raw_normals, s->normals, s->ws, s->d_err, st);
+        record(s, 5, st);
+        s->ev_used[2] = true;
+        if (s->cfg.ki <= 0 && s->T.n)
+            LVRGB_CUDA(cudaMemcpyAsync(s->normals, s->raw_normals, sizeof(float4) * size_t(s->T.n),
+                                       cudaMemcpyDeviceToDevice, st));
+        check_kernel_error(s, st);
+        s->has_normals = true;
+    });
+}
+
+lvrgb_status lvrgb_interpolate_normals(lvrgb_surface s, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(s->cfg.ki > 0, LVRGB_ERR_INVALID_ARGUMENT, "ki must be > 0");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        float4* tmp = s->ws.get<float4>("api.interp_tmp", size_t(s->T.n));
+        interpolate_normals(s->T, s->cfg.ki, s->normals, tmp, s->ws, s->d_err, st);
+        if (s->T.n)
+            LVRGB_CUDA(cudaMemcpyAsync(s->normals, tmp, sizeof(float4) * size_t(s->T.n), cudaMemcpyDeviceToDevice, st));
+        check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_get_normals(lvrgb_surface s, float* normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(normals != nullptr || s->T.n == 0, LVRGB_ERR_INVALID_ARGUMENT, "normals is NULL");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const int n = s->T.n;
+        float* d = stage_out(s->ws, "api.out3", normals, size_t(n) * 3, on_device);
+        if (n) {
+            morton_to_aos_kernel<<<ceil_div(n, 256), 256, 0, st>>>(s->normals, s->T.pts, n, d);
+            LVRGB_LAUNCH_CHECK();
+        }
+        finish_out(normals, d, size_t(n) * 3, on_device, st);
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_get_raw_normals(lvrgb_surface s, float* normals, int32_t* k_used, int32_t on_device,
+                                   void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_raw, LVRGB_ERR_STATE, "no estimated normals: call lvrgb_calculate_normals");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const int n = s->T.n;
+        if (normals) {
+            float* d = stage_out(s->ws, "api.out3", normals, size_t(n) * 3, on_device);
+            if (n) {
+                morton_to_aos_kernel<<<ceil_div(n, 256), 256, 0, st>>>(s->raw_normals, s->T.pts, n, d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(normals, d, size_t(n) * 3, on_device, st);
+        }
+        if (k_used) {
+            int32_t* d = stage_out(s->ws, "api.outk", k_used, size_t(n), on_device);
+            if (n) {
+                morton_to_orig_i32_kernel<<<ceil_div(n, 256), 256, 0, st>>>(s->kused, s->T.pts, n, d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(k_used, d, size_t(n), on_device, st);
+        }
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(normals != nullptr || s->T.n == 0, LVRGB_ERR_INVALID_ARGUMENT, "normals is NULL");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const int n = s->T.n;
+        const float* d = stage_in(s->ws, "api.in3", normals, size_t(n) * 3, on_device, st);
+        if (n) {
+            aos_to_morton_kernel<<<ceil_div(n, 256), 256, 0, st>>>(d, s->T.pts, n, s->normals);
+            LVRGB_LAUNCH_CHECK();
+        }
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+        s->has_normals = true;
+    });
+}
+
+lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[8]) {
+    return guarded([&] {
+        require(s != nullptr && out != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        DeviceScope dev(s->device);
+        LVRGB_CUDA(cudaMemcpy(out, s->d_stats, kNormalStats * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, uint32_t* idx, float* dist,
+                       int32_t* count, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(k > 0 && k <= (1 << 16), LVRGB_ERR_INVALID_ARGUMENT, "k must be in 1..65536");
+        require(nq == 0 || (q && idx && dist), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float4* qs = prepare_queries(s, q, nq, on_device, st);
+        const size_t rows = size_t(nq) * size_t(k);
+        uint32_t* di = stage_out(s->ws, "api.idx", idx, rows, on_device);
+        float* dd = stage_out(s->ws, "api.dist", dist, rows, on_device);
+        int32_t* dc = count ? stage_out(s->ws, "api.cnt", count, size_t(nq), on_device) : nullptr;
+        knn_rows(s->T, qs, int(nq), k, di, dd, dc, s->ws, s->d_err, st);
+        finish_out(idx, di, rows, on_device, st);
+        finish_out(dist, dd, rows, on_device, st);
+        if (count) finish_out(count, dc, size_t(nq), on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_distance(lvrgb_surface s, const float* q, int64_t nq, float* projected, float* euclidean,
+                            int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(nq == 0 || (q && projected), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float4* qs = prepare_queries(s, q, nq, on_device, st);
+        float* dp = stage_out(s->ws, "api.d1", projected, size_t(nq), on_device);
+        float* de = euclidean ? stage_out(s->ws, "api.d2", euclidean, size_t(nq), on_device) : nullptr;
+        signed_distance_rows(s->T, s->normals, s->cfg.kd, qs, int(nq), 1.0f, dp, de, nullptr, s->ws, s->d_err, st);
+        finish_out(projected, dp, size_t(nq), on_device, st);
+        if (euclidean) finish_out(euclidean, de, size_t(nq), on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_grid_distances(lvrgb_surface s, const float* q, int64_t nq, float voxel_size, float* distance,
+                                  uint8_t* invalid, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(voxel_size > 0, LVRGB_ERR_INVALID_ARGUMENT, "voxel_size must be > 0");
+        require(nq == 0 || (q && distance && invalid), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float4* qs = prepare_queries(s, q, nq, on_device, st);
+        float* dp = stage_out(s->ws, "api.d1", distance, size_t(nq), on_device);
+        uint8_t* di = stage_out(s->ws, "api.inv", invalid, size_t(nq), on_device);
+        signed_distance_rows(s->T, s->normals, s->cfg.kd, qs, int(nq), voxel_size, dp, nullptr, di, s->ws, s->d_err,
+                             st);
+        finish_out(distance, dp, size_t(nq), on_device, st);
+        finish_out(invalid, di, size_t(nq), on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_interpolated_normal(lvrgb_surface s, const float* q, int64_t nq, float* out, int32_t on_device,
+                                       void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(s->cfg.ki > 0, LVRGB_ERR_INVALID_ARGUMENT, "ki must be > 0");
+        require(nq == 0 || (q && out), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float4* qs = prepare_queries(s, q, nq, on_device, st);
+        float* d = stage_out(s->ws, "api.out3q", out, size_t(nq) * 3, on_device);
+        interpolated_normal_rows(s->T, s->normals, s->cfg.ki, qs, int(nq), d, s->ws, s->d_err, st);
+        finish_out(out, d, size_t(nq) * 3, on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrgb_mesh_info* info, void* stream) {
+    return guarded([&] {
+        require(s != nullptr && g != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(g->resolution > 0, LVRGB_ERR_INVALID_ARGUMENT, "resolution must be > 0");
+        require(g->decomposition == 0 || g->decomposition == 1, LVRGB_ERR_UNSUPPORTED,
+                "decomposition must be 0 (MC) or 1 (PMC)");
+        require(s->T.n > 0, LVRGB_ERR_INVALID_ARGUMENT, "empty point cloud");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        GridConfig c;
+        c.resolution = g->resolution;
+        c.is_voxelsize = g->is_voxelsize;
+        c.extrude = g->extrude;
+        c.kd = s->cfg.kd;
+        c.decomposition = g->decomposition;
+        GridTimings tm;
+        s->has_grid = false;
+        grid_reconstruct(s->T, s->normals, s->bb, c, s->ws, s->grid, s->d_err, st, &tm);
+        for (int i = 0; i < 4; i++) s->grid_ms[i] = tm.ms[i];
+        check_kernel_error(s, st);
+        s->has_grid = true;
+        if (info) {
+            info->cells_all = s->grid.ncells_all;
+            info->grid_vertices = s->grid.nqp;
+            info->cells_valid = s->grid.ncells_valid;
+            info->vertices = s->grid.nverts;
+            info->faces = s->grid.nfaces;
+            info->voxelsize = s->grid.vs;
+            for (int i = 0; i < 4; i++) info->stage_ms[i] = tm.ms[i];
+        }
+    });
+}
+
+lvrgb_status lvrgb_get_mesh(lvrgb_surface s, float* vertices, uint32_t* faces, int32_t* vertex_edges,
+                            int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const GridResult& R = s->grid;
+        const size_t nv = size_t(R.nverts), nf = size_t(R.nfaces);
+        if (vertices) {
+            if (on_device) {
+                if (nv) LVRGB_CUDA(cudaMemcpyAsync(vertices, R.verts, nv * 3 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            } else {
+                finish_out(vertices, R.verts, nv * 3, 0, st);
+            }
+        }
+        if (faces) {
+            if (on_device) {
+                if (nf) LVRGB_CUDA(cudaMemcpyAsync(faces, R.faces, nf * 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+            } else {
+                finish_out(faces, R.faces, nf * 3, 0, st);
+            }
+        }
+        if (vertex_edges) {
+            int32_t* d = stage_out(s->ws, "api.vedges", vertex_edges, nv * 4, on_device);
+            if (nv) {
+                decode_edges_kernel<<<ceil_div(nv, 256), 256, 0, st>>>(R.vert_keys, int(nv), R.base[0], R.base[1],
+                                                                             R.base[2], d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(vertex_edges, d, nv * 4, on_device, st);
+        }
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, float* distance, uint8_t* invalid,
+                            int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no grid: call lvrgb_reconstruct");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const GridResult& R = s->grid;
+        const size_t nq = size_t(R.nqp);
+        if (lattice) {
+            int32_t* d = stage_out(s->ws, "api.lat", lattice, nq * 3, on_device);
+            if (nq) {
+                decode_lattice_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(R.qp_keys, nullptr, int(nq), R.base[0],
+                                                                               R.base[1], R.base[2], d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(lattice, d, nq * 3, on_device, st);
+        }
+        if (position) {
+            float* d = stage_out(s->ws, "api.pos", position, nq * 3, on_device);
+            if (nq) {
+                pos3_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(R.qp_pos, int(nq), d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(position, d, nq * 3, on_device, st);
+        }
+        if (distance) {
+            if (on_device) {
+                if (nq) LVRGB_CUDA(cudaMemcpyAsync(distance, R.qp_dist, nq * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            } else {
+                finish_out(distance, R.qp_dist, nq, 0, st);
+            }
+        }
+        if (invalid) {
+            if (on_device) {
+                if (nq) LVRGB_CUDA(cudaMemcpyAsync(invalid, R.qp_invalid, nq, cudaMemcpyDeviceToDevice, st));
+            } else {
+                finish_out(invalid, R.qp_invalid, nq, 0, st);
+            }
+        }
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_get_cells(lvrgb_surface s, int32_t* cells_all, int32_t* cells_valid, int32_t on_device,
+                             void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no grid: call lvrgb_reconstruct");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const GridResult& R = s->grid;
+        if (cells_all) {
+            const size_t n = size_t(R.ncells_all);
+            int32_t* d = stage_out(s->ws, "api.ca", cells_all, n * 3, on_device);
+            if (n) {
+                decode_lattice_kernel<<<ceil_div(n, 256), 256, 0, st>>>(R.cell_keys, nullptr, int(n), R.base[0],
+                                                                             R.base[1], R.base[2], d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(cells_all, d, n * 3, on_device, st);
+        }
+        if (cells_valid) {
+            const size_t n = size_t(R.ncells_valid);
+            int32_t* d = stage_out(s->ws, "api.cv", cells_valid, n * 3, on_device);
+            if (n) {
+                decode_lattice_kernel<<<ceil_div(n, 256), 256, 0, st>>>(R.cell_keys, R.valid_cells, int(n),
+                                                                             R.base[0], R.base[1], R.base[2], d);
+                LVRGB_LAUNCH_CHECK();
+            }
+            finish_out(cells_valid, d, n * 3, on_device, st);
+        }
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_surface_set_points(lvrgb_surface s, const float* xyz, int64_t n, int32_t on_device,
+                                      void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        DeviceScope dev(s->device);
+        build_points(s, xyz, n, on_device, as_stream(stream));
+    });
+}
+
+lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]) {
+    return guarded([&] {
+        require(s != nullptr && out != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        DeviceScope dev(s->device);
+        for (int i = 0; i < 8; i++) out[i] = 0.0f;
+        for (int k = 0; k < 3; k++) {
+            if (!s->ev_used[k]) continue;
+            LVRGB_CUDA(cudaEventSynchronize(s->ev[2 * k + 1]));
+            LVRGB_CUDA(cudaEventElapsedTime(&out[k], s->ev[2 * k], s->ev[2 * k + 1]));
+        }
+        for (int i = 0; i < 4; i++) out[3 + i] = s->grid_ms[i];
+    });
+}
+
+lvrgb_status lvrgb_kernel_launches(uint64_t* out) {
+    if (!out) return fail(LVRGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = g_launches.load();
+    return LVRGB_OK;
+}
+
+const char* lvrgb_last_error(void) { return g_last_error.c_str(); }
+
+const char* lvrgb_version(void) { return "lvr2_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,525 @@
+// grid.cu -- PointsetGrid on the GPU: cell discovery and extrusion as sorted
+// lattice keys, grid vertices deduplicated by key, the kd-weighted signed
+// distance at every vertex, invalid-cell culling, and marching cubes with
+// edge-key vertex deduplication and compacted face output.
+//
+// Lattice keys are 3-D Morton codes of (coordinate - base), 20 bits per axis,
+// so that sorted cells and vertices are spatially coherent: consecutive grid
+// vertices form the 32-query groups of the signed-distance kNN.
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+#include "grid.h"
+#include "primitives.cuh"
+#include "surface.h"
+
+namespace lvrgb {
+
+namespace {
+
+// Cell corner offsets (box_creation_table of FastReconstructionTables.hpp:86,
+// mapped from -1/+1 to 0/1) and corner pairs of the 12 cell edges
+// (vertex_edge_table of FastBoxTables.hpp:71).
+__constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__constant__ int c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                  {6, 7}, {7, 4}, {0, 4}, {1, 5}, {3, 7}, {2, 6}};
+__constant__ unsigned long long c_mc[256] = {
+#include "mc_table.inc"
+};
+
+constexpr uint64_t kNoKey = ~0ull;
+
+struct Frame {
+    float vs;
+    int bx, by, bz;  // base
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float cell_center(int idx, float vs) { return __fmul_rn(__fadd_rn(float(idx), 0.5f), vs); }
+// Grid vertex coordinate: the centre of the cell whose lowest corner it is,
+// plus (-1) * (vs / 2) (HashGrid::addBox, HashGrid.tcc:235-259).
+__device__ __forceinline__ float lattice_coord(int L, float vs) {
+    return __fadd_rn(cell_center(L, vs), -__fdiv_rn(vs, 2.0f));
+}
+__device__ __forceinline__ bool inside(const Frame& F, float x, float y, float z) {
+    return (F.lo[0] <= x && F.hi[0] >= x) && (F.lo[1] <= y && F.hi[1] >= y) && (F.lo[2] <= z && F.hi[2] >= z);
+}
+
+__global__ void point_cells_kernel(const float4* __restrict__ pts, int n, Frame F, uint64_t* __restrict__ keys) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pts[i];
+    // HashGrid::calcIndex (HashGrid.hpp:263-268)
+    int ix = int(floorf(__fdiv_rn(p.x, F.vs)));
+    int iy = int(floorf(__fdiv_rn(p.y, F.vs)));
+    int iz = int(floorf(__fdiv_rn(p.z, F.vs)));
+    bool ok = inside(F, cell_center(ix, F.vs), cell_center(iy, F.vs), cell_center(iz, F.vs));
+    keys[i] = ok ? lattice_key(uint32_t(ix - F.bx), uint32_t(iy - F.by), uint32_t(iz - F.bz)) : kNoKey;
+}
+
+__global__ void extrude_kernel(const uint64_t* __restrict__ cells, int nc, Frame F, uint64_t* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 27) return;
+    int c = t / 27, o = t % 27;
+    uint32_t x, y, z;
+    lattice_decode(cells[c], x, y, z);
+    int dx = o / 9 - 1, dy = (o / 3) % 3 - 1, dz = o % 3 - 1;
+    int ix = int(x) + F.bx + dx, iy = int(y) + F.by + dy, iz = int(z) + F.bz + dz;
+    bool ok = inside(F, cell_center(ix, F.vs), cell_center(iy, F.vs), cell_center(iz, F.vs));
+    out[t] = ok ? lattice_key(uint32_t(int(x) + dx), uint32_t(int(y) + dy), uint32_t(int(z) + dz)) : kNoKey;
+}
+
+__global__ void corner_pairs_kernel(const uint64_t* __restrict__ cells, int nc, uint64_t* __restrict__ keys,
+                                    uint32_t* __restrict__ vals) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 8) return;
+    int c = t >> 3, k = t & 7;
+    uint32_t x, y, z;
+    lattice_decode(cells[c], x, y, z);
+    keys[t] = lattice_key(x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2]);
+    vals[t] = uint32_t(t);
+}
+
+// After sorting (key, slot) pairs: vertex id of every slot and the unique keys.
+__global__ void assign_ids_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                  const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, int n,
+                                  uint32_t* __restrict__ slot_id, uint64_t* __restrict__ ukeys,
+                                  uint32_t* __restrict__ first_slot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t id = pos[i] + flags[i] - 1u;
+    slot_id[vals[i]] = id;
+    if (flags[i]) {
+        ukeys[id] = keys[i];
+        if (first_slot) first_slot[id] = vals[i];
+    }
+}
+
+__global__ void qp_pos_kernel(const uint64_t* __restrict__ keys, int n, Frame F, float4* __restrict__ pos) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t x, y, z;
+    lattice_decode(keys[i], x, y, z);
+    pos[i] = make_float4(lattice_coord(int(x) + F.bx, F.vs), lattice_coord(int(y) + F.by, F.vs),
+                         lattice_coord(int(z) + F.bz, F.vs), __uint_as_float(uint32_t(i)));
+}
+
+struct SdfArgs {
+    Lbvh T;
+    int K;
+    const float4* normals;
+    const float4* qs;
+    int nq;
+    double limit;  // 1.75 * voxelsize
+    float* dist;
+    float* eucl;
+    uint8_t* invalid;
+    unsigned long long* gheap;
+    int* err;
+};
+
+__device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
+    if (!(x == 0.0f && y == 0.0f && z == 0.0f)) {
+        float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+        x = __fdiv_rn(x, len);
+        y = __fdiv_rn(y, len);
+        z = __fdiv_rn(z, len);
+    }
+}
+
+// AdaptiveKSearchSurface::distance (AdaptiveKSearchSurface.tcc:414-457) for
+// one query per lane, neighbours summed in ascending (d2, index) order, plus
+// the invalid rule of PointsetGrid::calcDistanceValues (PointsetGrid.tcc:133-140).
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_kernel(SdfArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
+    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
+         tile += gridDim.x * kWarpsPerBlock) {
+        const int qi = tile * 32 + lane;
+        const bool active = qi < A.nq;
+        const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
+        LaneHeap heap;
+        heap.init(ctx.heap, A.K);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        if (active) {
+            heap.sort_ascending();
+            float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
+            int cnt = 0;
+            for (int s = 0; s < A.K; s++) {
+                const unsigned long long key = heap.at(s);
+                if (key == kKeyEmpty) break;
+                const uint32_t j = __ldg(A.T.inv + key_idx(key));
+                const float4 p = __ldg(A.T.pts + j);
+                const float4 nn = __ldg(A.normals + j);
+                px = __fadd_rn(px, p.x); py = __fadd_rn(py, p.y); pz = __fadd_rn(pz, p.z);
+                nx = __fadd_rn(nx, nn.x); ny = __fadd_rn(ny, nn.y); nz = __fadd_rn(nz, nn.z);
+                cnt++;
+            }
+            float proj, eu;
+            if (cnt == 0) {
+                proj = eu = FLT_MAX;
+            } else {
+                const float c = float(cnt);
+                nx = __fdiv_rn(nx, c); ny = __fdiv_rn(ny, c); nz = __fdiv_rn(nz, c);
+                px = __fdiv_rn(px, c); py = __fdiv_rn(py, c); pz = __fdiv_rn(pz, c);
+                normalize_ieee(nx, ny, nz);
+                const float dx = __fsub_rn(q.x, px), dy = __fsub_rn(q.y, py), dz = __fsub_rn(q.z, pz);
+                proj = __fadd_rn(__fadd_rn(__fmul_rn(dx, nx), __fmul_rn(dy, ny)), __fmul_rn(dz, nz));
+                eu = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+            }
+            const uint32_t row = __float_as_uint(q.w);
+            A.dist[row] = proj;
+            if (A.eucl) A.eucl[row] = eu;
+            if (A.invalid) A.invalid[row] = double(eu) > A.limit ? 1 : 0;
+        }
+    }
+}
+
+__global__ void cell_valid_kernel(const uint32_t* __restrict__ corner, int nc, const uint8_t* __restrict__ invalid,
+                                  uint32_t* __restrict__ flags) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 8; k++) ok &= invalid[corner[size_t(c) * 8 + k]] == 0;
+    flags[c] = ok ? 1u : 0u;
+}
+
+// FastBox::calcIntersection (FastBox.tcc:134-158)
+__device__ __forceinline__ float calc_intersection(float x1, float x2, float d1, float d2) {
+    if (d1 == 0.0f) return x1;
+    if (d2 == 0.0f) return x2;
+    if ((d1 < 0.0f && d2 > 0.0f) || (d2 < 0.0f && d1 > 0.0f))
+        return __fsub_rn(x2, __fdiv_rn(__fmul_rn(d2, __fsub_rn(x1, x2)), __fsub_rn(d1, d2)));
+    return 0.0f;
+}
+
+struct McCell {
+    int L[3];       // lattice of corner 0
+    uint32_t rel[3];
+    float d[8];
+    int index;
+};
+
+__device__ __forceinline__ void load_cell(const uint64_t* cell_keys, const uint32_t* corner, const float* qp_dist,
+                                          uint32_t c, const Frame& F, McCell& C) {
+    lattice_decode(cell_keys[c], C.rel[0], C.rel[1], C.rel[2]);
+    C.L[0] = int(C.rel[0]) + F.bx;
+    C.L[1] = int(C.rel[1]) + F.by;
+    C.L[2] = int(C.rel[2]) + F.bz;
+    C.index = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        C.d[k] = qp_dist[corner[size_t(c) * 8 + k]];
+        if (C.d[k] > 0.0f) C.index |= 1 << k;
+    }
+}
+
+// Position and key of cell edge e (low corner -> high corner along its axis).
+__device__ __forceinline__ void edge_vertex(const McCell& C, const Frame& F, int e, float p[3], uint64_t& key) {
+    const int a = c_edge[e][0], b = c_edge[e][1];
+    int axis = 0;
+    if (c_corner[a][1] != c_corner[b][1]) axis = 1;
+    if (c_corner[a][2] != c_corner[b][2]) axis = 2;
+    const int lo = c_corner[a][axis] < c_corner[b][axis] ? a : b;
+    const int hi = lo == a ? b : a;
+#pragma unroll
+    for (int t = 0; t < 3; t++) p[t] = lattice_coord(C.L[t] + c_corner[lo][t], F.vs);
+    const float x2 = lattice_coord(C.L[axis] + 1, F.vs);
+    p[axis] = calc_intersection(p[axis], x2, C.d[lo], C.d[hi]);
+    key = (lattice_key(C.rel[0] + c_corner[lo][0], C.rel[1] + c_corner[lo][1], C.rel[2] + c_corner[lo][2]) << 2) |
+          uint64_t(axis);
+}
+
+__device__ __forceinline__ bool same3(const float* a, const float* b) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
+
+// FastBox::getSurface / BilinearFastBox::getSurface: count (emit == false)
+// or write (emit == true) the faces of one valid cell.
+template <bool kEmit>
+__global__ void mc_kernel(const uint64_t* __restrict__ cell_keys, const uint32_t* __restrict__ corner,
+                          const float* __restrict__ qp_dist, const uint32_t* __restrict__ valid, int nvalid, Frame F,
+                          int pmc, uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
+                          uint64_t* __restrict__ ref_key, uint32_t* __restrict__ ref_val, float4* __restrict__ ref_pos) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nvalid) return;
+    McCell C;
+    load_cell(cell_keys, corner, qp_dist, valid[t], F, C);
+    const unsigned long long word = c_mc[C.index];
+    const int ntri = int(word >> 60);
+    uint32_t f = kEmit ? offsets[t] : 0u;
+    int count = 0;
+    for (int tri = 0; tri < ntri; tri++) {
+        float p[3][3];
+        uint64_t k[3];
+#pragma unroll
+        for (int b = 0; b < 3; b++) edge_vertex(C, F, int((word >> (4 * (3 * tri + b))) & 0xf), p[b], k[b]);
+        if (pmc && (same3(p[0], p[1]) || same3(p[0], p[2]) || same3(p[2], p[1]))) continue;
+        count++;
+        if (kEmit) {
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const size_t r = size_t(f) * 3 + b;
+                ref_key[r] = k[b];
+                ref_val[r] = uint32_t(r);
+                ref_pos[r] = make_float4(p[b][0], p[b][1], p[b][2], 0.0f);
+            }
+            f++;
+        }
+    }
+    if (!kEmit) counts[t] = uint32_t(count);
+}
+
+__global__ void vertex_out_kernel(const uint32_t* __restrict__ first_ref, int nv, const float4* __restrict__ ref_pos,
+                                  float* __restrict__ verts) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    float4 p = ref_pos[first_ref[v]];
+    verts[3 * size_t(v)] = p.x;
+    verts[3 * size_t(v) + 1] = p.y;
+    verts[3 * size_t(v) + 2] = p.z;
+}
+
+template <typename Kernel>
+void set_smem(Kernel k, size_t bytes) {
+    if (bytes > 48 * 1024) LVRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+}
+
+uint64_t read_u64(Workspace& ws, const void* dptr, size_t bytes, cudaStream_t s) {
+    uint64_t* h = ws.pinned();
+    h[0] = 0;
+    LVRGB_CUDA(cudaMemcpyAsync(h, dptr, bytes, cudaMemcpyDeviceToHost, s));
+    LVRGB_CUDA(cudaStreamSynchronize(s));
+    return h[0];
+}
+
+// Sorts keys in place (result pointer returned), removes duplicates and a
+// trailing kNoKey; returns the unique count.
+size_t sort_unique(Workspace& ws, const std::string& tag, uint64_t*& keys, size_t n, int bits, cudaStream_t s) {
+    if (n == 0) return 0;
+    uint64_t* alt = ws.get<uint64_t>(tag + ".alt", n);
+    void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(n));
+    if (radix_sort_pairs<uint64_t>(keys, nullptr, alt, nullptr, n, 0, bits, tmp, s)) std::swap(keys, alt);
+    uint32_t* flags = ws.get<uint32_t>("grid.flags", n);
+    uint32_t* pos = ws.get<uint32_t>("grid.pos", n + 1);
+    head_flags_u64(keys, n, flags, s);
+    void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(n));
+    exclusive_scan_u32(flags, pos, n, stmp, pos + n, s);
+    scatter_flagged_u64(keys, flags, pos, n, alt, s);
+    size_t u = size_t(uint32_t(read_u64(ws, pos + n, sizeof(uint32_t), s)));
+    std::swap(keys, alt);
+    if (u > 0 && read_u64(ws, keys + (u - 1), sizeof(uint64_t), s) == kNoKey) u--;
+    return u;
+}
+
+struct StageTimer {
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool on = false;
+    explicit StageTimer(bool enable) : on(enable) {
+        if (on)
+            for (auto& e : ev) LVRGB_CUDA(cudaEventCreate(&e));
+    }
+    void mark(int i, cudaStream_t s) {
+        if (on) LVRGB_CUDA(cudaEventRecord(ev[i], s));
+    }
+    void finish(GridTimings* t, cudaStream_t s) {
+        if (!on) return;
+        LVRGB_CUDA(cudaStreamSynchronize(s));
+        for (int i = 0; i < 4; i++) LVRGB_CUDA(cudaEventElapsedTime(&t->ms[i], ev[i], ev[i + 1]));
+    }
+    ~StageTimer() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace
+
+void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const float4* qs, int nq, float vs,
+                          float* dist, float* eucl, uint8_t* invalid, Workspace& ws, int* d_err, cudaStream_t s) {
+    if (nq == 0) return;
+    SdfArgs A;
+    A.T = T;
+    A.K = kd > 0 ? kd : 1;
+    A.normals = normals;
+    A.qs = qs;
+    A.nq = nq;
+    A.limit = 1.75 * double(vs);
+    A.dist = dist;
+    A.eucl = eucl;
+    A.invalid = invalid;
+    A.err = d_err;
+    HeapPlan P = plan_heap(nq, A.K, ws);
+    A.gheap = P.gheap;
+    set_smem(sdf_kernel, P.smem);
+    sdf_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], const GridConfig& cfg, Workspace& ws,
+                      GridResult& R, int* d_err, cudaStream_t s, GridTimings* timings) {
+    StageTimer timer(timings != nullptr);
+    timer.mark(0, s);
+    R = GridResult();
+    // HashGrid ctor (HashGrid.tcc:48-52)
+    const float longest = std::max({bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2]});
+    const float vs = cfg.is_voxelsize ? cfg.resolution : longest / cfg.resolution;
+    if (!(vs > 0.0f) || !std::isfinite(vs)) throw std::invalid_argument("voxel size must be positive");
+    R.vs = vs;
+    Frame F;
+    F.vs = vs;
+    int top[3];
+    for (int a = 0; a < 3; a++) {
+        F.lo[a] = bb[a];
+        F.hi[a] = bb[3 + a];
+        const double lo = std::floor(double(bb[a] / vs));
+        const double hi = std::floor(double(bb[3 + a] / vs));
+        if (std::fabs(lo) > 1e9 || std::fabs(hi) > 1e9) throw std::invalid_argument("grid index out of range");
+        R.base[a] = int(lo) - 2;
+        top[a] = int(hi) - R.base[a] + 3;
+    }
+    F.bx = R.base[0]; F.by = R.base[1]; F.bz = R.base[2];
+    int nbits = 1;
+    while ((1 << nbits) <= std::max({top[0], top[1], top[2]}) + 1) nbits++;
+    if (nbits > 20) throw std::invalid_argument("grid extent exceeds 2^20 cells per axis");
+    R.nbits = nbits;
+    const int kbits = 3 * nbits;
+    const int n = T.n;
+
+    // ---- cells of the points, then extrusion (PointsetGrid.tcc:61-106) ----
+    uint64_t* ck = ws.get<uint64_t>("grid.cellsA", size_t(n));
+    point_cells_kernel<<<ceil_div(n, 256), 256, 0, s>>>(T.pts, n, F, ck);
+    LVRGB_LAUNCH_CHECK();
+    size_t nc = sort_unique(ws, "grid.cellsA", ck, size_t(n), kbits, s);
+    if (cfg.extrude && nc > 0) {
+        uint64_t* ek = ws.get<uint64_t>("grid.cellsB", nc * 27);
+        extrude_kernel<<<ceil_div(nc * 27, 256), 256, 0, s>>>(ck, int(nc), F, ek);
+        LVRGB_LAUNCH_CHECK();
+        nc = sort_unique(ws, "grid.cellsB", ek, nc * 27, kbits, s);
+        ck = ek;
+    }
+    R.ncells_all = (long long)nc;
+    R.cell_keys = ck;
+
+    // ---- grid vertices: the 8 corners of every cell, deduplicated --------
+    const size_t ncorner = nc * 8;
+    uint64_t* pk = ws.get<uint64_t>("grid.cornerk", ncorner);
+    uint32_t* pv = ws.get<uint32_t>("grid.cornerv", ncorner);
+    uint64_t* pk2 = ws.get<uint64_t>("grid.cornerk2", ncorner);
+    uint32_t* pv2 = ws.get<uint32_t>("grid.cornerv2", ncorner);
+    uint32_t* cell_corner = ws.get<uint32_t>("grid.cell_corner", ncorner);
+    uint64_t* qk = ws.get<uint64_t>("grid.qp_keys", ncorner);
+    size_t nqp = 0;
+    if (nc > 0) {
+        corner_pairs_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(ck, int(nc), pk, pv);
+        LVRGB_LAUNCH_CHECK();
+        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(ncorner));
+        if (radix_sort_pairs<uint64_t>(pk, pv, pk2, pv2, ncorner, 0, kbits, tmp, s)) {
+            std::swap(pk, pk2);
+            std::swap(pv, pv2);
+        }
+        uint32_t* flags = ws.get<uint32_t>("grid.flags", ncorner);
+        uint32_t* pos = ws.get<uint32_t>("grid.pos", ncorner + 1);
+        head_flags_u64(pk, ncorner, flags, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(ncorner));
+        exclusive_scan_u32(flags, pos, ncorner, stmp, pos + ncorner, s);
+        assign_ids_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(pk, pv, flags, pos, int(ncorner), cell_corner, qk,
+                                                                   nullptr);
+        LVRGB_LAUNCH_CHECK();
+        nqp = size_t(uint32_t(read_u64(ws, pos + ncorner, sizeof(uint32_t), s)));
+    }
+    R.nqp = (long long)nqp;
+    R.qp_keys = qk;
+    R.cell_corner = cell_corner;
+    float4* qpos = ws.get<float4>("grid.qp_pos", nqp);
+    R.qp_pos = qpos;
+    if (nqp) {
+        qp_pos_kernel<<<ceil_div(nqp, 256), 256, 0, s>>>(qk, int(nqp), F, qpos);
+        LVRGB_LAUNCH_CHECK();
+    }
+    timer.mark(1, s);
+
+    // ---- signed distance at every grid vertex (calcDistanceValues) -------
+    R.qp_dist = ws.get<float>("grid.qp_dist", nqp);
+    R.qp_eucl = ws.get<float>("grid.qp_eucl", nqp);
+    R.qp_invalid = ws.get<uint8_t>("grid.qp_invalid", nqp);
+    signed_distance_rows(T, normals, cfg.kd, qpos, int(nqp), vs, R.qp_dist, R.qp_eucl, R.qp_invalid, ws, d_err, s);
+    timer.mark(2, s);
+
+    // ---- remove cells with an invalid corner (PointsetGrid.tcc:153-184) --
+    uint32_t* vflags = ws.get<uint32_t>("grid.vflags", nc);
+    uint32_t* vpos = ws.get<uint32_t>("grid.vpos", nc + 1);
+    uint32_t* valid = ws.get<uint32_t>("grid.valid", nc);
+    size_t nvalid = 0;
+    if (nc) {
+        cell_valid_kernel<<<ceil_div(nc, 256), 256, 0, s>>>(cell_corner, int(nc), R.qp_invalid, vflags);
+        LVRGB_LAUNCH_CHECK();
+        uint32_t* ids = ws.get<uint32_t>("grid.ids", nc);
+        iota_u32(ids, nc, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nc));
+        exclusive_scan_u32(vflags, vpos, nc, stmp, vpos + nc, s);
+        scatter_flagged_u32(ids, vflags, vpos, nc, valid, s);
+        nvalid = size_t(uint32_t(read_u64(ws, vpos + nc, sizeof(uint32_t), s)));
+    }
+    R.ncells_valid = (long long)nvalid;
+    R.valid_cells = valid;
+    timer.mark(3, s);
+
+    // ---- marching cubes: count, scan, emit, deduplicate vertices ---------
+    size_t nf = 0;
+    uint32_t* fcount = ws.get<uint32_t>("mc.count", nvalid);
+    uint32_t* foff = ws.get<uint32_t>("mc.off", nvalid + 1);
+    if (nvalid) {
+        mc_kernel<false><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                               cfg.decomposition == 1, fcount, nullptr, nullptr,
+                                                               nullptr, nullptr);
+        LVRGB_LAUNCH_CHECK();
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nvalid));
+        exclusive_scan_u32(fcount, foff, nvalid, stmp, foff + nvalid, s);
+        nf = size_t(uint32_t(read_u64(ws, foff + nvalid, sizeof(uint32_t), s)));
+    }
+    const size_t nref = nf * 3;
+    uint64_t* rk = ws.get<uint64_t>("mc.rk", nref);
+    uint32_t* rv = ws.get<uint32_t>("mc.rv", nref);
+    uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
+    uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
+    float4* rp = ws.get<float4>("mc.rp", nref);
+    uint32_t* faces = ws.get<uint32_t>("mc.faces", nref);
+    uint64_t* vkeys = ws.get<uint64_t>("mc.vkeys", nref);
+    uint32_t* first = ws.get<uint32_t>("mc.first", nref);
+    size_t nv = 0;
+    if (nf) {
+        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
+        LVRGB_LAUNCH_CHECK();
+        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(nref));
+        if (radix_sort_pairs<uint64_t>(rk, rv, rk2, rv2, nref, 0, kbits + 2, tmp, s)) {
+            std::swap(rk, rk2);
+            std::swap(rv, rv2);
+        }
+        uint32_t* flags = ws.get<uint32_t>("grid.flags", nref);
+        uint32_t* pos = ws.get<uint32_t>("grid.pos", nref + 1);
+        head_flags_u64(rk, nref, flags, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nref));
+        exclusive_scan_u32(flags, pos, nref, stmp, pos + nref, s);
+        assign_ids_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rv, flags, pos, int(nref), faces, vkeys, first);
+        LVRGB_LAUNCH_CHECK();
+        nv = size_t(uint32_t(read_u64(ws, pos + nref, sizeof(uint32_t), s)));
+    }
+    float* verts = ws.get<float>("mc.verts", nv * 3);
+    if (nv) {
+        vertex_out_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(first, int(nv), rp, verts);
+        LVRGB_LAUNCH_CHECK();
+    }
+    timer.mark(4, s);
+    R.nfaces = (long long)nf;
+    R.nverts = (long long)nv;
+    R.faces = faces;
+    R.vert_keys = vkeys;
+    R.verts = verts;
+    timer.finish(timings, s);
+}
+
+}  // namespace lvrgb

@@ -1,0 +1,182 @@
+// lbvh.cu -- LBVH construction: bounding box, 30-bit Morton codes, device
+// radix sort, Karras radix tree over point buckets, bottom-up child boxes.
+#include "lbvh_build.h"
+#include "primitives.cuh"
+
+namespace lvrgb {
+
+namespace {
+
+__global__ void morton_kernel(const float* __restrict__ xyz, int n, const float* __restrict__ box,
+                              uint32_t* __restrict__ codes, uint32_t* __restrict__ idx) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float mnx = box[0], mny = box[1], mnz = box[2];
+    float ext = fmaxf(fmaxf(box[3] - mnx, box[4] - mny), box[5] - mnz);
+    float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    float fx = (xyz[3 * i] - mnx) * scale;
+    float fy = (xyz[3 * i + 1] - mny) * scale;
+    float fz = (xyz[3 * i + 2] - mnz) * scale;
+    uint32_t cx = uint32_t(fminf(fmaxf(fx, 0.0f), 1023.0f));
+    uint32_t cy = uint32_t(fminf(fmaxf(fy, 0.0f), 1023.0f));
+    uint32_t cz = uint32_t(fminf(fmaxf(fz, 0.0f), 1023.0f));
+    codes[i] = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    idx[i] = uint32_t(i);
+}
+
+__global__ void gather_sorted_kernel(const float* __restrict__ xyz, const uint32_t* __restrict__ order, int n,
+                                     float4* __restrict__ pts, uint32_t* __restrict__ inv) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t o = order[j];
+    pts[j] = make_float4(xyz[3 * size_t(o)], xyz[3 * size_t(o) + 1], xyz[3 * size_t(o) + 2], __uint_as_float(o));
+    inv[o] = uint32_t(j);
+}
+
+// Longest common prefix of bucket keys i and j, with the bucket index as
+// tie-break for equal keys (Karras 2012).
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, int bucket, int nb, int i, int j) {
+    if (j < 0 || j >= nb) return -1;
+    uint32_t ki = codes[size_t(i) * bucket], kj = codes[size_t(j) * bucket];
+    if (ki != kj) return __clz(ki ^ kj);
+    return 32 + __clz(uint32_t(i) ^ uint32_t(j));
+}
+
+__global__ void karras_kernel(const uint32_t* __restrict__ codes, int bucket, int nb, TreeNode* __restrict__ nodes,
+                              int* __restrict__ bparent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb - 1) return;
+    const int dir = (delta(codes, bucket, nb, i, i + 1) - delta(codes, bucket, nb, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(codes, bucket, nb, i, i - dir);
+    int lmax = 2;
+    while (delta(codes, bucket, nb, i, i + lmax * dir) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(codes, bucket, nb, i, i + (l + t) * dir) > dmin) l += t;
+    const int j = i + l * dir;
+    const int dnode = delta(codes, bucket, nb, i, j);
+    int s = 0;
+    int div = 2;
+    int t = (l + div - 1) / div;
+    while (true) {
+        if (delta(codes, bucket, nb, i, i + (s + t) * dir) > dnode) s += t;
+        if (t == 1) break;
+        div <<= 1;
+        t = (l + div - 1) / div;
+    }
+    const int gamma = i + s * dir + (dir < 0 ? -1 : 0);
+    const int lo = min(i, j), hi = max(i, j);
+    int left, right;
+    if (lo == gamma) {
+        left = -1 - gamma;
+        bparent[gamma] = (i << 1) | 0;
+    } else {
+        left = gamma;
+        nodes[gamma].d.z = (i << 1) | 0;
+    }
+    if (hi == gamma + 1) {
+        right = -1 - (gamma + 1);
+        bparent[gamma + 1] = (i << 1) | 1;
+    } else {
+        right = gamma + 1;
+        nodes[gamma + 1].d.z = (i << 1) | 1;
+    }
+    nodes[i].d.x = left;
+    nodes[i].d.y = right;
+    if (i == 0) nodes[0].d.z = -1;
+}
+
+__device__ __forceinline__ void write_child_box(TreeNode* nd, int side, const float* lo, const float* hi) {
+    float* f = reinterpret_cast<float*>(nd);
+    const int o = side ? 6 : 0;
+    f[o + 0] = lo[0]; f[o + 1] = lo[1]; f[o + 2] = lo[2];
+    f[o + 3] = hi[0]; f[o + 4] = hi[1]; f[o + 5] = hi[2];
+}
+
+// One warp per bucket: reduce the bucket box, then lane 0 climbs the tree;
+// the second child to arrive at a node merges both boxes and continues.
+__global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket, int nb, TreeNode* nodes,
+                              const int* __restrict__ bparent, int* __restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= nb) return;
+    const int first = b * bucket;
+    int cnt = min(bucket, n - first);
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int j = lane; j < cnt; j += 32) {
+        float4 p = pts[first + j];
+        lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+        hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(kFull, lo[c], o));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(kFull, hi[c], o));
+        }
+    if (lane != 0 || nb == 1) return;
+    int pw = bparent[b];
+    while (pw >= 0) {
+        const int p = pw >> 1, side = pw & 1;
+        TreeNode* nd = nodes + p;
+        write_child_box(nd, side, lo, hi);
+        __threadfence();
+        if (atomicAdd(counters + p, 1) == 0) return;
+        __threadfence();
+        const float* f = reinterpret_cast<const float*>(nd);
+        float o[12];
+#pragma unroll
+        for (int k = 0; k < 12; k++) o[k] = __ldcg(f + k);
+        lo[0] = fminf(o[0], o[6]); lo[1] = fminf(o[1], o[7]); lo[2] = fminf(o[2], o[8]);
+        hi[0] = fmaxf(o[3], o[9]); hi[1] = fmaxf(o[4], o[10]); hi[2] = fmaxf(o[5], o[11]);
+        pw = __ldcg(&nd->d.z);
+    }
+}
+
+}  // namespace
+
+void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::string& tag, Lbvh& T,
+                float* d_box, cudaStream_t s) {
+    if (bucket < 1 || bucket > 32) bucket = 32;
+    T.n = n;
+    T.bucket = bucket;
+    T.nbuckets = n > 0 ? (n + bucket - 1) / bucket : 0;
+    float4* pts = ws.get<float4>(tag + ".pts", size_t(n));
+    uint32_t* inv = ws.get<uint32_t>(tag + ".inv", size_t(n));
+    const int nb = T.nbuckets;
+    TreeNode* nodes = ws.get<TreeNode>(tag + ".nodes", size_t(nb > 1 ? nb - 1 : 1));
+    T.pts = pts;
+    T.inv = inv;
+    T.nodes = nodes;
+    if (n == 0) return;
+
+    void* btmp = ws.get<unsigned char>("lbvh.boxtmp", bbox_temp_bytes(size_t(n)));
+    bbox_float3(xyz, size_t(n), 3, d_box, btmp, s);
+
+    uint32_t* codes = ws.get<uint32_t>("lbvh.codes", size_t(n));
+    uint32_t* codes2 = ws.get<uint32_t>("lbvh.codes2", size_t(n));
+    uint32_t* idx = ws.get<uint32_t>("lbvh.idx", size_t(n));
+    uint32_t* idx2 = ws.get<uint32_t>("lbvh.idx2", size_t(n));
+    morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, d_box, codes, idx);
+    LVRGB_LAUNCH_CHECK();
+    void* stmp = ws.get<unsigned char>("lbvh.sorttmp", radix_sort_temp_bytes<uint32_t>(size_t(n)));
+    bool alt = radix_sort_pairs<uint32_t>(codes, idx, codes2, idx2, size_t(n), 0, 30, stmp, s);
+    const uint32_t* scodes = alt ? codes2 : codes;
+    const uint32_t* sidx = alt ? idx2 : idx;
+    gather_sorted_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, sidx, n, pts, inv);
+    LVRGB_LAUNCH_CHECK();
+
+    int* bparent = ws.get<int>("lbvh.bparent", size_t(nb));
+    if (nb == 1) {
+        LVRGB_CUDA(cudaMemsetAsync(bparent, 0xff, sizeof(int), s));
+        return;
+    }
+    int* counters = ws.get<int>("lbvh.counters", size_t(nb - 1));
+    LVRGB_CUDA(cudaMemsetAsync(counters, 0, sizeof(int) * size_t(nb - 1), s));
+    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(scodes, bucket, nb, nodes, bparent);
+    LVRGB_LAUNCH_CHECK();
+    bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, n, bucket, nb, nodes, bparent, counters);
+    LVRGB_LAUNCH_CHECK();
+}
+
+}  // namespace lvrgb

@@ -1,0 +1,241 @@
+// lbvh.cuh -- linear BVH over Morton-sorted point buckets, and the
+// warp-cooperative k-nearest-neighbour traversal shared by the normal,
+// interpolation, signed-distance and kNN kernels.
+//
+// Layout in HBM
+//   pts    float4[n]      points in Morton order: x, y, z, original index (bits)
+//   inv    uint32[n]      original index -> Morton position
+//   nodes  TreeNode[nb-1] Karras radix tree over the nb = ceil(n / B) buckets
+//                         of B consecutive Morton-ordered points; each node
+//                         holds both children's boxes (one 64-byte fetch per
+//                         visit) and the child links.
+//
+// Traversal: one warp serves 32 consecutive queries.  Child boxes are tested
+// per lane against that lane's current k-th distance; a child is entered when
+// any lane needs it (ballot), so control flow is warp-uniform.  A bucket is
+// loaded once (one coalesced float4 per lane), staged in shared memory and
+// broadcast to all lanes.  The warp's traversal stack is kept in registers,
+// one entry per lane (shuffle to pop).  Each lane keeps its own max-heap of
+// (squared distance, original index) keys.
+#pragma once
+#include "common.cuh"
+
+namespace lvrgb {
+
+struct __align__(16) TreeNode {
+    float4 a;  // child0 lo.x lo.y lo.z hi.x
+    float4 b;  // child0 hi.y hi.z, child1 lo.x lo.y
+    float4 c;  // child1 lo.z hi.x hi.y hi.z
+    int4 d;    // child0, child1 (>= 0 internal node, < 0 bucket -1-b), parent word, unused
+};
+
+struct Lbvh {
+    const float4* pts = nullptr;
+    const uint32_t* inv = nullptr;
+    const TreeNode* nodes = nullptr;
+    int n = 0;
+    int nbuckets = 0;
+    int bucket = 32;
+};
+
+constexpr int kStackMax = 64;  // two register entries per lane
+constexpr int kErrStack = 1;   // traversal stack would overflow (never for depth <= 63)
+
+// Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
+// base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.
+struct LaneHeap {
+    unsigned long long* h;
+    int K;
+    unsigned long long top;
+
+    __device__ __forceinline__ void init(unsigned long long* lane_base, int k) {
+        h = lane_base;
+        K = k;
+        for (int s = 0; s < K; s++) h[s * 32] = kKeyEmpty;
+        top = kKeyEmpty;
+    }
+    __device__ __forceinline__ float tau() const { return key_d2(top); }
+    // Replace the maximum by key (caller guarantees key < top).
+    __device__ __forceinline__ void push(unsigned long long key) {
+        int i = 0;
+        while (true) {
+            int l = 2 * i + 1;
+            if (l >= K) break;
+            unsigned long long cl = h[l * 32];
+            int c = l;
+            if (l + 1 < K) {
+                unsigned long long cr = h[(l + 1) * 32];
+                if (cr > cl) { cl = cr; c = l + 1; }
+            }
+            if (cl <= key) break;
+            h[i * 32] = cl;
+            i = c;
+        }
+        h[i * 32] = key;
+        top = h[0];
+    }
+    __device__ __forceinline__ void offer(float d2, uint32_t idx) {
+        unsigned long long key = make_key(d2, idx);
+        if (key < top) push(key);
+    }
+    // In-place heap sort: afterwards h[0..K) is ascending.
+    __device__ __forceinline__ void sort_ascending() {
+        for (int end = K - 1; end > 0; end--) {
+            unsigned long long mx = h[0];
+            unsigned long long key = h[end * 32];
+            h[end * 32] = mx;
+            int i = 0;
+            while (true) {
+                int l = 2 * i + 1;
+                if (l >= end) break;
+                unsigned long long cl = h[l * 32];
+                int c = l;
+                if (l + 1 < end) {
+                    unsigned long long cr = h[(l + 1) * 32];
+                    if (cr > cl) { cl = cr; c = l + 1; }
+                }
+                if (cl <= key) break;
+                h[i * 32] = cl;
+                i = c;
+            }
+            h[i * 32] = key;
+        }
+    }
+    __device__ __forceinline__ unsigned long long at(int s) const { return h[s * 32]; }
+    __device__ __forceinline__ int count() const {
+        int c = 0;
+        for (int s = 0; s < K; s++) c += (h[s * 32] != kKeyEmpty);
+        return c;
+    }
+};
+
+__device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, float qy, float qz, bool active,
+                                            LaneHeap& heap, float4* stage) {
+    const int lane = threadIdx.x & 31;
+    const int first = b * T.bucket;
+    int cnt = T.n - first;
+    if (cnt > T.bucket) cnt = T.bucket;
+    if (lane < cnt) stage[lane] = __ldg(T.pts + first + lane);
+    __syncwarp();
+    if (active) {
+        for (int j = 0; j < cnt; j++) {
+            float4 c = stage[j];
+            float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+            if (d2 <= heap.tau()) heap.offer(d2, __float_as_uint(c.w));
+        }
+    }
+    __syncwarp();
+}
+
+// k-nearest-neighbour search of one query per lane.  On return each lane's
+// heap holds its K smallest (d2, original index) keys (unordered).
+__device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
+                                             LaneHeap& heap, float4* stage, int* err) {
+    const int lane = threadIdx.x & 31;
+    if (T.nbuckets <= 0) return;
+    if (T.nbuckets == 1) {
+        scan_bucket(T, 0, qx, qy, qz, active, heap, stage);
+        return;
+    }
+    int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
+    int sp = 0;
+    int node = 0;  // root
+    while (true) {
+        // ---- expand an internal node -----------------------------------
+        const TreeNode* nd = T.nodes + node;
+        const float4 a = __ldg(&nd->a);
+        const float4 b = __ldg(&nd->b);
+        const float4 c = __ldg(&nd->c);
+        const int4 d = __ldg(&nd->d);
+        const float tau = heap.tau();
+        const float d0 = box_dist2(qx, qy, qz, a.x, a.y, a.z, a.w, b.x, b.y);
+        const float d1 = box_dist2(qx, qy, qz, b.z, b.w, c.x, c.y, c.z, c.w);
+        const bool n0 = active && d0 <= tau;
+        const bool n1 = active && d1 <= tau;
+        const unsigned m0 = __ballot_sync(kFull, n0);
+        const unsigned m1 = __ballot_sync(kFull, n1);
+        int next;
+        bool have_next = true;
+        if (m0 && m1) {
+            const unsigned p1 = __ballot_sync(kFull, n1 && (!n0 || d1 < d0));
+            const bool first1 = 2 * __popc(p1) > __popc(m0 | m1);
+            next = first1 ? d.y : d.x;
+            const int ref = (node << 1) | (first1 ? 0 : 1);
+            if (sp >= kStackMax) {
+                if (lane == 0) atomicOr(err, kErrStack);
+                return;
+            }
+            if (lane == (sp & 31)) {
+                if (sp < 32) stk0 = ref; else stk1 = ref;
+            }
+            sp++;
+        } else if (m0) {
+            next = d.x;
+        } else if (m1) {
+            next = d.y;
+        } else {
+            have_next = false;
+            next = 0;
+        }
+        // ---- resolve: scan buckets, pop until an internal node to expand --
+        while (true) {
+            if (have_next) {
+                if (next >= 0) {
+                    node = next;
+                    break;
+                }
+                scan_bucket(T, -1 - next, qx, qy, qz, active, heap, stage);
+                have_next = false;
+            }
+            if (sp == 0) return;
+            sp--;
+            const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+            const TreeNode* pn = T.nodes + (ref >> 1);
+            const int side = ref & 1;
+            float lx, ly, lz, hx, hy, hz;
+            int child;
+            if (side == 0) {
+                const float4 pa = __ldg(&pn->a);
+                const float4 pb = __ldg(&pn->b);
+                lx = pa.x; ly = pa.y; lz = pa.z; hx = pa.w; hy = pb.x; hz = pb.y;
+                child = __ldg(&pn->d.x);
+            } else {
+                const float4 pb = __ldg(&pn->b);
+                const float4 pc = __ldg(&pn->c);
+                lx = pb.z; ly = pb.w; lz = pc.x; hx = pc.y; hy = pc.z; hz = pc.w;
+                child = __ldg(&pn->d.y);
+            }
+            const float dd = box_dist2(qx, qy, qz, lx, ly, lz, hx, hy, hz);
+            if (__any_sync(kFull, active && dd <= heap.tau())) {
+                next = child;
+                have_next = true;
+            }
+        }
+    }
+}
+
+// Shared-memory carving of a kNN kernel block: kWarps stage areas of 32
+// float4, then (when gheap == nullptr) kWarps lane-interleaved heaps of K keys.
+// With a global heap buffer, each resident warp owns K*32 keys of it.
+struct WarpCtx {
+    float4* stage;
+    unsigned long long* heap;  // this lane's heap base (stride 32)
+};
+template <int kWarps>
+__device__ __forceinline__ WarpCtx warp_ctx(unsigned char* smem, unsigned long long* gheap, int K) {
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpCtx c;
+    c.stage = reinterpret_cast<float4*>(smem) + wib * 32;
+    if (gheap)
+        c.heap = gheap + (size_t(blockIdx.x) * kWarps + wib) * size_t(K) * 32 + lane;
+    else
+        c.heap = reinterpret_cast<unsigned long long*>(smem + kWarps * 32 * sizeof(float4)) +
+                 size_t(wib) * K * 32 + lane;
+    return c;
+}
+
+__device__ __forceinline__ float4 neighbour_point(const Lbvh& T, unsigned long long key) {
+    return __ldg(T.pts + __ldg(T.inv + key_idx(key)));
+}
+
+}  // namespace lvrgb

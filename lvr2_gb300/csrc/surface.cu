@@ -1,0 +1,648 @@
+// surface.cu -- fused kNN + plane fit + flip (AdaptiveKSearchSurface
+// calculateSurfaceNormals), normal interpolation, kNN rows and
+// getInterpolatedNormal, all on the warp-cooperative LBVH traversal.
+#include <algorithm>
+
+#include "primitives.cuh"
+#include "surface.h"
+
+namespace lvrgb {
+
+namespace {
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+    float y = __fsub_rn(v, c);
+    float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
+// Eigen-style choice among three eigenvalues (first strictly smallest wins,
+// then the second, else the third), as in calcPlaneIPCAExact.
+__device__ __forceinline__ int pick_smallest(double e0, double e1, double e2) {
+    if (e0 < e1 && e0 < e2) return 0;
+    if (e1 < e2) return 1;
+    return 2;
+}
+
+// Cyclic Jacobi eigen-decomposition in double; smallest eigenvector.
+__device__ void jacobi3_smallest(const double Ain[6], double v_out[3]) {
+    double A[3][3] = {{Ain[0], Ain[1], Ain[2]}, {Ain[1], Ain[3], Ain[4]}, {Ain[2], Ain[4], Ain[5]}};
+    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 50; sweep++) {
+        double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        if (off == 0.0) break;
+        for (int p = 0; p < 2; p++)
+            for (int q = p + 1; q < 3; q++) {
+                if (A[p][q] == 0.0) continue;
+                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; k++) {
+                    double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int m = pick_smallest(A[0][0], A[1][1], A[2][2]);
+    double n = sqrt(V[0][m] * V[0][m] + V[1][m] * V[1][m] + V[2][m] * V[2][m]);
+    for (int k = 0; k < 3; k++) v_out[k] = V[k][m] / n;
+}
+
+// Smallest eigenvector of a symmetric 3x3 matrix in FP32 by the closed-form
+// trigonometric eigenvalues (Smith 1961) and a cross product of two rows of
+// (A - lambda I).  Returns false when the result is not trustworthy in FP32
+// (relative eigengap below gap_thr or nearly parallel rows); the caller then
+// solves in FP64.
+__device__ bool eig_smallest_f32(const float A[6], float gap_thr, float v[3]) {
+    const float a00 = A[0], a01 = A[1], a02 = A[2], a11 = A[3], a12 = A[4], a22 = A[5];
+    const float p1 = a01 * a01 + a02 * a02 + a12 * a12;
+    if (p1 == 0.0f) {
+        int m = pick_smallest(a00, a11, a22);
+        v[0] = m == 0; v[1] = m == 1; v[2] = m == 2;
+        return true;
+    }
+    const float q = (a00 + a11 + a22) * (1.0f / 3.0f);
+    const float b00 = a00 - q, b11 = a11 - q, b22 = a22 - q;
+    const float p2 = b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * p1;
+    const float p = sqrtf(p2 * (1.0f / 6.0f));
+    if (!(p > 0.0f)) return false;
+    const float ip = 1.0f / p;
+    const float c00 = b00 * ip, c11 = b11 * ip, c22 = b22 * ip;
+    const float c01 = a01 * ip, c02 = a02 * ip, c12 = a12 * ip;
+    const float det = c00 * (c11 * c22 - c12 * c12) - c01 * (c01 * c22 - c12 * c02) + c02 * (c01 * c12 - c11 * c02);
+    const float r = fminf(fmaxf(0.5f * det, -1.0f), 1.0f);
+    const float phi = acosf(r) * (1.0f / 3.0f);
+    const float l1 = q + 2.0f * p * cosf(phi);
+    const float l3 = q + 2.0f * p * cosf(phi + 2.0943951023931953f);
+    const float l2 = 3.0f * q - l1 - l3;
+    const float scale = fmaxf(fabsf(l1), 1e-30f);
+    if ((l2 - l3) < gap_thr * scale) return false;
+    const float r0[3] = {a00 - l3, a01, a02};
+    const float r1[3] = {a01, a11 - l3, a12};
+    const float r2[3] = {a02, a12, a22 - l3};
+    float x[3][3];
+    x[0][0] = r0[1] * r1[2] - r0[2] * r1[1];
+    x[0][1] = r0[2] * r1[0] - r0[0] * r1[2];
+    x[0][2] = r0[0] * r1[1] - r0[1] * r1[0];
+    x[1][0] = r0[1] * r2[2] - r0[2] * r2[1];
+    x[1][1] = r0[2] * r2[0] - r0[0] * r2[2];
+    x[1][2] = r0[0] * r2[1] - r0[1] * r2[0];
+    x[2][0] = r1[1] * r2[2] - r1[2] * r2[1];
+    x[2][1] = r1[2] * r2[0] - r1[0] * r2[2];
+    x[2][2] = r1[0] * r2[1] - r1[1] * r2[0];
+    float best = -1.0f;
+    int bi = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float nn = x[i][0] * x[i][0] + x[i][1] * x[i][1] + x[i][2] * x[i][2];
+        if (nn > best) { best = nn; bi = i; }
+    }
+    const float rn = fmaxf(fmaxf(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2],
+                                 r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]),
+                           r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+    if (!(best > 1e-10f * rn * rn)) return false;
+    const float inv = rsqrtf(best);
+    v[0] = x[bi][0] * inv;
+    v[1] = x[bi][1] * inv;
+    v[2] = x[bi][2] * inv;
+    return true;
+}
+
+struct NormalsArgs {
+    Lbvh T;
+    int K;
+    int nem;
+    int adaptive;
+    int last_round;
+    int round;  // 1..5
+    const uint32_t* list;
+    int nq;
+    float fx, fy, fz;
+    float gap_thr;
+    float4* normals;
+    int32_t* kused;
+    uint32_t* retry;
+    uint32_t* retry_count;
+    unsigned long long* gheap;
+    int* err;
+    uint32_t* stats;
+};
+
+// BaseVector::normalize with IEEE operations (null vector unchanged).
+__device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
+    if (!(x == 0.0f && y == 0.0f && z == 0.0f)) {
+        float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+        x = __fdiv_rn(x, len);
+        y = __fdiv_rn(y, len);
+        z = __fdiv_rn(z, len);
+    }
+}
+
+template <int kNem>
+__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, float4 q, float n[3],
+                                          bool& fp64) {
+    fp64 = false;
+    if (kNem == 3) {
+        // PCA of {q} and its neighbours (calcPlaneIPCAExact starts its
+        // incremental mean at the query point), centred two-pass covariance in
+        // coordinates relative to q with compensated sums.
+        float sx = 0, sy = 0, sz = 0, cx = 0, cy = 0, cz = 0;
+        int cnt = 0;
+        for (int s = 0; s < A.K; s++) {
+            unsigned long long key = heap.at(s);
+            if (key == kKeyEmpty) continue;
+            float4 p = neighbour_point(A.T, key);
+            kahan_add(sx, cx, p.x - q.x);
+            kahan_add(sy, cy, p.y - q.y);
+            kahan_add(sz, cz, p.z - q.z);
+            cnt++;
+        }
+        const float m = float(cnt + 1);
+        const float mx = sx / m, my = sy / m, mz = sz / m;
+        float S[6] = {mx * mx, mx * my, mx * mz, my * my, my * mz, mz * mz};  // the query point itself
+        float C[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < A.K; s++) {
+            unsigned long long key = heap.at(s);
+            if (key == kKeyEmpty) continue;
+            float4 p = neighbour_point(A.T, key);
+            const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
+            kahan_add(S[0], C[0], ex * ex);
+            kahan_add(S[1], C[1], ex * ey);
+            kahan_add(S[2], C[2], ex * ez);
+            kahan_add(S[3], C[3], ey * ey);
+            kahan_add(S[4], C[4], ey * ez);
+            kahan_add(S[5], C[5], ez * ez);
+        }
+        float v[3];
+        if (eig_smallest_f32(S, A.gap_thr, v)) {
+            n[0] = v[0]; n[1] = v[1]; n[2] = v[2];
+        } else {
+            double D[6], w[3];
+            for (int i = 0; i < 6; i++) D[i] = double(S[i]);
+            jacobi3_smallest(D, w);
+            n[0] = float(w[0]); n[1] = float(w[1]); n[2] = float(w[2]);
+            fp64 = true;
+        }
+    } else if (kNem == 2) {
+        // calcPlaneIterative: sums of (p - q)(p - q)^T and the largest of the
+        // three cofactor determinants.
+        float xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0;
+        for (int s = 0; s < A.K; s++) {
+            unsigned long long key = heap.at(s);
+            if (key == kKeyEmpty) continue;
+            float4 p = neighbour_point(A.T, key);
+            const float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
+            xx = __fadd_rn(xx, __fmul_rn(rx, rx));
+            xy = __fadd_rn(xy, __fmul_rn(rx, ry));
+            xz = __fadd_rn(xz, __fmul_rn(rx, rz));
+            yy = __fadd_rn(yy, __fmul_rn(ry, ry));
+            yz = __fadd_rn(yz, __fmul_rn(ry, rz));
+            zz = __fadd_rn(zz, __fmul_rn(rz, rz));
+        }
+        const float det_x = __fsub_rn(__fmul_rn(yy, zz), __fmul_rn(yz, yz));
+        const float det_y = __fsub_rn(__fmul_rn(xx, zz), __fmul_rn(xz, xz));
+        const float det_z = __fsub_rn(__fmul_rn(xx, yy), __fmul_rn(xy, xy));
+        float dx, dy, dz;
+        if (det_x >= det_y && det_x >= det_z) {
+            dx = 1.0f;
+            dy = __fdiv_rn(__fsub_rn(__fmul_rn(xz, yz), __fmul_rn(xy, zz)), det_x);
+            dz = __fdiv_rn(__fsub_rn(__fmul_rn(xy, yz), __fmul_rn(xz, yy)), det_x);
+        } else if (det_y >= det_x && det_y >= det_z) {
+            dx = __fdiv_rn(__fsub_rn(__fmul_rn(yz, xz), __fmul_rn(xy, zz)), det_y);
+            dy = 1.0f;
+            dz = __fdiv_rn(__fsub_rn(__fmul_rn(xy, xz), __fmul_rn(yz, xx)), det_y);
+        } else {
+            dx = __fdiv_rn(__fsub_rn(__fmul_rn(yz, xy), __fmul_rn(xz, yy)), det_z);
+            dy = __fdiv_rn(__fsub_rn(__fmul_rn(xz, xy), __fmul_rn(yz, xx)), det_z);
+            dz = 1.0f;
+        }
+        const float invnorm = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                                  __fmul_rn(dz, dz))));
+        n[0] = __fmul_rn(dx, invnorm);
+        n[1] = __fmul_rn(dy, invnorm);
+        n[2] = __fmul_rn(dz, invnorm);
+    } else {
+        // calcPlane (nem 0): least-squares y = C0 + C1 x + C2 z over the
+        // neighbours; centred FP32 sums relative to q, 2x2 solve in FP64,
+        // then the reference's two in-plane vectors at +100 offsets.
+        float sx = 0, sy = 0, sz = 0, cx = 0, cy = 0, cz = 0;
+        int cnt = 0;
+        for (int s = 0; s < A.K; s++) {
+            unsigned long long key = heap.at(s);
+            if (key == kKeyEmpty) continue;
+            float4 p = neighbour_point(A.T, key);
+            kahan_add(sx, cx, p.x - q.x);
+            kahan_add(sy, cy, p.y - q.y);
+            kahan_add(sz, cz, p.z - q.z);
+            cnt++;
+        }
+        const float m = float(cnt > 0 ? cnt : 1);
+        const float mx = sx / m, my = sy / m, mz = sz / m;
+        float S[5] = {0, 0, 0, 0, 0}, C[5] = {0, 0, 0, 0, 0};  // xx xz zz xy zy
+        for (int s = 0; s < A.K; s++) {
+            unsigned long long key = heap.at(s);
+            if (key == kKeyEmpty) continue;
+            float4 p = neighbour_point(A.T, key);
+            const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
+            kahan_add(S[0], C[0], ex * ex);
+            kahan_add(S[1], C[1], ex * ez);
+            kahan_add(S[2], C[2], ez * ez);
+            kahan_add(S[3], C[3], ex * ey);
+            kahan_add(S[4], C[4], ez * ey);
+        }
+        const double sxx = S[0], sxz = S[1], szz = S[2], sxy = S[3], szy = S[4];
+        const double det = sxx * szz - sxz * sxz;
+        double c1 = 0, c2 = 0;
+        if (det != 0) {
+            c1 = (sxy * szz - szy * sxz) / det;
+            c2 = (szy * sxx - sxy * sxz) / det;
+        }
+        const double c0 = (double(q.y) + double(my)) - c1 * (double(q.x) + double(mx)) - c2 * (double(q.z) + double(mz));
+        const float C0 = float(c0), C1 = float(c1), C2 = float(c2);
+        const float eps = 100.0f;
+        const float z1 = __fadd_rn(__fadd_rn(C0, __fmul_rn(C1, __fadd_rn(q.x, eps))), __fmul_rn(C2, q.z));
+        const float z2 = __fadd_rn(__fadd_rn(C0, __fmul_rn(C1, q.x)), __fmul_rn(C2, __fadd_rn(q.z, eps)));
+        const float d1x = __fsub_rn(__fadd_rn(q.x, eps), q.x), d1y = __fsub_rn(z1, q.y), d1z = 0.0f;
+        const float d2x = 0.0f, d2y = __fsub_rn(z2, q.y), d2z = __fsub_rn(__fadd_rn(q.z, eps), q.z);
+        float nx = __fsub_rn(__fmul_rn(d1y, d2z), __fmul_rn(d1z, d2y));
+        float ny = __fsub_rn(__fmul_rn(d1z, d2x), __fmul_rn(d1x, d2z));
+        float nz = __fsub_rn(__fmul_rn(d1x, d2y), __fmul_rn(d1y, d2x));
+        normalize_ieee(nx, ny, nz);
+        n[0] = nx; n[1] = ny; n[2] = nz;
+    }
+}
+
+template <int kNem>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
+         tile += gridDim.x * kWarpsPerBlock) {
+        const int qi = tile * 32 + lane;
+        const bool active = qi < A.nq;
+        const int pos = active ? (A.list ? int(A.list[qi]) : qi) : 0;
+        const float4 q = __ldg(A.T.pts + pos);
+        LaneHeap heap;
+        heap.init(ctx.heap, A.K);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        bool retry = false;
+        if (active) {
+            bool fit = true;
+            if (A.adaptive && !A.last_round) {
+                // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
+                float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                for (int s = 0; s < A.K; s++) {
+                    unsigned long long key = heap.at(s);
+                    if (key == kKeyEmpty) continue;
+                    float4 p = neighbour_point(A.T, key);
+                    lo[0] = fminf(p.x, lo[0]); lo[1] = fminf(p.y, lo[1]); lo[2] = fminf(p.z, lo[2]);
+                    hi[0] = fmaxf(p.x, hi[0]); hi[1] = fmaxf(p.y, hi[1]); hi[2] = fmaxf(p.z, hi[2]);
+                }
+                const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
+                const float e = 0.05f;
+                fit = dx >= __fmul_rn(e, dy) && dx >= __fmul_rn(e, dz) && dy >= __fmul_rn(e, dx) &&
+                      dy >= __fmul_rn(e, dz) && dz >= __fmul_rn(e, dx) && dz >= __fmul_rn(e, dy);
+            }
+            if (fit) {
+                float n[3];
+                bool fp64;
+                fit_plane<kNem>(A, heap, q, n, fp64);
+                // Flip toward the flip point; Normal::operator-() re-normalises.
+                const float tx = __fsub_rn(A.fx, q.x), ty = __fsub_rn(A.fy, q.y), tz = __fsub_rn(A.fz, q.z);
+                const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
+                if (dot < 0.0f) {
+                    n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
+                    normalize_ieee(n[0], n[1], n[2]);
+                }
+                A.normals[pos] = make_float4(n[0], n[1], n[2], 0.0f);
+                if (A.kused) A.kused[pos] = A.K;
+                if (fp64) atomicAdd(A.stats + 5, 1u);
+            } else {
+                retry = true;
+            }
+        }
+        const unsigned fitted = __ballot_sync(kFull, active && !retry);
+        const unsigned rm = __ballot_sync(kFull, retry);
+        if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
+        if (rm) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(A.retry_count, uint32_t(__popc(rm)));
+            base = __shfl_sync(kFull, base, 0);
+            if (retry) A.retry[base + __popc(rm & lt)] = uint32_t(pos);
+        }
+    }
+}
+
+struct InterpArgs {
+    Lbvh T;
+    int K;
+    const float4* in;
+    float4* out;
+    unsigned long long* gheap;
+    int* err;
+};
+
+// interpolateSurfaceNormals (AdaptiveKSearchSurface.tcc:293-335)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) interpolate_kernel(InterpArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
+    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.T.n;
+         tile += gridDim.x * kWarpsPerBlock) {
+        const int pos = tile * 32 + lane;
+        const bool active = pos < A.T.n;
+        const float4 q = __ldg(A.T.pts + (active ? pos : 0));
+        LaneHeap heap;
+        heap.init(ctx.heap, A.K);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        if (active) {
+            heap.sort_ascending();
+            float4 m = A.in[pos];
+            float x = m.x, y = m.y, z = m.z;
+            for (int s = 0; s < A.K; s++) {
+                unsigned long long key = heap.at(s);
+                if (key == kKeyEmpty) break;
+                const float4 nj = __ldg(A.in + __ldg(A.T.inv + key_idx(key)));
+                x = __fadd_rn(x, nj.x);
+                y = __fadd_rn(y, nj.y);
+                z = __fadd_rn(z, nj.z);
+            }
+            normalize_ieee(x, y, z);
+            A.out[pos] = make_float4(x, y, z, 0.0f);
+        }
+    }
+}
+
+struct RowsArgs {
+    Lbvh T;
+    int K;
+    const float4* qs;
+    int nq;
+    uint32_t* idx;
+    float* dist;
+    int32_t* count;
+    const float4* normals;  // getInterpolatedNormal mode when non-null
+    float* nout;
+    unsigned long long* gheap;
+    int* err;
+};
+
+__device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, float4 q) {
+        heap.sort_ascending();
+        const size_t row = __float_as_uint(q.w);
+        if (A.normals) {
+            // PointsetSurface::getInterpolatedNormal: accumulator starts as the
+            // default Normal (0, 1, 0); neighbour normals are normalised when
+            // read; the sum is divided by ki and normalised.
+            float x = 0.0f, y = 1.0f, z = 0.0f;
+            for (int s = 0; s < A.K; s++) {
+                unsigned long long key = heap.at(s);
+                if (key == kKeyEmpty) break;
+                float4 nj = __ldg(A.normals + __ldg(A.T.inv + key_idx(key)));
+                float a = nj.x, b = nj.y, c = nj.z;
+                normalize_ieee(a, b, c);
+                x = __fadd_rn(x, a);
+                y = __fadd_rn(y, b);
+                z = __fadd_rn(z, c);
+            }
+            const float kf = float(A.K);
+            x = __fdiv_rn(x, kf);
+            y = __fdiv_rn(y, kf);
+            z = __fdiv_rn(z, kf);
+            normalize_ieee(x, y, z);
+            A.nout[row * 3 + 0] = x;
+            A.nout[row * 3 + 1] = y;
+            A.nout[row * 3 + 2] = z;
+        } else {
+            int c = 0;
+            for (int s = 0; s < A.K; s++) {
+                unsigned long long key = heap.at(s);
+                const bool real = key != kKeyEmpty;
+                c += real;
+                A.idx[row * A.K + s] = real ? key_idx(key) : 0xffffffffu;
+                A.dist[row * A.K + s] = real ? __fsqrt_rn(key_d2(key)) : __int_as_float(0x7f800000);
+            }
+            if (A.count) A.count[row] = c;
+        }
+}
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
+    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
+         tile += gridDim.x * kWarpsPerBlock) {
+        const int qi = tile * 32 + lane;
+        const bool active = qi < A.nq;
+        const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
+        LaneHeap heap;
+        heap.init(ctx.heap, A.K);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        if (active) emit_row(A, heap, q);
+    }
+}
+
+__global__ void query_morton_kernel(const float* __restrict__ q, int nq, const float* __restrict__ box,
+                                    uint32_t* __restrict__ codes, uint32_t* __restrict__ idx) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const float mnx = box[0], mny = box[1], mnz = box[2];
+    float ext = fmaxf(fmaxf(box[3] - mnx, box[4] - mny), box[5] - mnz);
+    float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    uint32_t cx = uint32_t(fminf(fmaxf((q[3 * i] - mnx) * scale, 0.0f), 1023.0f));
+    uint32_t cy = uint32_t(fminf(fmaxf((q[3 * i + 1] - mny) * scale, 0.0f), 1023.0f));
+    uint32_t cz = uint32_t(fminf(fmaxf((q[3 * i + 2] - mnz) * scale, 0.0f), 1023.0f));
+    codes[i] = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    idx[i] = uint32_t(i);
+}
+
+__global__ void query_gather_kernel(const float* __restrict__ q, const uint32_t* __restrict__ order, int nq,
+                                    float4* __restrict__ qs) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nq) return;
+    uint32_t o = order[j];
+    qs[j] = make_float4(q[3 * size_t(o)], q[3 * size_t(o) + 1], q[3 * size_t(o) + 2], __uint_as_float(o));
+}
+
+int g_num_sms = 0;
+
+template <typename Kernel>
+void set_smem(Kernel k, size_t bytes) {
+    if (bytes > 48 * 1024) LVRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+}
+
+}  // namespace
+
+HeapPlan plan_heap(int nq, int K, Workspace& ws) {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        LVRGB_CUDA(cudaGetDevice(&dev));
+        LVRGB_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    HeapPlan p;
+    const int tiles = (nq + 31) / 32;
+    const int need_blocks = std::max(1, (tiles + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    const size_t stage = size_t(kWarpsPerBlock) * 32 * sizeof(float4);
+    if (K <= kSmemHeapMax) {
+        p.smem = stage + size_t(kWarpsPerBlock) * K * 32 * sizeof(unsigned long long);
+        p.blocks = need_blocks;
+        p.gheap = nullptr;
+    } else {
+        p.smem = stage;
+        p.blocks = std::min(need_blocks, g_num_sms * 2);
+        p.gheap = ws.get<unsigned long long>("knn.gheap", size_t(p.blocks) * kWarpsPerBlock * K * 32);
+    }
+    return p;
+}
+
+void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
+                     int* d_err, uint32_t* d_stats, cudaStream_t s) {
+    const int n = T.n;
+    if (n == 0) return;
+    uint32_t* lists[2] = {ws.get<uint32_t>("normals.listA", size_t(n)), ws.get<uint32_t>("normals.listB", size_t(n))};
+    uint32_t* counter = ws.get<uint32_t>("normals.counter", 2);
+    uint64_t* h_count = ws.pinned();
+    int nq = n;
+    const uint32_t* list = nullptr;
+    size_t k = size_t(cfg.kn);
+    for (int round = 1; round <= 5 && nq > 0; round++) {
+        k *= 2;  // the reference doubles k before every search
+        const int K = int(std::min<size_t>(k, size_t(1) << 20));
+        const int last = (!cfg.adaptive || round == 5) ? 1 : 0;
+        uint32_t* retry = lists[round & 1];
+        LVRGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), s));
+        NormalsArgs A;
+        A.T = T;
+        A.K = K;
+        A.nem = cfg.nem;
+        A.adaptive = cfg.adaptive;
+        A.last_round = last;
+        A.round = round;
+        A.list = list;
+        A.nq = nq;
+        A.fx = cfg.flip[0]; A.fy = cfg.flip[1]; A.fz = cfg.flip[2];
+        A.gap_thr = cfg.gap_threshold;
+        A.normals = normals;
+        A.kused = kused;
+        A.retry = retry;
+        A.retry_count = counter;
+        A.err = d_err;
+        A.stats = d_stats;
+        HeapPlan P = plan_heap(nq, K, ws);
+        A.gheap = P.gheap;
+        const int threads = kWarpsPerBlock * 32;
+        switch (cfg.nem) {
+            case 2:
+                set_smem(normals_kernel<2>, P.smem);
+                normals_kernel<2><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+            case 3:
+                set_smem(normals_kernel<3>, P.smem);
+                normals_kernel<3><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+            default:
+                set_smem(normals_kernel<0>, P.smem);
+                normals_kernel<0><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+        }
+        LVRGB_LAUNCH_CHECK();
+        if (last) break;
+        h_count[0] = 0;
+        LVRGB_CUDA(cudaMemcpyAsync(h_count, counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        LVRGB_CUDA(cudaStreamSynchronize(s));
+        nq = int(uint32_t(h_count[0]));
+        list = retry;
+    }
+}
+
+void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,
+                         cudaStream_t s) {
+    if (T.n == 0) return;
+    if (ki <= 0) {
+        LVRGB_CUDA(cudaMemcpyAsync(out, in, sizeof(float4) * size_t(T.n), cudaMemcpyDeviceToDevice, s));
+        return;
+    }
+    InterpArgs A;
+    A.T = T;
+    A.K = ki;
+    A.in = in;
+    A.out = out;
+    A.err = d_err;
+    HeapPlan P = plan_heap(T.n, ki, ws);
+    A.gheap = P.gheap;
+    set_smem(interpolate_kernel, P.smem);
+    interpolate_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Workspace& ws, cudaStream_t s) {
+    if (nq == 0) return;
+    uint32_t* codes = ws.get<uint32_t>("q.codes", size_t(nq));
+    uint32_t* codes2 = ws.get<uint32_t>("q.codes2", size_t(nq));
+    uint32_t* idx = ws.get<uint32_t>("q.idx", size_t(nq));
+    uint32_t* idx2 = ws.get<uint32_t>("q.idx2", size_t(nq));
+    query_morton_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(q, nq, d_box, codes, idx);
+    LVRGB_LAUNCH_CHECK();
+    void* tmp = ws.get<unsigned char>("q.sorttmp", radix_sort_temp_bytes<uint32_t>(size_t(nq)));
+    bool alt = radix_sort_pairs<uint32_t>(codes, idx, codes2, idx2, size_t(nq), 0, 30, tmp, s);
+    query_gather_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(q, alt ? idx2 : idx, nq, qs);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
+              Workspace& ws, int* d_err, cudaStream_t s) {
+    if (nq == 0 || k <= 0) return;
+    RowsArgs A;
+    A.T = T;
+    A.K = k;
+    A.qs = qs;
+    A.nq = nq;
+    A.idx = idx;
+    A.dist = dist;
+    A.count = count;
+    A.normals = nullptr;
+    A.nout = nullptr;
+    A.err = d_err;
+    HeapPlan P = plan_heap(nq, k, ws);
+    A.gheap = P.gheap;
+    set_smem(rows_kernel, P.smem);
+    rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, const float4* qs, int nq, float* out,
+                              Workspace& ws, int* d_err, cudaStream_t s) {
+    if (nq == 0 || ki <= 0) return;
+    RowsArgs A;
+    A.T = T;
+    A.K = ki;
+    A.qs = qs;
+    A.nq = nq;
+    A.idx = nullptr;
+    A.dist = nullptr;
+    A.count = nullptr;
+    A.normals = normals;
+    A.nout = out;
+    A.err = d_err;
+    HeapPlan P = plan_heap(nq, ki, ws);
+    A.gheap = P.gheap;
+    set_smem(rows_kernel, P.smem);
+    rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+}  // namespace lvrgb

@@ -1,0 +1,54 @@
+// surface.h -- host launchers of the point-surface kernels (surface.cu).
+#pragma once
+#include "lbvh.cuh"
+#include "workspace.h"
+
+namespace lvrgb {
+
+struct NormalsConfig {
+    int kn = 10;          // AdaptiveKSearchSurface kn
+    int nem = 0;          // 0 LSQ plane, 2 iterative, 3 PCA (IPCA exact)
+    int adaptive = 1;     // k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed
+    float flip[3] = {0, 0, 0};
+    float gap_threshold = 1e-3f;  // relative eigengap below which the eigensolve runs in FP64
+};
+
+// Device counters written by compute_normals (uint32[8]):
+//   [0..4] number of points whose plane was fitted in search round 1..5,
+//   [5]    number of PCA eigensolves that fell back to FP64.
+constexpr int kNormalStats = 8;
+
+// Normals in Morton order (float4, w = 0).  kused (optional, Morton order)
+// receives the k of the search whose neighbourhood was used.
+void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
+                     int* d_err, uint32_t* d_stats, cudaStream_t s);
+
+// out_i = normalize(in_i + sum_{j in kNN_ki(p_i)} in_j), Morton order.
+void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,
+                         cudaStream_t s);
+
+// Sorts nq AoS query points into Morton order relative to the tree's box.
+// qs[i] = (x, y, z, row index bits).  d_box: 6 floats (min, max).
+void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Workspace& ws, cudaStream_t s);
+
+// k nearest neighbours for sorted queries; rows (by qs[i].w) of idx (original
+// indices, 0xffffffff padding) and dist (sqrt of d2, +inf padding), ascending.
+void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
+              Workspace& ws, int* d_err, cudaStream_t s);
+
+// PointsetSurface::getInterpolatedNormal for sorted queries; out rows float3.
+void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, const float4* qs, int nq,
+                              float* out, Workspace& ws, int* d_err, cudaStream_t s);
+
+// Common launch plan for the per-lane heaps: heaps of up to kSmemHeapMax
+// entries live in shared memory, larger ones in a global scratch buffer.
+constexpr int kWarpsPerBlock = 4;
+constexpr int kSmemHeapMax = 96;
+struct HeapPlan {
+    int blocks = 0;
+    size_t smem = 0;
+    unsigned long long* gheap = nullptr;
+};
+HeapPlan plan_heap(int nq, int K, Workspace& ws);
+
+}  // namespace lvrgb

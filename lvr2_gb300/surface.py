@@ -1,0 +1,252 @@
+"""Python mirror of the lvr2 surface interface over liblvrgb.so.
+
+`Surface` follows AdaptiveKSearchSurface / PointsetSurface
+(include/lvr2/reconstruction/AdaptiveKSearchSurface.hpp:99-107,
+PointsetSurface.hpp:61-166) and CudaSurface
+(include/lvr2/reconstruction/cuda/CudaSurface.hpp:70-158): same parameter
+names and defaults, same call order (construct, setKn/Ki/Kd, setFlipPoint,
+calculateSurfaceNormals, distance, reconstruction).  Arrays are numpy
+float32 (N, 3) on the host, or torch CUDA tensors (device path, pointers are
+passed straight to the library).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GridConfig, LvrgbError, MeshInfo, SurfaceConfig, check
+
+
+def _is_torch_cuda(a):
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch_cuda(a):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f32x3(a):
+    if _is_torch_cuda(a):
+        if a.dtype != __import__("torch").float32 or not a.is_contiguous() or a.dim() != 2 or a.shape[1] != 3:
+            raise ValueError("device points must be a contiguous float32 (N, 3) CUDA tensor")
+        return a, 1
+    arr = np.ascontiguousarray(a, dtype=np.float32)
+    if arr.ndim != 2 or arr.shape[1] != 3:
+        arr = arr.reshape(-1, 3)
+    return arr, 0
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+class Surface:
+    """A point cloud on the GPU with its LBVH, normals and signed distance.
+
+    Surface(points, kn=10, ki=10, kd=5, nem=0, flip_point=(0,0,0)) matches the
+    way lvr2_reconstruct sets up AdaptiveKSearchSurface (Main.cpp:283-349);
+    flip_point=None keeps AdaptiveKSearchSurface's own default, the bounding
+    box centroid.
+    """
+
+    def __init__(self, points, kn=10, ki=10, kd=5, nem=0, adaptive=True, flip_point=(0.0, 0.0, 0.0),
+                 bucket=32, gap_threshold=1e-3, device=0, stream=None):
+        L = _lib.load()
+        cfg = SurfaceConfig()
+        L.lvrgb_surface_config_default(ctypes.byref(cfg))
+        cfg.kn, cfg.ki, cfg.kd, cfg.nem = int(kn), int(ki), int(kd), int(nem)
+        cfg.adaptive = int(bool(adaptive))
+        if flip_point is None:
+            cfg.flip_set = 0
+        else:
+            cfg.flip_set = 1
+            cfg.flip[0], cfg.flip[1], cfg.flip[2] = (float(v) for v in flip_point)
+        cfg.bucket = int(bucket)
+        cfg.gap_threshold = float(gap_threshold)
+        cfg.device = int(device)
+        pts, on_dev = _f32x3(points)
+        self._h = ctypes.c_void_p()
+        self._stream = _stream_ptr(stream)
+        check(L.lvrgb_surface_create(ctypes.byref(cfg), _ptr(pts), len(pts), on_dev, self._stream,
+                                     ctypes.byref(self._h)))
+        self.n = int(len(pts))
+        self.kn, self.ki, self.kd = int(kn), int(ki), int(kd)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().lvrgb_surface_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_points(self, points):
+        """Replaces the points (rebuilds the LBVH in the handle's memory)."""
+        pts, on_dev = _f32x3(points)
+        check(_lib.load().lvrgb_surface_set_points(self._h, _ptr(pts), len(pts), on_dev, self._stream))
+        self.n = int(len(pts))
+
+    def timings(self):
+        """Device ms of the last calls: build, normals, interpolation, grid,
+        signed distance, culling, marching cubes."""
+        out = np.zeros(8, np.float32)
+        check(_lib.load().lvrgb_surface_timings(self._h, _ptr(out)))
+        return out[:7]
+
+    # ---- parameters (PointsetSurface::setKn/setKi/setKd/setFlipPoint) ------
+    def set_k(self, kn=-1, ki=-1, kd=-1):
+        check(_lib.load().lvrgb_surface_set_k(self._h, kn, ki, kd))
+        if kn > 0:
+            self.kn = kn
+        if ki >= 0:
+            self.ki = ki
+        if kd > 0:
+            self.kd = kd
+
+    def set_flip_point(self, x, y, z):
+        check(_lib.load().lvrgb_surface_set_flip_point(self._h, x, y, z))
+
+    def set_method(self, nem):
+        check(_lib.load().lvrgb_surface_set_method(self._h, nem))
+
+    def bounding_box(self):
+        out = np.zeros(9, np.float32)
+        check(_lib.load().lvrgb_surface_bounding_box(self._h, _ptr(out)))
+        return out[:3], out[3:6], out[6:]
+
+    # ---- normals -------------------------------------------------------------
+    def calculate_normals(self):
+        check(_lib.load().lvrgb_calculate_normals(self._h, self._stream))
+
+    def interpolate_normals(self):
+        check(_lib.load().lvrgb_interpolate_normals(self._h, self._stream))
+
+    def normals(self, out=None):
+        if out is not None and _is_torch_cuda(out):
+            check(_lib.load().lvrgb_get_normals(self._h, _ptr(out), 1, self._stream))
+            return out
+        res = np.empty((self.n, 3), np.float32)
+        check(_lib.load().lvrgb_get_normals(self._h, _ptr(res), 0, self._stream))
+        return res
+
+    def raw_normals(self):
+        res = np.empty((self.n, 3), np.float32)
+        k = np.empty(self.n, np.int32)
+        check(_lib.load().lvrgb_get_raw_normals(self._h, _ptr(res), _ptr(k), 0, self._stream))
+        return res, k
+
+    def set_normals(self, normals):
+        arr, on_dev = _f32x3(normals)
+        check(_lib.load().lvrgb_set_normals(self._h, _ptr(arr), on_dev, self._stream))
+
+    def normal_stats(self):
+        out = np.zeros(8, np.uint32)
+        check(_lib.load().lvrgb_normal_stats(self._h, _ptr(out)))
+        return out
+
+    # ---- queries -------------------------------------------------------------
+    def knn(self, queries, k):
+        q, on_dev = _f32x3(queries)
+        if on_dev:
+            import torch
+            idx = torch.empty((len(q), k), dtype=torch.int32, device=q.device)
+            dist = torch.empty((len(q), k), dtype=torch.float32, device=q.device)
+            cnt = torch.empty(len(q), dtype=torch.int32, device=q.device)
+        else:
+            idx = np.empty((len(q), k), np.uint32)
+            dist = np.empty((len(q), k), np.float32)
+            cnt = np.empty(len(q), np.int32)
+        check(_lib.load().lvrgb_knn(self._h, _ptr(q), len(q), int(k), _ptr(idx), _ptr(dist), _ptr(cnt), on_dev,
+                                    self._stream))
+        return idx, dist, cnt
+
+    def distance(self, queries):
+        q, on_dev = _f32x3(queries)
+        proj = np.empty(len(q), np.float32)
+        eucl = np.empty(len(q), np.float32)
+        if on_dev:
+            raise ValueError("use host arrays with distance()")
+        check(_lib.load().lvrgb_distance(self._h, _ptr(q), len(q), _ptr(proj), _ptr(eucl), 0, self._stream))
+        return proj, eucl
+
+    def grid_distances(self, queries, voxel_size):
+        q, on_dev = _f32x3(queries)
+        if on_dev:
+            raise ValueError("use host arrays with grid_distances()")
+        dist = np.empty(len(q), np.float32)
+        inv = np.empty(len(q), np.uint8)
+        check(_lib.load().lvrgb_grid_distances(self._h, _ptr(q), len(q), float(voxel_size), _ptr(dist), _ptr(inv),
+                                               0, self._stream))
+        return dist, inv
+
+    def interpolated_normal(self, queries):
+        q, on_dev = _f32x3(queries)
+        if on_dev:
+            raise ValueError("use host arrays with interpolated_normal()")
+        out = np.empty((len(q), 3), np.float32)
+        check(_lib.load().lvrgb_interpolated_normal(self._h, _ptr(q), len(q), _ptr(out), 0, self._stream))
+        return out
+
+    # ---- grid + marching cubes ---------------------------------------------------
+    def reconstruct(self, voxelsize=10.0, intersections=-1, extrude=True, decomposition="PMC"):
+        g = GridConfig()
+        if intersections is not None and intersections > 0:
+            g.resolution, g.is_voxelsize = float(intersections), 0
+        else:
+            g.resolution, g.is_voxelsize = float(voxelsize), 1
+        g.extrude = int(bool(extrude))
+        g.decomposition = {"MC": 0, "PMC": 1}[decomposition]
+        info = MeshInfo()
+        check(_lib.load().lvrgb_reconstruct(self._h, ctypes.byref(g), ctypes.byref(info), self._stream))
+        self.info = info
+        return info
+
+    def mesh(self, with_edges=True):
+        info = self.info
+        v = np.empty((info.vertices, 3), np.float32)
+        f = np.empty((info.faces, 3), np.uint32)
+        e = np.empty((info.vertices, 4), np.int32) if with_edges else None
+        check(_lib.load().lvrgb_get_mesh(self._h, _ptr(v), _ptr(f), _ptr(e), 0, self._stream))
+        return v, f, e
+
+    def grid(self):
+        nq = self.info.grid_vertices
+        lat = np.empty((nq, 3), np.int32)
+        pos = np.empty((nq, 3), np.float32)
+        dist = np.empty(nq, np.float32)
+        inv = np.empty(nq, np.uint8)
+        check(_lib.load().lvrgb_get_grid(self._h, _ptr(lat), _ptr(pos), _ptr(dist), _ptr(inv), 0, self._stream))
+        return lat, pos, dist, inv
+
+    def cells(self):
+        a = np.empty((self.info.cells_all, 3), np.int32)
+        v = np.empty((self.info.cells_valid, 3), np.int32)
+        check(_lib.load().lvrgb_get_cells(self._h, _ptr(a), _ptr(v), 0, self._stream))
+        return a, v
+
+
+def kernel_launches():
+    """Kernels launched by liblvrgb.so in this process."""
+    out = np.zeros(1, np.uint64)
+    check(_lib.load().lvrgb_kernel_launches(_ptr(out)))
+    return int(out[0])
+
+
+__all__ = ["Surface", "LvrgbError", "kernel_launches"]

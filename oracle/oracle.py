@@ -1,0 +1,195 @@
+"""ctypes wrapper of the CPU oracle (oracle/lvr_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker, and by bench.py for the CPU baseline / reference arm.  The
+product path (lvr2_gb300) never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liblvroracle.so"
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+
+_lib = None
+
+
+def build(quiet=True):
+    """Compile the oracle with its Makefile (g++, OpenMP)."""
+    out = subprocess.run(["make", "-C", str(HERE)], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        build()
+    L = ctypes.CDLL(str(LIB_PATH))
+    L.orc_create.restype = _vp
+    L.orc_create.argtypes = [_f32p, _i64, _int, _int]
+    L.orc_destroy.argtypes = [_vp]
+    L.orc_bbox.argtypes = [_vp, _f32p]
+    L.orc_knn.argtypes = [_vp, _f32p, _i64, _int, _int, _u32p, _f32p, _i32p, _int]
+    L.orc_normals.argtypes = [_vp, _int, _int, _int, ctypes.c_void_p, _int, _f32p, ctypes.c_void_p, _int]
+    L.orc_interpolate.argtypes = [_vp, _int, _f32p, _f32p, _int, _int]
+    L.orc_distance.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _f32p, _int]
+    L.orc_interpolated_normal.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _int]
+    L.orc_reconstruct.restype = _vp
+    L.orc_reconstruct.argtypes = [_vp, _f32p, ctypes.c_float, _int, _int, _int, _int, _int,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _i64, _int]
+    L.orc_recon_destroy.argtypes = [_vp]
+    L.orc_recon_counts.argtypes = [_vp, _i64p, _f32p]
+    L.orc_recon_grid.argtypes = [_vp, _i32p, _f32p, _f32p, _u8p]
+    L.orc_recon_cells.argtypes = [_vp, _i32p, _i32p]
+    L.orc_recon_mesh.argtypes = [_vp, _i32p, _f32p, _i32p]
+    L.orc_mc_table.argtypes = [_i32p]
+    _lib = L
+    return L
+
+
+def _pts(a):
+    return np.ascontiguousarray(a, dtype=np.float32).reshape(-1, 3)
+
+
+class OracleSurface:
+    """The reference CPU surface: SearchKDTree + AdaptiveKSearchSurface."""
+
+    def __init__(self, points, leaf_size=20, threads=0):
+        self.points = _pts(points)
+        self.threads = threads
+        self._h = lib().orc_create(self.points.reshape(-1), len(self.points), leaf_size, threads)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    @property
+    def n(self):
+        return len(self.points)
+
+    def bbox(self):
+        out = np.zeros(9, np.float32)
+        lib().orc_bbox(self._h, out)
+        return out[0:3], out[3:6], out[6:9]
+
+    def knn(self, queries, k, canonical=True):
+        q = _pts(queries)
+        idx = np.empty((len(q), k), np.uint32)
+        dist = np.empty((len(q), k), np.float32)
+        cnt = np.empty(len(q), np.int32)
+        lib().orc_knn(self._h, q.reshape(-1), len(q), k, int(canonical), idx, dist, cnt, self.threads)
+        return idx, dist, cnt
+
+    def normals(self, kn, nem=3, adaptive=True, flip=None, canonical=True, with_k=False):
+        out = np.empty((self.n, 3), np.float32)
+        kused = np.empty(self.n, np.int32) if with_k else None
+        fl = None
+        if flip is not None:
+            fl_arr = np.ascontiguousarray(flip, np.float32)
+            fl = fl_arr.ctypes.data_as(ctypes.c_void_p)
+        rc = lib().orc_normals(self._h, kn, nem, int(adaptive), fl, int(canonical), out,
+                               kused.ctypes.data_as(ctypes.c_void_p) if with_k else None, self.threads)
+        if rc != 0:
+            raise ValueError("oracle normals: unsupported nem %d" % nem)
+        return (out, kused) if with_k else out
+
+    def interpolate(self, normals, ki, canonical=True):
+        nin = _pts(normals)
+        out = np.empty_like(nin)
+        lib().orc_interpolate(self._h, ki, nin.reshape(-1), out, int(canonical), self.threads)
+        return out
+
+    def distance(self, normals, kd, queries, canonical=True):
+        nrm = _pts(normals)
+        q = _pts(queries)
+        proj = np.empty(len(q), np.float32)
+        eucl = np.empty(len(q), np.float32)
+        lib().orc_distance(self._h, nrm.reshape(-1), kd, q.reshape(-1), len(q), int(canonical),
+                           proj, eucl, self.threads)
+        return proj, eucl
+
+    def interpolated_normal(self, normals, ki, queries, canonical=True):
+        nrm = _pts(normals)
+        q = _pts(queries)
+        out = np.empty((len(q), 3), np.float32)
+        lib().orc_interpolated_normal(self._h, nrm.reshape(-1), ki, q.reshape(-1), len(q),
+                                      int(canonical), out, self.threads)
+        return out
+
+    def reconstruct(self, normals, voxelsize=None, intersections=None, extrude=True, kd=5,
+                    decomposition="PMC", canonical=True, grid_override=None):
+        """PointsetGrid + calcDistanceValues + marching cubes.  Returns a dict."""
+        nrm = _pts(normals)
+        if intersections is not None and intersections > 0:
+            res, isvs = float(intersections), 0
+        else:
+            res, isvs = float(voxelsize), 1
+        dec = {"MC": 0, "PMC": 1}[decomposition]
+        args = [None, None, None, 0]
+        keep = None
+        if grid_override is not None:
+            lat, dist, inv = grid_override
+            keep = (np.ascontiguousarray(lat, np.int32), np.ascontiguousarray(dist, np.float32),
+                    np.ascontiguousarray(inv, np.uint8))
+            args = [keep[0].ctypes.data_as(ctypes.c_void_p), keep[1].ctypes.data_as(ctypes.c_void_p),
+                    keep[2].ctypes.data_as(ctypes.c_void_p), len(keep[1])]
+        L = lib()
+        h = L.orc_reconstruct(self._h, nrm.reshape(-1), res, isvs, int(extrude), kd, dec,
+                              int(canonical), *args, self.threads)
+        try:
+            c = np.zeros(8, np.int64)
+            f = np.zeros(4, np.float32)
+            L.orc_recon_counts(h, c, f)
+            ncell, nqp, nvalid, nv, nf = (int(x) for x in c[:5])
+            lat = np.empty((nqp, 3), np.int32)
+            pos = np.empty((nqp, 3), np.float32)
+            dist = np.empty(nqp, np.float32)
+            inv = np.empty(nqp, np.uint8)
+            L.orc_recon_grid(h, lat, pos, dist, inv)
+            cells_all = np.empty((ncell, 3), np.int32)
+            cells_valid = np.empty((nvalid, 3), np.int32)
+            L.orc_recon_cells(h, cells_all, cells_valid)
+            vkeys = np.empty((nv, 4), np.int32)
+            vpos = np.empty((nv, 3), np.float32)
+            faces = np.empty((nf, 3), np.int32)
+            L.orc_recon_mesh(h, vkeys, vpos, faces)
+        finally:
+            L.orc_recon_destroy(h)
+        return dict(voxelsize=float(f[0]), cells_all=cells_all, cells_valid=cells_valid,
+                    qp_lattice=lat, qp_pos=pos, qp_dist=dist, qp_invalid=inv,
+                    vkeys=vkeys, vpos=vpos, faces=faces)
+
+
+def mc_table():
+    out = np.empty((256, 13), np.int32)
+    lib().orc_mc_table(out)
+    return out
+
+
+def reference_tables():
+    """Tables printed by oracle/_ref/ref_tables (compiled from the lvr2 headers),
+    or None when that binary has not been built (no lvr2 tree present)."""
+    import json
+    exe = HERE / "_ref" / "ref_tables"
+    if not exe.exists():
+        return None
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True)
+    return json.loads(out.stdout)

@@ -1,0 +1,262 @@
+"""GPU parity: every stage of the CUDA path against the CPU oracle, through
+the C ABI (lvr2_gb300.Surface -> liblvrgb.so).
+
+Bars (stated per test): kNN index rows and distances bit-exact; adaptive-k
+round per point identical; normals within 0.5 degrees at the 99.9th
+percentile of the oracle and of float64 PCA, sign-consistent; interpolation,
+signed distance, grid and marching-cubes results bit-exact when fed the same
+inputs as the oracle.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tests.helpers import angle_deg, canonical_mesh, fp64_pca_normals
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLD = np.load(ROOT / "tests/golden/oracle_small.npz")
+ANGLE_P999_DEG = 0.5
+
+
+@pytest.fixture(scope="module")
+def gb(lib):
+    import lvr2_gb300
+    return lvr2_gb300
+
+
+def clouds():
+    rng = np.random.Generator(np.random.PCG64(21))
+    out = {}
+    out["uniform"] = rng.uniform(-1, 1, (50_000, 3)).astype(np.float32)
+    g = np.stack(np.meshgrid(*[np.arange(24)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    out["lattice"] = (g * 0.125).astype(np.float32)
+    base = rng.uniform(0, 1, (20_000, 3)).astype(np.float32)
+    out["duplicates"] = np.concatenate([base, base[:5000], base[:1000]])
+    from lvr2_gb300 import synthetic
+    out["spheres"] = synthetic.spheres_tori(60_000, seed=2)
+    out["scan"] = synthetic.scan_scene(40_000, seed=9)[0]
+    return out
+
+
+CLOUDS = None
+
+
+def cloud(name):
+    global CLOUDS
+    if CLOUDS is None:
+        CLOUDS = clouds()
+    return CLOUDS[name]
+
+
+@pytest.mark.parametrize("name", ["uniform", "lattice", "duplicates", "spheres", "scan"])
+@pytest.mark.parametrize("bucket", [32, 8])
+def test_knn_bit_exact(gb, oracle_mod, name, bucket):
+    P = cloud(name)
+    rng = np.random.Generator(np.random.PCG64(3))
+    lo, hi = P.min(0), P.max(0)
+    Q = np.concatenate([P[::17], rng.uniform(lo - 0.2 * (hi - lo), hi + 0.2 * (hi - lo), (500, 3)).astype(np.float32)])
+    o = oracle_mod.OracleSurface(P, threads=0)
+    with gb.Surface(P, bucket=bucket) as s:
+        for k in (1, 10, 40, 150):
+            gi, gd, gc = s.knn(Q, k)
+            oi, od, oc = o.knn(Q, k)
+            assert (gc == oc).all()
+            assert (gi == oi).all(), "kNN rows differ (k=%d)" % k
+            assert np.array_equal(gd, od), "kNN distances differ (k=%d)" % k
+
+
+def test_knn_edge_cases(gb, oracle_mod):
+    # fewer points than k, a single point, one bucket
+    P = np.array([[0, 0, 0], [1, 0, 0], [0, 2, 0]], np.float32)
+    with gb.Surface(P) as s:
+        i, d, c = s.knn(np.array([[0.1, 0, 0]], np.float32), 5)
+        assert c[0] == 3 and list(i[0, :3]) == [0, 1, 2] and (i[0, 3:] == 0xFFFFFFFF).all()
+        assert np.isinf(d[0, 3:]).all()
+    with gb.Surface(P[:1]) as s:
+        i, d, c = s.knn(np.array([[5, 5, 5]], np.float32), 2)
+        assert c[0] == 1 and i[0, 0] == 0
+    with gb.Surface(np.zeros((0, 3), np.float32)) as s:
+        i, d, c = s.knn(np.array([[5, 5, 5]], np.float32), 2)
+        assert c[0] == 0
+        with pytest.raises(gb.LvrgbError):
+            s.reconstruct(voxelsize=1.0)
+
+
+def test_knn_golden(gb):
+    for name in ("sphere", "scan", "lattice"):
+        P = GOLD[name + "/points"]
+        with gb.Surface(P) as s:
+            i, d, _ = s.knn(P[::7], 8)
+        assert (i == GOLD[name + "/knn_idx"]).all() and np.array_equal(d, GOLD[name + "/knn_dist"])
+
+
+@pytest.mark.parametrize("name", ["spheres", "scan", "golden_sphere"])
+@pytest.mark.parametrize("nem", [3, 2, 0])
+def test_normals_against_oracle(gb, oracle_mod, name, nem):
+    if name == "golden_sphere":
+        P = GOLD["sphere/points"]
+    else:
+        P = cloud(name)
+    flip = (P.min(0) + P.max(0)) / 2 if name != "scan" else np.zeros(3, np.float32)
+    kn = 10
+    o = oracle_mod.OracleSurface(P)
+    on, ok = o.normals(kn, nem=nem, adaptive=True, flip=np.asarray(flip, np.float32), with_k=True)
+    with gb.Surface(P, kn=kn, ki=0, nem=nem, flip_point=flip) as s:
+        s.calculate_normals()
+        gn, gk = s.raw_normals()
+        stats = s.normal_stats()
+    # identical neighbour sets => identical adaptive rounds (bounding-box test in float)
+    assert (gk == ok).all()
+    assert stats[:5].sum() == len(P)
+    good = np.isfinite(on).all(1) & np.isfinite(gn).all(1)
+    if nem == 0:
+        # least-squares y = f(x, z) is ill-conditioned for planes parallel to y:
+        # compare where the normal is not within 25 degrees of horizontal
+        good &= np.abs(on[:, 1]) > 0.42
+    ang = angle_deg(gn[good], on[good])
+    assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG, np.percentile(ang, [50, 99, 99.9, 100])
+    # sign consistency: same orientation wherever the flip direction is not
+    # nearly tangent to the surface
+    tvec = np.asarray(flip, np.float32) - P
+    tvec /= np.maximum(np.linalg.norm(tvec, axis=1, keepdims=True), 1e-30)
+    clear = np.abs(np.sum(on * tvec, axis=1)) > 0.05
+    assert (np.sum(gn * on, axis=1)[good & clear] > 0).all()
+
+
+@pytest.mark.parametrize("name", ["spheres", "scan"])
+def test_pca_against_fp64(gb, oracle_mod, name):
+    """nem 3 (FP32 centred covariance, FP64 fallback on small eigengaps)
+    against float64 PCA of the same neighbourhoods."""
+    P = cloud(name)
+    flip = (P.min(0) + P.max(0)) / 2
+    with gb.Surface(P, kn=10, ki=0, nem=3, flip_point=flip) as s:
+        s.calculate_normals()
+        gn, gk = s.raw_normals()
+        sel = np.arange(0, len(P), 7)
+        rows = []
+        for k in np.unique(gk[sel]):
+            m = sel[gk[sel] == k]
+            i, _, _ = s.knn(P[m], int(k))
+            rows.append((m, i))
+    idx = np.concatenate([m for m, _ in rows])
+    nbr = [r for _, i in rows for r in i]
+    ref = fp64_pca_normals(P, idx, nbr, flip)
+    ang = angle_deg(gn[idx], ref, unsigned=True)
+    assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG, np.percentile(ang, [50, 99, 99.9, 100])
+
+
+def test_interpolation_bit_exact(gb, oracle_mod):
+    for name in ("sphere", "scan", "lattice"):
+        P = GOLD[name + "/points"]
+        with gb.Surface(P, ki=6) as s:
+            s.set_normals(GOLD[name + "/normals_nem3"])
+            s.interpolate_normals()
+            out = s.normals()
+        assert np.array_equal(out, GOLD[name + "/interp"], equal_nan=True), name
+
+
+def test_distance_bit_exact(gb, oracle_mod):
+    for name in ("sphere", "scan", "lattice"):
+        P = GOLD[name + "/points"]
+        with gb.Surface(P, kd=4) as s:
+            s.set_normals(GOLD[name + "/interp"])
+            proj, eucl = s.distance(GOLD[name + "/dist_q"])
+        assert np.array_equal(proj, GOLD[name + "/dist_proj"], equal_nan=True), name
+        assert np.array_equal(eucl, GOLD[name + "/dist_eucl"], equal_nan=True), name
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+@pytest.mark.parametrize("dec", ["MC", "PMC"])
+def test_grid_and_mesh_bit_exact(gb, oracle_mod, name, dec):
+    P = GOLD[name + "/points"]
+    vs = float(GOLD[name + "/voxelsize"])
+    with gb.Surface(P, kd=4) as s:
+        s.set_normals(GOLD[name + "/interp"])
+        info = s.reconstruct(voxelsize=vs, decomposition=dec)
+        cells_all, cells_valid = s.cells()
+        lat, pos, dist, inv = s.grid()
+        v, f, e = s.mesh()
+    key = "%s/%s/" % (name, dec)
+    ca = cells_all[np.lexsort((cells_all[:, 2], cells_all[:, 1], cells_all[:, 0]))]
+    assert np.array_equal(ca, GOLD[key + "cells_all"])
+    order = np.lexsort((lat[:, 2], lat[:, 1], lat[:, 0]))
+    assert np.array_equal(lat[order], GOLD[key + "qp_lattice"])
+    assert np.array_equal(pos[order], GOLD[key + "qp_pos"])
+    assert np.array_equal(dist[order], GOLD[key + "qp_dist"], equal_nan=True)
+    assert np.array_equal(inv[order], GOLD[key + "qp_invalid"])
+    cv = cells_valid[np.lexsort((cells_valid[:, 2], cells_valid[:, 1], cells_valid[:, 0]))]
+    assert np.array_equal(cv, GOLD[key + "cells_valid"])
+    assert info.faces == len(GOLD[key + "faces"]) and info.vertices == len(GOLD[key + "vkeys"])
+    a = canonical_mesh(e, v, f)
+    b = canonical_mesh(GOLD[key + "vkeys"], GOLD[key + "vpos"], GOLD[key + "faces"])
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("dec", ["MC", "PMC"])
+def test_end_to_end_mesh_against_oracle(gb, oracle_mod, dec):
+    """Whole pipeline on a scan-shaped cloud: GPU normals feed the GPU grid; the
+    oracle runs marching cubes on the GPU's grid values (same input), and its
+    own grid from the GPU normals must agree on cells and signed distances."""
+    P = cloud("scan")
+    o = oracle_mod.OracleSurface(P)
+    with gb.Surface(P, kn=10, ki=10, kd=5, nem=3, flip_point=(0, 0, 0)) as s:
+        s.calculate_normals()
+        gn = s.normals()
+        info = s.reconstruct(voxelsize=10.0, decomposition=dec)
+        lat, pos, dist, inv = s.grid()
+        v, f, e = s.mesh()
+        ca, cv = s.cells()
+    r = o.reconstruct(gn, voxelsize=10.0, kd=5, decomposition=dec)
+    order = np.lexsort((lat[:, 2], lat[:, 1], lat[:, 0]))
+    assert np.array_equal(lat[order], r["qp_lattice"])
+    assert np.array_equal(dist[order], r["qp_dist"])
+    assert np.array_equal(inv[order], r["qp_invalid"])
+    a = canonical_mesh(e, v, f)
+    b = canonical_mesh(r["vkeys"], r["vpos"], r["faces"])
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert info.faces > 1000
+
+
+def test_grid_distances_invalid_rule(gb):
+    P = GOLD["scan/points"]
+    vs = float(GOLD["scan/voxelsize"])
+    with gb.Surface(P, kd=4) as s:
+        s.set_normals(GOLD["scan/interp"])
+        q = GOLD["scan/PMC/qp_pos"]
+        d, inv = s.grid_distances(q, vs)
+    assert np.array_equal(d, GOLD["scan/PMC/qp_dist"])
+    assert np.array_equal(inv, GOLD["scan/PMC/qp_invalid"])
+
+
+def test_interpolated_normal_matches_oracle(gb, oracle_mod):
+    P = GOLD["scan/points"]
+    o = oracle_mod.OracleSurface(P)
+    q = GOLD["scan/dist_q"]
+    ref = o.interpolated_normal(GOLD["scan/interp"], 6, q)
+    with gb.Surface(P, ki=6) as s:
+        s.set_normals(GOLD["scan/interp"])
+        out = s.interpolated_normal(q)
+    assert np.array_equal(out, ref)
+
+
+def test_status_codes_on_gpu(gb):
+    P = GOLD["sphere/points"]
+    with gb.Surface(P) as s:
+        with pytest.raises(gb.LvrgbError) as e:
+            s.distance(P[:4])
+        assert e.value.status == 5  # no normals yet
+        with pytest.raises(gb.LvrgbError) as e:
+            s.knn(P[:4], 0)
+        assert e.value.status == 1
+        s.calculate_normals()
+        with pytest.raises(gb.LvrgbError) as e:
+            s.reconstruct(voxelsize=-1.0)
+        assert e.value.status == 1
+        with pytest.raises(gb.LvrgbError) as e:
+            s.reconstruct(voxelsize=1e-9)
+        assert e.value.status == 1  # grid extent beyond 2^20 cells per axis

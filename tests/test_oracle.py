@@ -1,0 +1,137 @@
+"""The CPU oracle against brute force, float64 PCA and its frozen outputs."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tests.helpers import angle_deg, canonical_mesh, fp64_pca_normals
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLD = np.load(ROOT / "tests/golden/oracle_small.npz")
+
+
+def brute_knn(P, Q, k):
+    d = Q[:, None, :].astype(np.float32) - P[None, :, :].astype(np.float32)
+    sq = d * d
+    d2 = (sq[..., 0] + sq[..., 1]) + sq[..., 2]
+    idx = np.broadcast_to(np.arange(len(P)), d2.shape)
+    order = np.lexsort((idx, d2), axis=1)[:, :k]
+    return order.astype(np.uint32), np.sqrt(np.take_along_axis(d2, order, 1))
+
+
+@pytest.mark.parametrize("kind", ["uniform", "lattice", "duplicates"])
+def test_canonical_knn_is_exact(oracle_mod, kind):
+    rng = np.random.Generator(np.random.PCG64(5))
+    if kind == "uniform":
+        P = rng.uniform(-1, 1, (3000, 3)).astype(np.float32)
+    elif kind == "lattice":
+        g = np.stack(np.meshgrid(*[np.arange(14)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        P = (g * 0.25).astype(np.float32)
+    else:
+        P = rng.uniform(0, 1, (1000, 3)).astype(np.float32)
+        P = np.concatenate([P, P[:300], P[:50]])
+    Q = np.concatenate([P[::11], rng.uniform(-1.5, 1.5, (50, 3)).astype(np.float32)])
+    s = oracle_mod.OracleSurface(P, threads=2)
+    for k in (1, 7, 20):
+        idx, dist, cnt = s.knn(Q, k)
+        bi, bd = brute_knn(P, Q, k)
+        assert (idx == bi).all()
+        assert (dist == bd).all()
+        assert (cnt == k).all()
+
+
+def test_knn_fewer_points_than_k(oracle_mod):
+    P = np.array([[0, 0, 0], [1, 0, 0], [0, 2, 0]], np.float32)
+    s = oracle_mod.OracleSurface(P)
+    idx, dist, cnt = s.knn(np.zeros((1, 3), np.float32), 5)
+    assert cnt[0] == 3
+    assert list(idx[0, :3]) == [0, 1, 2] and (idx[0, 3:] == 0xFFFFFFFF).all()
+    assert np.isinf(dist[0, 3:]).all()
+
+
+def test_reference_order_agrees_except_near_ties(oracle_mod):
+    """The reference kd-tree ranks by double d2; the canonical order by float32
+    d2 and index.  Sets may differ only where float32 d2 ties at the k-th."""
+    rng = np.random.Generator(np.random.PCG64(6))
+    P = rng.uniform(0, 1, (20000, 3)).astype(np.float32)
+    s = oracle_mod.OracleSurface(P, threads=2)
+    Q = P[::13]
+    a, da, _ = s.knn(Q, 10, canonical=True)
+    b, db, _ = s.knn(Q, 10, canonical=False)
+    same = np.array([set(x) == set(y) for x, y in zip(a, b)])
+    assert same.mean() > 0.999
+    for r in np.nonzero(~same)[0]:
+        assert abs(float(da[r, -1]) - float(db[r, -1])) <= 1e-6 * float(da[r, -1])
+
+
+def test_ipca_normals_match_fp64_pca(oracle_mod):
+    pts = GOLD["sphere/points"]
+    s = oracle_mod.OracleSurface(pts)
+    flip = np.array([0.5, 0.5, 0.5], np.float32)
+    n, k = s.normals(5, nem=3, adaptive=True, flip=flip, with_k=True)
+    sel = np.arange(0, len(pts), 5)
+    nb = np.concatenate([s.knn(pts[i:i + 1], int(k[i]))[0] for i in sel])
+    ref = fp64_pca_normals(pts, sel, nb, flip)
+    assert np.percentile(angle_deg(n[sel], ref), 99.9) < 0.05
+
+
+def test_oracle_reproduces_frozen_outputs(oracle_mod):
+    for name in ("sphere", "scan", "lattice"):
+        pts = GOLD[name + "/points"]
+        s = oracle_mod.OracleSurface(pts, threads=2)
+        idx, dist, _ = s.knn(pts[::7], 8)
+        assert (idx == GOLD[name + "/knn_idx"]).all() and (dist == GOLD[name + "/knn_dist"]).all()
+        flip = np.array([0.5, 0.5, 0.5], np.float32) if name == "sphere" else np.zeros(3, np.float32)
+        for nem in (0, 2, 3):
+            n, k = s.normals(5, nem=nem, adaptive=True, flip=flip, with_k=True)
+            assert (k == GOLD["%s/kused_nem%d" % (name, nem)]).all()
+            assert np.array_equal(n, GOLD["%s/normals_nem%d" % (name, nem)], equal_nan=True)
+        inter = s.interpolate(GOLD[name + "/normals_nem3"], 6)
+        assert np.array_equal(inter, GOLD[name + "/interp"], equal_nan=True)
+        proj, eucl = s.distance(inter, 4, GOLD[name + "/dist_q"])
+        assert np.array_equal(proj, GOLD[name + "/dist_proj"], equal_nan=True)
+        vs = float(GOLD[name + "/voxelsize"])
+        r = s.reconstruct(inter, voxelsize=vs, kd=4, decomposition="PMC")
+        for key in ("cells_all", "cells_valid", "qp_lattice", "qp_pos", "qp_dist", "qp_invalid"):
+            assert np.array_equal(r[key], GOLD["%s/PMC/%s" % (name, key)], equal_nan=True), key
+        a = canonical_mesh(r["vkeys"], r["vpos"], r["faces"])
+        b = canonical_mesh(GOLD[name + "/PMC/vkeys"], GOLD[name + "/PMC/vpos"], GOLD[name + "/PMC/faces"])
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_mesh_is_closed_on_a_sphere(oracle_mod):
+    """Marching cubes on a closed surface gives a mesh in which no edge is
+    shared by more than two faces and almost every edge by exactly two (the
+    rest border the few holes left by culled cells)."""
+    pts = GOLD["sphere/points"]
+    s = oracle_mod.OracleSurface(pts)
+    flip = np.array([0.5, 0.5, 0.5], np.float32)
+    n = s.interpolate(s.normals(5, nem=3, flip=flip), 6)
+    r = s.reconstruct(n, voxelsize=0.05, kd=4, decomposition="MC")
+    f = r["faces"].astype(np.int64)
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    _, counts = np.unique(e, axis=0, return_counts=True)
+    assert len(f) > 100
+    assert counts.max() == 2
+    assert (counts == 2).mean() > 0.98
+
+
+def test_grid_invalid_rule_and_culling(oracle_mod):
+    pts = GOLD["scan/points"]
+    vs = float(GOLD["scan/voxelsize"])
+    s = oracle_mod.OracleSurface(pts)
+    r = s.reconstruct(GOLD["scan/interp"], voxelsize=vs, kd=4)
+    # culled cells are exactly the cells with an invalid corner
+    lat = {tuple(x): bool(i) for x, i in zip(r["qp_lattice"], r["qp_invalid"])}
+    corner = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+    valid = {tuple(c) for c in r["cells_valid"]}
+    for c in r["cells_all"]:
+        ok = not any(lat[tuple(c + o)] for o in corner)
+        assert ok == (tuple(c) in valid)
+
+
+def test_unsupported_method(oracle_mod):
+    s = oracle_mod.OracleSurface(GOLD["sphere/points"])
+    with pytest.raises(ValueError):
+        s.normals(5, nem=1)
