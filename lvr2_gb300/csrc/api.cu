@@ -126,7 +126,8 @@ void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
     LVRGB_CUDA(cudaStreamSynchronize(st));
     if (h[0]) {
         LVRGB_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int), st));
-        throw ApiError{LVRGB_ERR_KERNEL, "kNN traversal exceeded its stack depth"};
+        throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack) ? "kNN traversal exceeded its stack depth"
+                                                            : "tree walk exceeded its bound (malformed tree)"};
     }
 }
 
@@ -223,7 +224,7 @@ void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, c
     s->has_normals = s->has_raw = s->has_grid = false;
     const float* dx = stage_in(s->ws, "api.xyz", xyz, size_t(n) * 3, on_device, st);
     record(s, 0, st);
-    lbvh_build(dx, int(n), s->cfg.bucket, s->ws, "tree", s->T, s->d_box, st);
+    lbvh_build(dx, int(n), s->cfg.bucket, s->ws, "tree", s->T, s->d_box, s->d_err, st);
     record(s, 1, st);
     s->ev_used[0] = true;
     float h[6] = {0, 0, 0, 0, 0, 0};
@@ -238,6 +239,7 @@ void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, c
     for (int i = 0; i < 6; i++) s->bb[i] = h[i];
     // BoundingBox centroid (BoundingBox.tcc:210-214)
     for (int a = 0; a < 3; a++) s->bb[6 + a] = h[a] + 0.5f * (h[3 + a] - h[a]);
+    check_kernel_error(s, st);
     s->normals = s->ws.get<float4>("api.normals", size_t(n));
     s->raw_normals = s->ws.get<float4>("api.raw_normals", size_t(n));
     s->kused = s->ws.get<int32_t>("api.kused", size_t(n));

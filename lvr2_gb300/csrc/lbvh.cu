@@ -96,7 +96,7 @@ __device__ __forceinline__ void write_child_box(TreeNode* nd, int side, const fl
 // One warp per bucket: reduce the bucket box, then lane 0 climbs the tree;
 // the second child to arrive at a node merges both boxes and continues.
 __global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket, int nb, TreeNode* nodes,
-                              const int* __restrict__ bparent, int* __restrict__ counters) {
+                              const int* __restrict__ bparent, int* __restrict__ counters, int* __restrict__ err) {
     const int lane = threadIdx.x & 31;
     const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (b >= nb) return;
@@ -116,7 +116,14 @@ __global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket,
         }
     if (lane != 0 || nb == 1) return;
     int pw = bparent[b];
-    while (pw >= 0) {
+    // The path to the root of a radix tree over 30-bit keys with index
+    // tie-breaks has fewer than 64 + 32 links; the bound only guards against a
+    // malformed parent chain.
+    for (int hops = 0; pw >= 0; hops++) {
+        if (hops > 128) {
+            atomicOr(err, kErrWalk);
+            return;
+        }
         const int p = pw >> 1, side = pw & 1;
         TreeNode* nd = nodes + p;
         write_child_box(nd, side, lo, hi);
@@ -136,7 +143,7 @@ __global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket,
 }  // namespace
 
 void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::string& tag, Lbvh& T,
-                float* d_box, cudaStream_t s) {
+                float* d_box, int* d_err, cudaStream_t s) {
     if (bucket < 1 || bucket > 32) bucket = 32;
     T.n = n;
     T.bucket = bucket;
@@ -175,7 +182,8 @@ void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::s
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, sizeof(int) * size_t(nb - 1), s));
     karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(scodes, bucket, nb, nodes, bparent);
     LVRGB_LAUNCH_CHECK();
-    bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, n, bucket, nb, nodes, bparent, counters);
+    bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, n, bucket, nb, nodes, bparent, counters,
+                                                                 d_err);
     LVRGB_LAUNCH_CHECK();
 }
 

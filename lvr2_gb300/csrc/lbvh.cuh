@@ -40,6 +40,7 @@ struct Lbvh {
 
 constexpr int kStackMax = 64;  // two register entries per lane
 constexpr int kErrStack = 1;   // traversal stack would overflow (never for depth <= 63)
+constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can have
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
 // base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.
@@ -140,7 +141,14 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
     int sp = 0;
     int node = 0;  // root
+    // A tree over nb buckets has nb - 1 internal nodes; each is expanded at
+    // most once per warp.  The bound only guards against a malformed tree.
+    int budget = T.nbuckets + 1;
     while (true) {
+        if (--budget < 0) {
+            if (lane == 0) atomicOr(err, kErrWalk);
+            return;
+        }
         // ---- expand an internal node -----------------------------------
         const TreeNode* nd = T.nodes + node;
         const float4 a = __ldg(&nd->a);

@@ -9,8 +9,9 @@ namespace lvrgb {
 
 // Builds the LBVH of n AoS float32 points held in device memory.  The sorted
 // points, inverse permutation and nodes live in ws under the given tag;
-// d_box (6 device floats) receives the point bounding box.
+// d_box (6 device floats) receives the point bounding box; d_err receives
+// kErrWalk if the bottom-up pass meets a malformed parent chain.
 void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::string& tag, Lbvh& T,
-                float* d_box, cudaStream_t s);
+                float* d_box, int* d_err, cudaStream_t s);
 
 }  // namespace lvrgb
