@@ -147,16 +147,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_kernel(SdfArgs A) {
         if (active) {
             heap.sort_ascending();
             float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
-            int cnt = 0;
-            for (int s = 0; s < A.K; s++) {
+            const int cnt = min(A.K, A.T.n);
+#pragma unroll 4
+            for (int s = 0; s < cnt; s++) {
                 const unsigned long long key = heap.at(s);
-                if (key == kKeyEmpty) break;
                 const uint32_t j = __ldg(A.T.inv + key_idx(key));
                 const float4 p = __ldg(A.T.pts + j);
                 const float4 nn = __ldg(A.normals + j);
                 px = __fadd_rn(px, p.x); py = __fadd_rn(py, p.y); pz = __fadd_rn(pz, p.z);
                 nx = __fadd_rn(nx, nn.x); ny = __fadd_rn(ny, nn.y); nz = __fadd_rn(nz, nn.z);
-                cnt++;
             }
             float proj, eu;
             if (cnt == 0) {

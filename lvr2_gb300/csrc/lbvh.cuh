@@ -110,18 +110,34 @@ struct LaneHeap {
     }
 };
 
+// Scans one bucket for all lanes.  The bucket (<= 32 points) is staged in
+// shared memory with NaN padding, each lane computes all 32 distances as
+// independent straight-line code and keeps an acceptance mask, and only the
+// accepted candidates go through the heap (re-tested against the shrinking
+// bound).
 __device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, float qy, float qz, bool active,
                                             LaneHeap& heap, float4* stage) {
     const int lane = threadIdx.x & 31;
     const int first = b * T.bucket;
     int cnt = T.n - first;
     if (cnt > T.bucket) cnt = T.bucket;
-    if (lane < cnt) stage[lane] = __ldg(T.pts + first + lane);
+    const float nan = __int_as_float(0x7fffffff);
+    stage[lane] = lane < cnt ? __ldg(T.pts + first + lane) : make_float4(nan, nan, nan, 0.0f);
     __syncwarp();
     if (active) {
-        for (int j = 0; j < cnt; j++) {
-            float4 c = stage[j];
-            float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+        const float tau = heap.tau();
+        unsigned mask = 0;
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const float4 c = stage[j];
+            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+            mask |= (d2 <= tau ? 1u : 0u) << j;
+        }
+        while (mask) {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const float4 c = stage[j];
+            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
             if (d2 <= heap.tau()) heap.offer(d2, __float_as_uint(c.w));
         }
     }

@@ -150,33 +150,58 @@ __device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
     }
 }
 
+// First pass over the neighbourhood: bounding box (for the adaptive-k test)
+// and the sums each plane fit needs.  Real heap entries occupy [0, cnt).
+struct NbrPass {
+    float lo[3], hi[3];
+    float s[3], c[3];  // compensated sums of p - q (nem 0 and 3)
+    float r[6];        // sums of (p - q)(p - q)^T in IEEE order (nem 2)
+};
+
 template <int kNem>
-__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, float4 q, float n[3],
-                                          bool& fp64) {
+__device__ __forceinline__ void neighbour_pass(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, NbrPass& P) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        P.lo[a] = FLT_MAX; P.hi[a] = -FLT_MAX; P.s[a] = 0.0f; P.c[a] = 0.0f;
+    }
+#pragma unroll
+    for (int a = 0; a < 6; a++) P.r[a] = 0.0f;
+#pragma unroll 4
+    for (int s = 0; s < cnt; s++) {
+        const float4 p = neighbour_point(T, heap.at(s));
+        P.lo[0] = fminf(p.x, P.lo[0]); P.lo[1] = fminf(p.y, P.lo[1]); P.lo[2] = fminf(p.z, P.lo[2]);
+        P.hi[0] = fmaxf(p.x, P.hi[0]); P.hi[1] = fmaxf(p.y, P.hi[1]); P.hi[2] = fmaxf(p.z, P.hi[2]);
+        if (kNem == 2) {
+            const float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
+            P.r[0] = __fadd_rn(P.r[0], __fmul_rn(rx, rx));
+            P.r[1] = __fadd_rn(P.r[1], __fmul_rn(rx, ry));
+            P.r[2] = __fadd_rn(P.r[2], __fmul_rn(rx, rz));
+            P.r[3] = __fadd_rn(P.r[3], __fmul_rn(ry, ry));
+            P.r[4] = __fadd_rn(P.r[4], __fmul_rn(ry, rz));
+            P.r[5] = __fadd_rn(P.r[5], __fmul_rn(rz, rz));
+        } else {
+            kahan_add(P.s[0], P.c[0], p.x - q.x);
+            kahan_add(P.s[1], P.c[1], p.y - q.y);
+            kahan_add(P.s[2], P.c[2], p.z - q.z);
+        }
+    }
+}
+
+template <int kNem>
+__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, int cnt, float4 q,
+                                          const NbrPass& P, float n[3], bool& fp64) {
     fp64 = false;
     if (kNem == 3) {
         // PCA of {q} and its neighbours (calcPlaneIPCAExact starts its
-        // incremental mean at the query point), centred two-pass covariance in
-        // coordinates relative to q with compensated sums.
-        float sx = 0, sy = 0, sz = 0, cx = 0, cy = 0, cz = 0;
-        int cnt = 0;
-        for (int s = 0; s < A.K; s++) {
-            unsigned long long key = heap.at(s);
-            if (key == kKeyEmpty) continue;
-            float4 p = neighbour_point(A.T, key);
-            kahan_add(sx, cx, p.x - q.x);
-            kahan_add(sy, cy, p.y - q.y);
-            kahan_add(sz, cz, p.z - q.z);
-            cnt++;
-        }
+        // incremental mean at the query point): covariance about the centroid,
+        // second pass, coordinates relative to q, compensated sums.
         const float m = float(cnt + 1);
-        const float mx = sx / m, my = sy / m, mz = sz / m;
+        const float mx = P.s[0] / m, my = P.s[1] / m, mz = P.s[2] / m;
         float S[6] = {mx * mx, mx * my, mx * mz, my * my, my * mz, mz * mz};  // the query point itself
         float C[6] = {0, 0, 0, 0, 0, 0};
-        for (int s = 0; s < A.K; s++) {
-            unsigned long long key = heap.at(s);
-            if (key == kKeyEmpty) continue;
-            float4 p = neighbour_point(A.T, key);
+#pragma unroll 4
+        for (int s = 0; s < cnt; s++) {
+            const float4 p = neighbour_point(A.T, heap.at(s));
             const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
             kahan_add(S[0], C[0], ex * ex);
             kahan_add(S[1], C[1], ex * ey);
@@ -196,21 +221,9 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
             fp64 = true;
         }
     } else if (kNem == 2) {
-        // calcPlaneIterative: sums of (p - q)(p - q)^T and the largest of the
-        // three cofactor determinants.
-        float xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0;
-        for (int s = 0; s < A.K; s++) {
-            unsigned long long key = heap.at(s);
-            if (key == kKeyEmpty) continue;
-            float4 p = neighbour_point(A.T, key);
-            const float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
-            xx = __fadd_rn(xx, __fmul_rn(rx, rx));
-            xy = __fadd_rn(xy, __fmul_rn(rx, ry));
-            xz = __fadd_rn(xz, __fmul_rn(rx, rz));
-            yy = __fadd_rn(yy, __fmul_rn(ry, ry));
-            yz = __fadd_rn(yz, __fmul_rn(ry, rz));
-            zz = __fadd_rn(zz, __fmul_rn(rz, rz));
-        }
+        // calcPlaneIterative: the largest of the three cofactor determinants
+        // of the sums of (p - q)(p - q)^T.
+        const float xx = P.r[0], xy = P.r[1], xz = P.r[2], yy = P.r[3], yz = P.r[4], zz = P.r[5];
         const float det_x = __fsub_rn(__fmul_rn(yy, zz), __fmul_rn(yz, yz));
         const float det_y = __fsub_rn(__fmul_rn(xx, zz), __fmul_rn(xz, xz));
         const float det_z = __fsub_rn(__fmul_rn(xx, yy), __fmul_rn(xy, xy));
@@ -237,24 +250,12 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
         // calcPlane (nem 0): least-squares y = C0 + C1 x + C2 z over the
         // neighbours; centred FP32 sums relative to q, 2x2 solve in FP64,
         // then the reference's two in-plane vectors at +100 offsets.
-        float sx = 0, sy = 0, sz = 0, cx = 0, cy = 0, cz = 0;
-        int cnt = 0;
-        for (int s = 0; s < A.K; s++) {
-            unsigned long long key = heap.at(s);
-            if (key == kKeyEmpty) continue;
-            float4 p = neighbour_point(A.T, key);
-            kahan_add(sx, cx, p.x - q.x);
-            kahan_add(sy, cy, p.y - q.y);
-            kahan_add(sz, cz, p.z - q.z);
-            cnt++;
-        }
         const float m = float(cnt > 0 ? cnt : 1);
-        const float mx = sx / m, my = sy / m, mz = sz / m;
+        const float mx = P.s[0] / m, my = P.s[1] / m, mz = P.s[2] / m;
         float S[5] = {0, 0, 0, 0, 0}, C[5] = {0, 0, 0, 0, 0};  // xx xz zz xy zy
-        for (int s = 0; s < A.K; s++) {
-            unsigned long long key = heap.at(s);
-            if (key == kKeyEmpty) continue;
-            float4 p = neighbour_point(A.T, key);
+#pragma unroll 4
+        for (int s = 0; s < cnt; s++) {
+            const float4 p = neighbour_point(A.T, heap.at(s));
             const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
             kahan_add(S[0], C[0], ex * ex);
             kahan_add(S[1], C[1], ex * ez);
@@ -290,6 +291,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
     const unsigned lt = (1u << lane) - 1u;
+    const int cnt = min(A.K, A.T.n);
     for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
          tile += gridDim.x * kWarpsPerBlock) {
         const int qi = tile * 32 + lane;
@@ -301,18 +303,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
         bool retry = false;
         if (active) {
+            if (A.T.n < A.K) heap.sort_ascending();  // real entries first
+            NbrPass P;
+            neighbour_pass<kNem>(A.T, heap, cnt, q, P);
             bool fit = true;
             if (A.adaptive && !A.last_round) {
                 // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
-                float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-                for (int s = 0; s < A.K; s++) {
-                    unsigned long long key = heap.at(s);
-                    if (key == kKeyEmpty) continue;
-                    float4 p = neighbour_point(A.T, key);
-                    lo[0] = fminf(p.x, lo[0]); lo[1] = fminf(p.y, lo[1]); lo[2] = fminf(p.z, lo[2]);
-                    hi[0] = fmaxf(p.x, hi[0]); hi[1] = fmaxf(p.y, hi[1]); hi[2] = fmaxf(p.z, hi[2]);
-                }
-                const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
+                const float dx = __fsub_rn(P.hi[0], P.lo[0]), dy = __fsub_rn(P.hi[1], P.lo[1]),
+                            dz = __fsub_rn(P.hi[2], P.lo[2]);
                 const float e = 0.05f;
                 fit = dx >= __fmul_rn(e, dy) && dx >= __fmul_rn(e, dz) && dy >= __fmul_rn(e, dx) &&
                       dy >= __fmul_rn(e, dz) && dz >= __fmul_rn(e, dx) && dz >= __fmul_rn(e, dy);
@@ -320,7 +318,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
             if (fit) {
                 float n[3];
                 bool fp64;
-                fit_plane<kNem>(A, heap, q, n, fp64);
+                fit_plane<kNem>(A, heap, cnt, q, P, n, fp64);
                 // Flip toward the flip point; Normal::operator-() re-normalises.
                 const float tx = __fsub_rn(A.fx, q.x), ty = __fsub_rn(A.fy, q.y), tz = __fsub_rn(A.fz, q.z);
                 const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
@@ -373,9 +371,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) interpolate_kernel(Interp
             heap.sort_ascending();
             float4 m = A.in[pos];
             float x = m.x, y = m.y, z = m.z;
-            for (int s = 0; s < A.K; s++) {
-                unsigned long long key = heap.at(s);
-                if (key == kKeyEmpty) break;
+            const int cnt = min(A.K, A.T.n);
+#pragma unroll 4
+            for (int s = 0; s < cnt; s++) {
+                const unsigned long long key = heap.at(s);
                 const float4 nj = __ldg(A.in + __ldg(A.T.inv + key_idx(key)));
                 x = __fadd_rn(x, nj.x);
                 y = __fadd_rn(y, nj.y);
