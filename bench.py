@@ -224,7 +224,7 @@ def run_gpu(args):
         dist.barrier()
     l0 = kernel_launches()
     stage = np.zeros(7)
-    stats_acc = np.zeros(8)
+    stats_acc = np.zeros(16)
     infos = []
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
@@ -301,7 +301,10 @@ def run_gpu(args):
                   "sdf_evals_per_s_stage": nq / (sdf_ms / 1000.0),
                   "mc_cells_per_s_stage": ncv / (stage[6] / 1000.0) if stage[6] > 0 else None},
         "counts": {"grid_vertices": int(nq), "cells_valid": int(ncv), "faces": int(nf), "vertices": int(nv),
-                   "fitted_per_round": [int(x) for x in stats[:5]], "fp64_eigensolves": int(stats[5])},
+                   "fitted_per_round": [int(x) for x in stats[:5]], "fp64_eigensolves": int(stats[5]),
+                   "normals_buckets_per_warp": float(stats[8]) / max(1.0, n / 32.0),
+                   "normals_nodes_per_warp": float(stats[9]) / max(1.0, n / 32.0),
+                   "normals_heap_pushes_per_query": float(stats[10]) / max(1.0, n)},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": int(dom["bytes"]), "traffic": None},

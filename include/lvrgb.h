@@ -130,8 +130,10 @@ lvrgb_status lvrgb_get_raw_normals(lvrgb_surface s, float* normals, int32_t* k_u
 lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on_device, void* stream);
 
 /* Counters of the last lvrgb_calculate_normals: out[0..4] planes fitted in
- * search round 1..5, out[5] PCA eigensolves done in FP64. */
-lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[8]);
+ * search round 1..5, out[5] PCA eigensolves done in FP64, out[8] LBVH
+ * buckets scanned (per 32-query warp), out[9] tree nodes expanded (per warp),
+ * out[10] heap insertions (per query); other entries 0. */
+lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]);
 
 /* Batched k-nearest-neighbour search: SearchTree::kSearch / kSearchParallel
  * (include/lvr2/reconstruction/SearchTree.hpp:71, 101-125),

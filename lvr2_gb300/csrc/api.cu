@@ -1,6 +1,7 @@
 // api.cu -- the C ABI (include/lvrgb.h): handle, input staging, call
 // sequencing and error translation.  No exception crosses this file's
 // extern "C" functions.
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <stdexcept>
@@ -239,6 +240,10 @@ void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, c
     for (int i = 0; i < 6; i++) s->bb[i] = h[i];
     // BoundingBox centroid (BoundingBox.tcc:210-214)
     for (int a = 0; a < 3; a++) s->bb[6 + a] = h[a] + 0.5f * (h[3 + a] - h[a]);
+    // Morton frame of the tree (used to seed searches of arbitrary positions)
+    const float ext = std::max(std::max(h[3] - h[0], h[4] - h[1]), h[5] - h[2]);
+    for (int a = 0; a < 3; a++) s->T.mn[a] = h[a];
+    s->T.scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
     check_kernel_error(s, st);
     s->normals = s->ws.get<float4>("api.normals", size_t(n));
     s->raw_normals = s->ws.get<float4>("api.raw_normals", size_t(n));
@@ -448,7 +453,7 @@ lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on
     });
 }
 
-lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[8]) {
+lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]) {
     return guarded([&] {
         require(s != nullptr && out != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
         DeviceScope dev(s->device);

@@ -143,7 +143,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_kernel(SdfArgs A) {
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        const float4 q0 = A.qs[tile * 32];
+        const int seed = seed_bucket_for(A.T, q0.x, q0.y, q0.z);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, seed);
         if (active) {
             heap.sort_ascending();
             float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;

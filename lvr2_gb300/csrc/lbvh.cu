@@ -86,6 +86,11 @@ __global__ void karras_kernel(const uint32_t* __restrict__ codes, int bucket, in
     if (i == 0) nodes[0].d.z = -1;
 }
 
+__global__ void bucket_keys_kernel(const uint32_t* __restrict__ codes, int bucket, int nb, uint32_t* __restrict__ bkeys) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb) bkeys[b] = codes[size_t(b) * bucket];
+}
+
 __device__ __forceinline__ void write_child_box(TreeNode* nd, int side, const float* lo, const float* hi) {
     float* f = reinterpret_cast<float*>(nd);
     const int o = side ? 6 : 0;
@@ -171,6 +176,10 @@ void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::s
     const uint32_t* scodes = alt ? codes2 : codes;
     const uint32_t* sidx = alt ? idx2 : idx;
     gather_sorted_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, sidx, n, pts, inv);
+    LVRGB_LAUNCH_CHECK();
+    uint32_t* bkeys = ws.get<uint32_t>(tag + ".bkeys", size_t(nb));
+    T.bkeys = bkeys;
+    bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(scodes, bucket, nb, bkeys);
     LVRGB_LAUNCH_CHECK();
 
     int* bparent = ws.get<int>("lbvh.bparent", size_t(nb));

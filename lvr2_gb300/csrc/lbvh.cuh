@@ -33,14 +33,24 @@ struct Lbvh {
     const float4* pts = nullptr;
     const uint32_t* inv = nullptr;
     const TreeNode* nodes = nullptr;
+    const uint32_t* bkeys = nullptr;  // Morton code of each bucket's first point
     int n = 0;
     int nbuckets = 0;
     int bucket = 32;
+    float mn[3] = {0, 0, 0};  // Morton frame: code axis = (x - mn) * scale
+    float scale = 0;
+    int seed_radius = 1;      // buckets scanned on each side of the seed bucket
 };
 
 constexpr int kStackMax = 64;  // two register entries per lane
 constexpr int kErrStack = 1;   // traversal stack would overflow (never for depth <= 63)
 constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can have
+
+// Traversal counters of one warp (nodes, buckets) and one lane (heap
+// insertions); kernels that do not report them let the compiler drop them.
+struct TravStats {
+    unsigned nodes = 0, buckets = 0, pushes = 0;
+};
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
 // base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.
@@ -116,7 +126,8 @@ struct LaneHeap {
 // accepted candidates go through the heap (re-tested against the shrinking
 // bound).
 __device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, float qy, float qz, bool active,
-                                            LaneHeap& heap, float4* stage) {
+                                            LaneHeap& heap, float4* stage, TravStats& st) {
+    st.buckets++;
     const int lane = threadIdx.x & 31;
     const int first = b * T.bucket;
     int cnt = T.n - first;
@@ -138,21 +149,59 @@ __device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, floa
             mask &= mask - 1;
             const float4 c = stage[j];
             const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-            if (d2 <= heap.tau()) heap.offer(d2, __float_as_uint(c.w));
+            if (d2 <= heap.tau()) {
+                const unsigned long long key = make_key(d2, __float_as_uint(c.w));
+                if (key < heap.top) {
+                    heap.push(key);
+                    st.pushes++;
+                }
+            }
         }
     }
     __syncwarp();
 }
 
+// Bucket whose first Morton code is the largest <= the code of (x, y, z):
+// a 32-ary search by the whole warp over the sorted bucket keys (warp-uniform
+// inputs and result).
+__device__ __forceinline__ int seed_bucket_for(const Lbvh& T, float x, float y, float z) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t cx = uint32_t(fminf(fmaxf((x - T.mn[0]) * T.scale, 0.0f), 1023.0f));
+    const uint32_t cy = uint32_t(fminf(fmaxf((y - T.mn[1]) * T.scale, 0.0f), 1023.0f));
+    const uint32_t cz = uint32_t(fminf(fmaxf((z - T.mn[2]) * T.scale, 0.0f), 1023.0f));
+    const uint32_t code = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    int lo = 0, hi = T.nbuckets;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const int step = (hi - lo + 31) / 32;
+        const int probe = lo + lane * step;
+        const bool le = probe < hi && __ldg(T.bkeys + probe) <= code;
+        const int c = __popc(__ballot_sync(kFull, le));
+        if (c == 0) return lo;  // code below the first key of the range
+        lo = lo + (c - 1) * step;
+        hi = min(hi, lo + step);
+    }
+    return lo;
+}
+
 // k-nearest-neighbour search of one query per lane.  On return each lane's
-// heap holds its K smallest (d2, original index) keys (unordered).
+// heap holds its K smallest (d2, original index) keys (unordered).  The
+// warp-uniform seed bucket (and seed_radius buckets on each side, which are
+// Morton neighbours) are scanned first so that the k-th distance bound is
+// small before the tree walk; the walk skips them.
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
-                                             LaneHeap& heap, float4* stage, int* err) {
+                                             LaneHeap& heap, float4* stage, int* err, TravStats& st,
+                                             int seed = -1) {
     const int lane = threadIdx.x & 31;
     if (T.nbuckets <= 0) return;
     if (T.nbuckets == 1) {
-        scan_bucket(T, 0, qx, qy, qz, active, heap, stage);
+        scan_bucket(T, 0, qx, qy, qz, active, heap, stage, st);
         return;
+    }
+    int skip_lo = 1, skip_hi = 0;  // empty range
+    if (seed >= 0) {
+        skip_lo = max(0, seed - T.seed_radius);
+        skip_hi = min(T.nbuckets - 1, seed + T.seed_radius);
+        for (int b = skip_lo; b <= skip_hi; b++) scan_bucket(T, b, qx, qy, qz, active, heap, stage, st);
     }
     int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
     int sp = 0;
@@ -165,6 +214,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
             if (lane == 0) atomicOr(err, kErrWalk);
             return;
         }
+        st.nodes++;
         // ---- expand an internal node -----------------------------------
         const TreeNode* nd = T.nodes + node;
         const float4 a = __ldg(&nd->a);
@@ -208,7 +258,8 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                     node = next;
                     break;
                 }
-                scan_bucket(T, -1 - next, qx, qy, qz, active, heap, stage);
+                const int b = -1 - next;
+                if (b < skip_lo || b > skip_hi) scan_bucket(T, b, qx, qy, qz, active, heap, stage, st);
                 have_next = false;
             }
             if (sp == 0) return;
@@ -236,6 +287,12 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
             }
         }
     }
+}
+
+__device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
+                                             LaneHeap& heap, float4* stage, int* err, int seed = -1) {
+    TravStats st;
+    knn_traverse(T, qx, qy, qz, active, heap, stage, err, st, seed);
 }
 
 // Shared-memory carving of a kNN kernel block: kWarps stage areas of 32

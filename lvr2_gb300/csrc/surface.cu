@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
     const unsigned lt = (1u << lane) - 1u;
     const int cnt = min(A.K, A.T.n);
+    TravStats st;
     for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
          tile += gridDim.x * kWarpsPerBlock) {
         const int qi = tile * 32 + lane;
@@ -300,7 +301,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         const float4 q = __ldg(A.T.pts + pos);
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        const int seed = __shfl_sync(kFull, pos, 0) / A.T.bucket;
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
         bool retry = false;
         if (active) {
             if (A.T.n < A.K) heap.sort_ascending();  // real entries first
@@ -343,6 +345,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
             if (retry) A.retry[base + __popc(rm & lt)] = uint32_t(pos);
         }
     }
+    unsigned pushes = st.pushes;
+    for (int o = 16; o > 0; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
+    if (lane == 0 && st.nodes) {
+        atomicAdd(A.stats + 8, st.buckets);
+        atomicAdd(A.stats + 9, st.nodes);
+        atomicAdd(A.stats + 10, pushes);
+    }
 }
 
 struct InterpArgs {
@@ -366,7 +375,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) interpolate_kernel(Interp
         const float4 q = __ldg(A.T.pts + (active ? pos : 0));
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, (tile * 32) / A.T.bucket);
         if (active) {
             heap.sort_ascending();
             float4 m = A.in[pos];
@@ -450,7 +459,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err);
+        const float4 q0 = A.qs[tile * 32];
+        const int seed = seed_bucket_for(A.T, q0.x, q0.y, q0.z);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, seed);
         if (active) emit_row(A, heap, q);
     }
 }

@@ -13,10 +13,12 @@ struct NormalsConfig {
     float gap_threshold = 1e-3f;  // relative eigengap below which the eigensolve runs in FP64
 };
 
-// Device counters written by compute_normals (uint32[8]):
+// Device counters written by compute_normals (uint32[16]):
 //   [0..4] number of points whose plane was fitted in search round 1..5,
-//   [5]    number of PCA eigensolves that fell back to FP64.
-constexpr int kNormalStats = 8;
+//   [5]    number of PCA eigensolves that fell back to FP64,
+//   [8]    buckets scanned (per warp), [9] tree nodes expanded (per warp),
+//   [10]   heap insertions (per query).
+constexpr int kNormalStats = 16;
 
 // Normals in Morton order (float4, w = 0).  kused (optional, Morton order)
 // receives the k of the search whose neighbourhood was used.

@@ -157,7 +157,7 @@ class Surface:
         check(_lib.load().lvrgb_set_normals(self._h, _ptr(arr), on_dev, self._stream))
 
     def normal_stats(self):
-        out = np.zeros(8, np.uint32)
+        out = np.zeros(16, np.uint32)
         check(_lib.load().lvrgb_normal_stats(self._h, _ptr(out)))
         return out
 
