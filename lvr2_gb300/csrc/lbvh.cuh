@@ -53,28 +53,29 @@ struct TravStats {
 };
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
-// base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.
+// base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.  The
+// first K keys are stored without sifting and heapified once; until then the
+// bound is +inf.
 struct LaneHeap {
     unsigned long long* h;
     int K;
+    int fill;
     unsigned long long top;
 
     __device__ __forceinline__ void init(unsigned long long* lane_base, int k) {
         h = lane_base;
         K = k;
-        for (int s = 0; s < K; s++) h[s * 32] = kKeyEmpty;
+        fill = 0;
         top = kKeyEmpty;
     }
     __device__ __forceinline__ float tau() const { return key_d2(top); }
-    // Replace the maximum by key (caller guarantees key < top).
-    __device__ __forceinline__ void push(unsigned long long key) {
-        int i = 0;
+    __device__ __forceinline__ void sift_down(int i, int end, unsigned long long key) {
         while (true) {
             int l = 2 * i + 1;
-            if (l >= K) break;
+            if (l >= end) break;
             unsigned long long cl = h[l * 32];
             int c = l;
-            if (l + 1 < K) {
+            if (l + 1 < end) {
                 unsigned long long cr = h[(l + 1) * 32];
                 if (cr > cl) { cl = cr; c = l + 1; }
             }
@@ -83,7 +84,28 @@ struct LaneHeap {
             i = c;
         }
         h[i * 32] = key;
+    }
+    __device__ __forceinline__ void heapify() {
+        for (int i = K / 2 - 1; i >= 0; i--) sift_down(i, K, h[i * 32]);
         top = h[0];
+    }
+    // Replace the maximum by key (caller guarantees key < top).
+    __device__ __forceinline__ void push(unsigned long long key) {
+        if (fill < K) {
+            h[(fill++) * 32] = key;
+            if (fill == K) heapify();
+            return;
+        }
+        sift_down(0, K, key);
+        top = h[0];
+    }
+    // Completes the heap when fewer than K keys were offered (sentinels).
+    __device__ __forceinline__ void finish() {
+        if (fill < K) {
+            for (int s = fill; s < K; s++) h[s * 32] = kKeyEmpty;
+            fill = K;
+            heapify();
+        }
     }
     __device__ __forceinline__ void offer(float d2, uint32_t idx) {
         unsigned long long key = make_key(d2, idx);
@@ -95,67 +117,67 @@ struct LaneHeap {
             unsigned long long mx = h[0];
             unsigned long long key = h[end * 32];
             h[end * 32] = mx;
-            int i = 0;
-            while (true) {
-                int l = 2 * i + 1;
-                if (l >= end) break;
-                unsigned long long cl = h[l * 32];
-                int c = l;
-                if (l + 1 < end) {
-                    unsigned long long cr = h[(l + 1) * 32];
-                    if (cr > cl) { cl = cr; c = l + 1; }
-                }
-                if (cl <= key) break;
-                h[i * 32] = cl;
-                i = c;
-            }
-            h[i * 32] = key;
+            sift_down(0, end, key);
         }
     }
     __device__ __forceinline__ unsigned long long at(int s) const { return h[s * 32]; }
-    __device__ __forceinline__ int count() const {
-        int c = 0;
-        for (int s = 0; s < K; s++) c += (h[s * 32] != kKeyEmpty);
-        return c;
-    }
 };
 
-// Scans one bucket for all lanes.  The bucket (<= 32 points) is staged in
-// shared memory with NaN padding, each lane computes all 32 distances as
-// independent straight-line code and keeps an acceptance mask, and only the
-// accepted candidates go through the heap (re-tested against the shrinking
-// bound).
+// Scans one bucket (<= 32 points) for the lanes in `need` (lanes whose
+// k-th bound reaches the bucket's box).  The bucket is staged with NaN
+// padding, one point per lane and in shared memory.  When many lanes need it,
+// every needing lane tests all 32 points (broadcast loads, independent
+// straight-line code); when few do, the warp is transposed: for each needing
+// lane the 32 lanes test its query against their own point and a ballot hands
+// the acceptance mask to the owner.  Both forms evaluate the same dist2
+// expression, so the accepted sets are identical.  Accepted candidates then
+// go through the heap, re-tested against the shrinking bound.
 __device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, float qy, float qz, bool active,
-                                            LaneHeap& heap, float4* stage, TravStats& st) {
+                                            unsigned need, LaneHeap& heap, float4* stage, TravStats& st) {
     st.buckets++;
     const int lane = threadIdx.x & 31;
     const int first = b * T.bucket;
     int cnt = T.n - first;
     if (cnt > T.bucket) cnt = T.bucket;
     const float nan = __int_as_float(0x7fffffff);
-    stage[lane] = lane < cnt ? __ldg(T.pts + first + lane) : make_float4(nan, nan, nan, 0.0f);
+    const float4 mine = lane < cnt ? __ldg(T.pts + first + lane) : make_float4(nan, nan, nan, 0.0f);
+    stage[lane] = mine;
     __syncwarp();
-    if (active) {
-        const float tau = heap.tau();
-        unsigned mask = 0;
+    const float tau = heap.tau();
+    unsigned mask = 0;
+    if (__popc(need) >= 20) {
+        if (active) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const float4 c = stage[j];
-            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-            mask |= (d2 <= tau ? 1u : 0u) << j;
-        }
-        while (mask) {
-            const int j = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const float4 c = stage[j];
-            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-            if (d2 <= heap.tau()) {
-                const unsigned long long key = make_key(d2, __float_as_uint(c.w));
-                if (key < heap.top) {
-                    heap.push(key);
-                    st.pushes++;
-                }
+            for (int j = 0; j < 32; j++) {
+                const float4 c = stage[j];
+                const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+                mask |= (d2 <= tau ? 1u : 0u) << j;
             }
+        }
+    } else {
+        unsigned rest = need;
+        while (rest) {
+            const int i = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const float x = __shfl_sync(kFull, qx, i);
+            const float y = __shfl_sync(kFull, qy, i);
+            const float z = __shfl_sync(kFull, qz, i);
+            const float t = __shfl_sync(kFull, tau, i);
+            const float d2 = dist2(x, y, z, mine.x, mine.y, mine.z);
+            const unsigned m = __ballot_sync(kFull, d2 <= t);
+            if (lane == i) mask = m;
+        }
+        if (!active) mask = 0;
+    }
+    while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const float4 c = stage[j];
+        const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+        const unsigned long long key = make_key(d2, __float_as_uint(c.w));
+        if (key < heap.top) {
+            heap.push(key);
+            st.pushes++;
         }
     }
     __syncwarp();
@@ -192,16 +214,21 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                                              LaneHeap& heap, float4* stage, int* err, TravStats& st,
                                              int seed = -1) {
     const int lane = threadIdx.x & 31;
-    if (T.nbuckets <= 0) return;
+    if (T.nbuckets <= 0) {
+        heap.finish();
+        return;
+    }
+    const unsigned all = __ballot_sync(kFull, active);
     if (T.nbuckets == 1) {
-        scan_bucket(T, 0, qx, qy, qz, active, heap, stage, st);
+        scan_bucket(T, 0, qx, qy, qz, active, all, heap, stage, st);
+        heap.finish();
         return;
     }
     int skip_lo = 1, skip_hi = 0;  // empty range
     if (seed >= 0) {
         skip_lo = max(0, seed - T.seed_radius);
         skip_hi = min(T.nbuckets - 1, seed + T.seed_radius);
-        for (int b = skip_lo; b <= skip_hi; b++) scan_bucket(T, b, qx, qy, qz, active, heap, stage, st);
+        for (int b = skip_lo; b <= skip_hi; b++) scan_bucket(T, b, qx, qy, qz, active, all, heap, stage, st);
     }
     int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
     int sp = 0;
@@ -209,10 +236,11 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     // A tree over nb buckets has nb - 1 internal nodes; each is expanded at
     // most once per warp.  The bound only guards against a malformed tree.
     int budget = T.nbuckets + 1;
-    while (true) {
+    bool done = false;
+    while (!done) {
         if (--budget < 0) {
             if (lane == 0) atomicOr(err, kErrWalk);
-            return;
+            break;
         }
         st.nodes++;
         // ---- expand an internal node -----------------------------------
@@ -228,16 +256,17 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         const bool n1 = active && d1 <= tau;
         const unsigned m0 = __ballot_sync(kFull, n0);
         const unsigned m1 = __ballot_sync(kFull, n1);
-        int next;
-        bool have_next = true;
+        int next = 0;
+        unsigned need = 0;
         if (m0 && m1) {
             const unsigned p1 = __ballot_sync(kFull, n1 && (!n0 || d1 < d0));
             const bool first1 = 2 * __popc(p1) > __popc(m0 | m1);
             next = first1 ? d.y : d.x;
+            need = first1 ? m1 : m0;
             const int ref = (node << 1) | (first1 ? 0 : 1);
             if (sp >= kStackMax) {
                 if (lane == 0) atomicOr(err, kErrStack);
-                return;
+                break;
             }
             if (lane == (sp & 31)) {
                 if (sp < 32) stk0 = ref; else stk1 = ref;
@@ -245,24 +274,26 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
             sp++;
         } else if (m0) {
             next = d.x;
+            need = m0;
         } else if (m1) {
             next = d.y;
-        } else {
-            have_next = false;
-            next = 0;
+            need = m1;
         }
         // ---- resolve: scan buckets, pop until an internal node to expand --
         while (true) {
-            if (have_next) {
+            if (need) {
                 if (next >= 0) {
                     node = next;
                     break;
                 }
-                const int b = -1 - next;
-                if (b < skip_lo || b > skip_hi) scan_bucket(T, b, qx, qy, qz, active, heap, stage, st);
-                have_next = false;
+                const int bk = -1 - next;
+                if (bk < skip_lo || bk > skip_hi) scan_bucket(T, bk, qx, qy, qz, active, need, heap, stage, st);
+                need = 0;
             }
-            if (sp == 0) return;
+            if (sp == 0) {
+                done = true;
+                break;
+            }
             sp--;
             const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
             const TreeNode* pn = T.nodes + (ref >> 1);
@@ -281,12 +312,11 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                 child = __ldg(&pn->d.y);
             }
             const float dd = box_dist2(qx, qy, qz, lx, ly, lz, hx, hy, hz);
-            if (__any_sync(kFull, active && dd <= heap.tau())) {
-                next = child;
-                have_next = true;
-            }
+            need = __ballot_sync(kFull, active && dd <= heap.tau());
+            next = child;
         }
     }
+    heap.finish();
 }
 
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
