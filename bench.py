@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--points", type=int, default=10_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--bucket", type=int, default=32, help="LBVH bucket size (tuning)")
+    ap.add_argument("--seed-radius", type=int, default=1, help="seed buckets on each side (tuning)")
     return ap.parse_args()
 
 
@@ -210,7 +212,8 @@ def run_gpu(args):
     pts = workload(args.points)
     n = len(pts)
     d_pts = torch.from_numpy(pts).to(f"cuda:{local}")
-    s = lvr2_gb300.Surface(d_pts, kn=KN, ki=KI, kd=KD, nem=NEM, adaptive=True, flip_point=None, device=local)
+    s = lvr2_gb300.Surface(d_pts, kn=KN, ki=KI, kd=KD, nem=NEM, adaptive=True, flip_point=None, device=local,
+                           bucket=args.bucket, seed_radius=args.seed_radius)
 
     def step():
         s.set_points(d_pts)
@@ -293,7 +296,8 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "normals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(n, {"parallelism": "replicas" if world > 1 else "single"}),
+        "config": config(n, {"parallelism": "replicas" if world > 1 else "single", "bucket": args.bucket,
+                             "seed_radius": args.seed_radius}),
         "stages_ms": {"lbvh_build": float(stage[0]), "normals": normals_ms, "interpolation": float(stage[2]),
                       "grid_build": float(stage[3]), "signed_distance": sdf_ms, "culling": float(stage[5]),
                       "marching_cubes": float(stage[6])},

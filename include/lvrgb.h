@@ -64,6 +64,7 @@ typedef struct lvrgb_surface_config {
     int32_t bucket;        /* LBVH bucket size 1..32 (0 = 32) */
     float gap_threshold;   /* relative eigengap below which PCA solves in FP64 (0 = 1e-3) */
     int32_t device;        /* CUDA device ordinal */
+    int32_t seed_radius;   /* Morton-neighbour buckets scanned on each side of a search's start (0 = 1) */
 } lvrgb_surface_config;
 
 /* Fills the lvr2_reconstruct defaults: kn 10, ki 10, kd 5, nem 0, adaptive,

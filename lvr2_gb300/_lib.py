@@ -42,6 +42,7 @@ class SurfaceConfig(ctypes.Structure):
         ("kn", ctypes.c_int32), ("ki", ctypes.c_int32), ("kd", ctypes.c_int32), ("nem", ctypes.c_int32),
         ("adaptive", ctypes.c_int32), ("flip_set", ctypes.c_int32), ("flip", ctypes.c_float * 3),
         ("bucket", ctypes.c_int32), ("gap_threshold", ctypes.c_float), ("device", ctypes.c_int32),
+        ("seed_radius", ctypes.c_int32),
     ]
 
 

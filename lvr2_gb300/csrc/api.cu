@@ -226,6 +226,7 @@ void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, c
     const float* dx = stage_in(s->ws, "api.xyz", xyz, size_t(n) * 3, on_device, st);
     record(s, 0, st);
     lbvh_build(dx, int(n), s->cfg.bucket, s->ws, "tree", s->T, s->d_box, s->d_err, st);
+    s->T.seed_radius = s->cfg.seed_radius;
     record(s, 1, st);
     s->ev_used[0] = true;
     float h[6] = {0, 0, 0, 0, 0, 0};
@@ -266,6 +267,7 @@ void lvrgb_surface_config_default(lvrgb_surface_config* cfg) {
     cfg->bucket = 32;
     cfg->gap_threshold = 1e-3f;
     cfg->device = 0;
+    cfg->seed_radius = 1;
 }
 
 lvrgb_status lvrgb_surface_create(const lvrgb_surface_config* cfg, const float* xyz, int64_t n, int32_t on_device,
@@ -280,11 +282,14 @@ lvrgb_status lvrgb_surface_create(const lvrgb_surface_config* cfg, const float* 
         require(cfg->kn > 0 && cfg->ki >= 0 && cfg->kd > 0, LVRGB_ERR_INVALID_ARGUMENT, "kn, kd must be > 0, ki >= 0");
         check_nem(cfg->nem);
         require(cfg->bucket >= 0 && cfg->bucket <= 32, LVRGB_ERR_INVALID_ARGUMENT, "bucket must be in 0..32");
+        require(cfg->seed_radius >= 0 && cfg->seed_radius <= 16, LVRGB_ERR_INVALID_ARGUMENT,
+                "seed_radius must be in 0..16");
         DeviceScope dev(cfg->device);
         cudaStream_t st = as_stream(stream);
         s = new lvrgb_surface_s();
         s->cfg = *cfg;
         if (s->cfg.bucket == 0) s->cfg.bucket = 32;
+        if (s->cfg.seed_radius == 0) s->cfg.seed_radius = 1;
         s->device = cfg->device;
         s->d_box = s->ws.get<float>("api.box", 8);
         s->d_err = s->ws.get<int>("api.err", 4);

@@ -58,7 +58,7 @@ class Surface:
     """
 
     def __init__(self, points, kn=10, ki=10, kd=5, nem=0, adaptive=True, flip_point=(0.0, 0.0, 0.0),
-                 bucket=32, gap_threshold=1e-3, device=0, stream=None):
+                 bucket=32, gap_threshold=1e-3, device=0, stream=None, seed_radius=1):
         L = _lib.load()
         cfg = SurfaceConfig()
         L.lvrgb_surface_config_default(ctypes.byref(cfg))
@@ -72,6 +72,7 @@ class Surface:
         cfg.bucket = int(bucket)
         cfg.gap_threshold = float(gap_threshold)
         cfg.device = int(device)
+        cfg.seed_radius = int(seed_radius)
         pts, on_dev = _f32x3(points)
         self._h = ctypes.c_void_p()
         self._stream = _stream_ptr(stream)
