@@ -133,7 +133,8 @@ lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on
 /* Counters of the last lvrgb_calculate_normals: out[0..4] planes fitted in
  * search round 1..5, out[5] PCA eigensolves done in FP64, out[8] LBVH
  * buckets scanned (per 32-query warp), out[9] tree nodes expanded (per warp),
- * out[10] heap insertions (per query); other entries 0. */
+ * out[10] heap insertions (per query), out[11] 32-candidate chunks scanned
+ * (per warp); other entries 0. */
 lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]);
 
 /* Batched k-nearest-neighbour search: SearchTree::kSearch / kSearchParallel

@@ -49,7 +49,7 @@ constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can
 // Traversal counters of one warp (nodes, buckets) and one lane (heap
 // insertions); kernels that do not report them let the compiler drop them.
 struct TravStats {
-    unsigned nodes = 0, buckets = 0, pushes = 0;
+    unsigned nodes = 0, buckets = 0, chunks = 0, pushes = 0;
 };
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
@@ -123,64 +123,75 @@ struct LaneHeap {
     __device__ __forceinline__ unsigned long long at(int s) const { return h[s * 32]; }
 };
 
-// Scans one bucket (<= 32 points) for the lanes in `need` (lanes whose
-// k-th bound reaches the bucket's box).  The bucket is staged with NaN
-// padding, one point per lane and in shared memory.  When many lanes need it,
-// every needing lane tests all 32 points (broadcast loads, independent
-// straight-line code); when few do, the warp is transposed: for each needing
-// lane the 32 lanes test its query against their own point and a ballot hands
-// the acceptance mask to the owner.  Both forms evaluate the same dist2
-// expression, so the accepted sets are identical.  Accepted candidates then
-// go through the heap, re-tested against the shrinking bound.
-__device__ __forceinline__ void scan_bucket(const Lbvh& T, int b, float qx, float qy, float qz, bool active,
-                                            unsigned need, LaneHeap& heap, float4* stage, TravStats& st) {
-    st.buckets++;
+// Per-warp candidate buffer (64 float4 in shared memory, NaN padded) and the
+// warp's query box.  Bucket points pass a cheap warp-level filter (one point
+// per lane: distance to the box of the warp's queries against the largest
+// k-th bound of the warp, a conservative test) and are compacted into the
+// buffer; every 32 buffered candidates are scanned by all lanes with their
+// own exact bound.
+struct WarpCand {
+    float4* buf;
+    int count;  // warp-uniform
+    float lo[3], hi[3];
+};
+
+// Scans buf[0..32) for every lane (entries past `count` are NaN and never
+// accepted), pushes accepted candidates, and drops the scanned entries.
+__device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, float qz, bool active, LaneHeap& heap,
+                                            TravStats& st) {
     const int lane = threadIdx.x & 31;
+    st.chunks++;
+    if (active) {
+        const float tau = heap.tau();
+        unsigned mask = 0;
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const float4 c = W.buf[j];
+            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+            mask |= (d2 <= tau ? 1u : 0u) << j;
+        }
+        while (mask) {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const float4 c = W.buf[j];
+            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+            const unsigned long long key = make_key(d2, __float_as_uint(c.w));
+            if (key < heap.top) {
+                heap.push(key);
+                st.pushes++;
+            }
+        }
+    }
+    __syncwarp();
+    const float nan = __int_as_float(0x7fffffff);
+    const float4 tail = W.buf[32 + lane];
+    __syncwarp();
+    W.buf[lane] = tail;
+    W.buf[32 + lane] = make_float4(nan, nan, nan, 0.0f);
+    __syncwarp();
+    W.count = W.count > 32 ? W.count - 32 : 0;
+}
+
+// Adds the points of bucket b that may be within some lane's bound.
+__device__ __forceinline__ void add_bucket(const Lbvh& T, int b, WarpCand& W, float qx, float qy, float qz,
+                                           bool active, LaneHeap& heap, TravStats& st) {
+    const int lane = threadIdx.x & 31;
+    st.buckets++;
     const int first = b * T.bucket;
     int cnt = T.n - first;
     if (cnt > T.bucket) cnt = T.bucket;
-    const float nan = __int_as_float(0x7fffffff);
-    const float4 mine = lane < cnt ? __ldg(T.pts + first + lane) : make_float4(nan, nan, nan, 0.0f);
-    stage[lane] = mine;
-    __syncwarp();
-    const float tau = heap.tau();
-    unsigned mask = 0;
-    if (__popc(need) >= 20) {
-        if (active) {
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const float4 c = stage[j];
-                const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-                mask |= (d2 <= tau ? 1u : 0u) << j;
-            }
-        }
-    } else {
-        unsigned rest = need;
-        while (rest) {
-            const int i = __ffs(rest) - 1;
-            rest &= rest - 1;
-            const float x = __shfl_sync(kFull, qx, i);
-            const float y = __shfl_sync(kFull, qy, i);
-            const float z = __shfl_sync(kFull, qz, i);
-            const float t = __shfl_sync(kFull, tau, i);
-            const float d2 = dist2(x, y, z, mine.x, mine.y, mine.z);
-            const unsigned m = __ballot_sync(kFull, d2 <= t);
-            if (lane == i) mask = m;
-        }
-        if (!active) mask = 0;
+    const float tmax = __uint_as_float(__reduce_max_sync(kFull, active ? __float_as_uint(heap.tau()) : 0u));
+    bool keep = false;
+    float4 p = make_float4(0, 0, 0, 0);
+    if (lane < cnt) {
+        p = __ldg(T.pts + first + lane);
+        keep = box_dist2(p.x, p.y, p.z, W.lo[0], W.lo[1], W.lo[2], W.hi[0], W.hi[1], W.hi[2]) <= tmax;
     }
-    while (mask) {
-        const int j = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const float4 c = stage[j];
-        const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-        const unsigned long long key = make_key(d2, __float_as_uint(c.w));
-        if (key < heap.top) {
-            heap.push(key);
-            st.pushes++;
-        }
-    }
+    const unsigned m = __ballot_sync(kFull, keep);
+    if (keep) W.buf[W.count + __popc(m & ((1u << lane) - 1u))] = p;
+    W.count += __popc(m);
     __syncwarp();
+    if (W.count >= 32) flush_chunk(W, qx, qy, qz, active, heap, st);
 }
 
 // Bucket whose first Morton code is the largest <= the code of (x, y, z):
@@ -218,9 +229,31 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         heap.finish();
         return;
     }
-    const unsigned all = __ballot_sync(kFull, active);
+    // warp query box and an empty, NaN-padded candidate buffer
+    WarpCand W;
+    W.buf = stage;
+    W.count = 0;
+    {
+        const float nan = __int_as_float(0x7fffffff);
+        stage[lane] = make_float4(nan, nan, nan, 0.0f);
+        stage[32 + lane] = make_float4(nan, nan, nan, 0.0f);
+        const float big = FLT_MAX;
+        float v[6] = {active ? qx : big, active ? qy : big, active ? qz : big,
+                      active ? qx : -big, active ? qy : -big, active ? qz : -big};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                v[a] = fminf(v[a], __shfl_xor_sync(kFull, v[a], o));
+                v[3 + a] = fmaxf(v[3 + a], __shfl_xor_sync(kFull, v[3 + a], o));
+            }
+        }
+        for (int a = 0; a < 3; a++) { W.lo[a] = v[a]; W.hi[a] = v[3 + a]; }
+        __syncwarp();
+    }
     if (T.nbuckets == 1) {
-        scan_bucket(T, 0, qx, qy, qz, active, all, heap, stage, st);
+        add_bucket(T, 0, W, qx, qy, qz, active, heap, st);
+        if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
         heap.finish();
         return;
     }
@@ -228,7 +261,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     if (seed >= 0) {
         skip_lo = max(0, seed - T.seed_radius);
         skip_hi = min(T.nbuckets - 1, seed + T.seed_radius);
-        for (int b = skip_lo; b <= skip_hi; b++) scan_bucket(T, b, qx, qy, qz, active, all, heap, stage, st);
+        for (int b = skip_lo; b <= skip_hi; b++) add_bucket(T, b, W, qx, qy, qz, active, heap, st);
     }
     int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
     int sp = 0;
@@ -287,7 +320,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                     break;
                 }
                 const int bk = -1 - next;
-                if (bk < skip_lo || bk > skip_hi) scan_bucket(T, bk, qx, qy, qz, active, need, heap, stage, st);
+                if (bk < skip_lo || bk > skip_hi) add_bucket(T, bk, W, qx, qy, qz, active, heap, st);
                 need = 0;
             }
             if (sp == 0) {
@@ -316,6 +349,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
             next = child;
         }
     }
+    if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
     heap.finish();
 }
 
@@ -325,7 +359,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     knn_traverse(T, qx, qy, qz, active, heap, stage, err, st, seed);
 }
 
-// Shared-memory carving of a kNN kernel block: kWarps stage areas of 32
+// Shared-memory carving of a kNN kernel block: kWarps candidate buffers of 64
 // float4, then (when gheap == nullptr) kWarps lane-interleaved heaps of K keys.
 // With a global heap buffer, each resident warp owns K*32 keys of it.
 struct WarpCtx {
@@ -336,11 +370,11 @@ template <int kWarps>
 __device__ __forceinline__ WarpCtx warp_ctx(unsigned char* smem, unsigned long long* gheap, int K) {
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpCtx c;
-    c.stage = reinterpret_cast<float4*>(smem) + wib * 32;
+    c.stage = reinterpret_cast<float4*>(smem) + wib * 64;
     if (gheap)
         c.heap = gheap + (size_t(blockIdx.x) * kWarps + wib) * size_t(K) * 32 + lane;
     else
-        c.heap = reinterpret_cast<unsigned long long*>(smem + kWarps * 32 * sizeof(float4)) +
+        c.heap = reinterpret_cast<unsigned long long*>(smem + kWarps * 64 * sizeof(float4)) +
                  size_t(wib) * K * 32 + lane;
     return c;
 }

@@ -351,6 +351,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         atomicAdd(A.stats + 8, st.buckets);
         atomicAdd(A.stats + 9, st.nodes);
         atomicAdd(A.stats + 10, pushes);
+        atomicAdd(A.stats + 11, st.chunks);
     }
 }
 
@@ -506,7 +507,7 @@ HeapPlan plan_heap(int nq, int K, Workspace& ws) {
     HeapPlan p;
     const int tiles = (nq + 31) / 32;
     const int need_blocks = std::max(1, (tiles + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    const size_t stage = size_t(kWarpsPerBlock) * 32 * sizeof(float4);
+    const size_t stage = size_t(kWarpsPerBlock) * 64 * sizeof(float4);
     if (K <= kSmemHeapMax) {
         p.smem = stage + size_t(kWarpsPerBlock) * K * 32 * sizeof(unsigned long long);
         p.blocks = need_blocks;
