@@ -7,7 +7,7 @@
 #include <stdexcept>
 #include <string>
 
-#include "../../include/lvrgb.h"
+#include "lvrgb.h"
 #include "grid.h"
 #include "lbvh_build.h"
 #include "surface.h"
