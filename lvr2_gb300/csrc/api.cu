@@ -362,13 +362,19 @@ lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
         cudaStream_t st = as_stream(stream);
         LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
         NormalsConfig c = normals_config(s);
+        // The interpolation's kNN(ki) is the first ki of the estimation's
+        // kNN(k >= 2kn): keep those lists instead of searching again.
+        const bool lists = s->cfg.ki > 0 && s->cfg.ki <= 2 * s->cfg.kn;
+        uint32_t* nbr = lists ? s->ws.get<uint32_t>("api.nbr", size_t(s->T.n) * size_t(s->cfg.ki)) : nullptr;
         record(s, 2, st);
-        compute_normals(s->T, c, s->raw_normals, s->kused, s->ws, s->d_err, s->d_stats, st);
+        compute_normals(s->T, c, s->raw_normals, s->kused, s->ws, s->d_err, s->d_stats, st, nbr, s->cfg.ki);
         record(s, 3, st);
         s->ev_used[1] = true;
         s->has_raw = true;
         record(s, 4, st);
-        if (s->cfg.ki > 0)
+        if (lists)
+            interpolate_from_lists(s->T.n, s->cfg.ki, nbr, s->raw_normals, s->normals, st);
+        else if (s->cfg.ki > 0)
             interpolate_normals(s->T, s->cfg.ki, s->raw_normals, s->normals, s->ws, s->d_err, st);
         record(s, 5, st);
         s->ev_used[2] = true;

@@ -138,6 +138,8 @@ struct NormalsArgs {
     unsigned long long* gheap;
     int* err;
     uint32_t* stats;
+    uint32_t* nbr;  // optional: first ki neighbours (Morton positions), column s at nbr[s * n]
+    int ki;
 };
 
 // BaseVector::normalize with IEEE operations (null vector unchanged).
@@ -305,7 +307,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
         bool retry = false;
         if (active) {
-            if (A.T.n < A.K) heap.sort_ascending();  // real entries first
+            // Ascending order puts the real entries first (fewer points than K)
+            // and gives the interpolation its ki nearest in lvr2's order.
+            if (A.T.n < A.K || A.nbr) heap.sort_ascending();
             NbrPass P;
             neighbour_pass<kNem>(A.T, heap, cnt, q, P);
             bool fit = true;
@@ -330,6 +334,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
                 }
                 A.normals[pos] = make_float4(n[0], n[1], n[2], 0.0f);
                 if (A.kused) A.kused[pos] = A.K;
+                if (A.nbr) {
+                    // kNN(ki) of the interpolation = the first ki of this kNN(K >= ki)
+                    for (int j = 0; j < A.ki; j++)
+                        A.nbr[size_t(j) * A.T.n + pos] = j < cnt ? __ldg(A.T.inv + key_idx(heap.at(j))) : 0xffffffffu;
+                }
                 if (fp64) atomicAdd(A.stats + 5, 1u);
             } else {
                 retry = true;
@@ -353,6 +362,26 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         atomicAdd(A.stats + 10, pushes);
         atomicAdd(A.stats + 11, st.chunks);
     }
+}
+
+// interpolateSurfaceNormals from stored neighbour lists: the same sums as
+// interpolate_kernel, in the same order, without a second search.
+__global__ void interpolate_lists_kernel(const float4* __restrict__ in, const uint32_t* __restrict__ nbr, int n,
+                                         int ki, float4* __restrict__ out) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n) return;
+    const float4 m = in[pos];
+    float x = m.x, y = m.y, z = m.z;
+    const int cnt = min(ki, n);
+#pragma unroll 4
+    for (int s = 0; s < cnt; s++) {
+        const float4 nj = __ldg(in + __ldg(nbr + size_t(s) * n + pos));
+        x = __fadd_rn(x, nj.x);
+        y = __fadd_rn(y, nj.y);
+        z = __fadd_rn(z, nj.z);
+    }
+    normalize_ieee(x, y, z);
+    out[pos] = make_float4(x, y, z, 0.0f);
 }
 
 struct InterpArgs {
@@ -521,7 +550,7 @@ HeapPlan plan_heap(int nq, int K, Workspace& ws) {
 }
 
 void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
-                     int* d_err, uint32_t* d_stats, cudaStream_t s) {
+                     int* d_err, uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki) {
     const int n = T.n;
     if (n == 0) return;
     uint32_t* lists[2] = {ws.get<uint32_t>("normals.listA", size_t(n)), ws.get<uint32_t>("normals.listB", size_t(n))};
@@ -553,6 +582,8 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.retry_count = counter;
         A.err = d_err;
         A.stats = d_stats;
+        A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
+        A.ki = ki;
         HeapPlan P = plan_heap(nq, K, ws);
         A.gheap = P.gheap;
         const int threads = kWarpsPerBlock * 32;
@@ -597,6 +628,12 @@ void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, W
     A.gheap = P.gheap;
     set_smem(interpolate_kernel, P.smem);
     interpolate_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s) {
+    if (n == 0) return;
+    interpolate_lists_kernel<<<ceil_div(n, 256), 256, 0, s>>>(in, nbr, n, ki, out);
     LVRGB_LAUNCH_CHECK();
 }
 

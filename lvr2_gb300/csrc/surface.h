@@ -21,9 +21,15 @@ struct NormalsConfig {
 constexpr int kNormalStats = 16;
 
 // Normals in Morton order (float4, w = 0).  kused (optional, Morton order)
-// receives the k of the search whose neighbourhood was used.
+// receives the k of the search whose neighbourhood was used.  When nbr is
+// given and ki <= 2 * kn, every point's ki nearest neighbours (Morton
+// positions, ascending (d2, index)) are written column-wise to nbr[s * n + pos]
+// for interpolate_from_lists.
 void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
-                     int* d_err, uint32_t* d_stats, cudaStream_t s);
+                     int* d_err, uint32_t* d_stats, cudaStream_t s, uint32_t* nbr = nullptr, int ki = 0);
+
+// Interpolation from the neighbour lists written by compute_normals.
+void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s);
 
 // out_i = normalize(in_i + sum_{j in kNN_ki(p_i)} in_j), Morton order.
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,

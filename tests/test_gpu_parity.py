@@ -260,3 +260,19 @@ def test_status_codes_on_gpu(gb):
         with pytest.raises(gb.LvrgbError) as e:
             s.reconstruct(voxelsize=1e-9)
         assert e.value.status == 1  # grid extent beyond 2^20 cells per axis
+
+
+@pytest.mark.parametrize("kn,ki", [(10, 10), (10, 20), (5, 20), (3, 7)])
+def test_calculate_normals_interpolation_bit_exact(gb, oracle_mod, kn, ki):
+    """calculateSurfaceNormals with interpolation: the GPU interpolates from
+    the estimation's neighbour lists when ki <= 2kn and searches again
+    otherwise; either way the result equals the oracle's interpolation of the
+    GPU's raw normals bit for bit."""
+    P = cloud("scan")
+    o = oracle_mod.OracleSurface(P)
+    with gb.Surface(P, kn=kn, ki=ki, nem=3, flip_point=(0, 0, 0)) as s:
+        s.calculate_normals()
+        raw, _ = s.raw_normals()
+        final = s.normals()
+    ref = o.interpolate(raw, ki)
+    assert np.array_equal(final, ref, equal_nan=True)
