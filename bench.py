@@ -309,7 +309,8 @@ def run_gpu(args):
                    "normals_buckets_per_warp": float(stats[8]) / max(1.0, n / 32.0),
                    "normals_nodes_per_warp": float(stats[9]) / max(1.0, n / 32.0),
                    "normals_heap_pushes_per_query": float(stats[10]) / max(1.0, n),
-                   "normals_chunks_per_warp": float(stats[11]) / max(1.0, n / 32.0)},
+                   "normals_chunks_per_warp": float(stats[11]) / max(1.0, n / 32.0),
+                   "normals_push_rounds_per_warp": float(stats[12]) / max(1.0, n / 32.0)},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": int(dom["bytes"]), "traffic": None},

@@ -49,7 +49,7 @@ constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can
 // Traversal counters of one warp (nodes, buckets) and one lane (heap
 // insertions); kernels that do not report them let the compiler drop them.
 struct TravStats {
-    unsigned nodes = 0, buckets = 0, chunks = 0, pushes = 0;
+    unsigned nodes = 0, buckets = 0, chunks = 0, pushes = 0, rounds = 0;
 };
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
@@ -141,25 +141,26 @@ __device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, flo
                                             TravStats& st) {
     const int lane = threadIdx.x & 31;
     st.chunks++;
+    unsigned mask = 0;
     if (active) {
         const float tau = heap.tau();
-        unsigned mask = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) {
             const float4 c = W.buf[j];
             const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
             mask |= (d2 <= tau ? 1u : 0u) << j;
         }
-        while (mask) {
-            const int j = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const float4 c = W.buf[j];
-            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-            const unsigned long long key = make_key(d2, __float_as_uint(c.w));
-            if (key < heap.top) {
-                heap.push(key);
-                st.pushes++;
-            }
+    }
+    st.rounds += __reduce_max_sync(kFull, unsigned(__popc(mask)));
+    while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const float4 c = W.buf[j];
+        const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+        const unsigned long long key = make_key(d2, __float_as_uint(c.w));
+        if (key < heap.top) {
+            heap.push(key);
+            st.pushes++;
         }
     }
     __syncwarp();

@@ -356,11 +356,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     }
     unsigned pushes = st.pushes;
     for (int o = 16; o > 0; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
+
     if (lane == 0 && st.nodes) {
         atomicAdd(A.stats + 8, st.buckets);
         atomicAdd(A.stats + 9, st.nodes);
         atomicAdd(A.stats + 10, pushes);
         atomicAdd(A.stats + 11, st.chunks);
+        atomicAdd(A.stats + 12, st.rounds);
     }
 }
 
