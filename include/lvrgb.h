@@ -232,6 +232,28 @@ lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]);
  * no lvr2 counterpart). */
 lvrgb_status lvrgb_kernel_launches(uint64_t* out);
 
+/* k nearest neighbours of nq queries among n points WITHOUT ANY DEVICE
+ * ALLOCATION.  No counterpart in lvr2: it exists for callers that cannot
+ * call cudaMalloc during a call (real-time loops or driver callbacks where an
+ * allocation would synchronize the device, hosts that give a library a fixed
+ * device-memory budget, plugins whose host owns every allocation).
+ *  - points (n x 3), queries (nq x 3), idx and dist (nq x k) are DEVICE
+ *    pointers on the current device; results as lvrgb_knn (ascending,
+ *    0xffffffff / +inf padding when n < k).
+ *  - Limits: 1 <= n <= 65536, 0 <= nq <= 65536, 1 <= k <= 96; larger inputs
+ *    are rejected with LVRGB_ERR_INVALID_ARGUMENT.  Use lvrgb_surface_create
+ *    and lvrgb_knn for anything bigger.
+ *  - Scratch is one 8 MiB static device array that every GPU loading this
+ *    library holds until the process exits.  The first call on a device looks
+ *    up its address (cudaGetSymbolAddress); make that first call before any
+ *    stream capture.
+ *  - All calls share the array: calls that overlap on the GPU (other streams,
+ *    other host threads) race and must be serialized by the caller.
+ *  - Synchronizes `stream` (one small read of the point bounding box and of
+ *    the error flag). */
+lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float* queries, int64_t nq, int32_t k,
+                                     uint32_t* idx, float* dist, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* lvrgb_last_error(void);
 

@@ -26,7 +26,7 @@ EXPORTS = [
     "lvrgb_surface_num_points", "lvrgb_calculate_normals", "lvrgb_get_normals", "lvrgb_get_raw_normals",
     "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance", "lvrgb_grid_distances",
     "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
-    "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches",
+    "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches", "lvrgb_knn_small_noalloc",
     "lvrgb_last_error", "lvrgb_version",
 ]
 
@@ -97,6 +97,7 @@ def load(path=None):
     L.lvrgb_surface_set_points.argtypes = [vp, vp, i64, i32, vp]
     L.lvrgb_surface_timings.argtypes = [vp, vp]
     L.lvrgb_kernel_launches.argtypes = [vp]
+    L.lvrgb_knn_small_noalloc.argtypes = [vp, i64, vp, i64, i32, vp, vp, vp]
     L.lvrgb_last_error.restype = ctypes.c_char_p
     L.lvrgb_version.restype = ctypes.c_char_p
     for name in EXPORTS:

@@ -4,12 +4,14 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
 #include "lvrgb.h"
 #include "grid.h"
 #include "lbvh_build.h"
+#include "primitives.cuh"
 #include "surface.h"
 
 using namespace lvrgb;
@@ -729,6 +731,126 @@ lvrgb_status lvrgb_kernel_launches(uint64_t* out) {
     if (!out) return fail(LVRGB_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = g_launches.load();
     return LVRGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free kNN for small point sets (lvrgb_knn_small_noalloc).
+//
+// Some callers must not allocate device memory during a call: code running
+// inside a real-time loop or a driver callback where cudaMalloc/cudaFree would
+// synchronize the device and stall other work, hosts that hand a library a
+// fixed device-memory budget up front, and plugins whose host process owns
+// every allocation.  For them this entry point takes its scratch (sorted
+// points, tree, sort buffers, packed queries) from one file-scope device
+// array of kNoAllocBytes that every GPU loading this library reserves until
+// the process exits.  Its device address is looked up once per device with
+// cudaGetSymbolAddress (the host-side name of a __device__ array is not a
+// device address and must never be passed to a kernel).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocBytes = size_t(8) << 20;
+constexpr int64_t kNoAllocMaxPoints = 65536;
+constexpr int64_t kNoAllocMaxQueries = 65536;
+constexpr int kNoAllocMaxK = kSmemHeapMax;
+constexpr int kNoAllocBucket = 32;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 128;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (set-up on the
+// first call per device).
+unsigned char* noalloc_scratch() {
+    int dev = 0;
+    LVRGB_CUDA(cudaGetDevice(&dev));
+    require(dev >= 0 && dev < kMaxDevices, LVRGB_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        LVRGB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+
+struct Carver {
+    unsigned char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        T* p = reinterpret_cast<T*>(base + off);
+        off += (count * sizeof(T) + 255) & ~size_t(255);
+        if (off > kNoAllocBytes) throw ApiError{LVRGB_ERR_OUT_OF_MEMORY, "allocation-free scratch exhausted"};
+        return p;
+    }
+};
+
+__global__ void pack_queries_kernel(const float* __restrict__ q, int nq, float4* __restrict__ qs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    qs[i] = make_float4(q[3 * size_t(i)], q[3 * size_t(i) + 1], q[3 * size_t(i) + 2], __uint_as_float(uint32_t(i)));
+}
+
+}  // namespace
+
+extern "C" {
+
+lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float* queries, int64_t nq, int32_t k,
+                                     uint32_t* idx, float* dist, void* stream) {
+    return guarded([&] {
+        require(n >= 1 && n <= kNoAllocMaxPoints, LVRGB_ERR_INVALID_ARGUMENT,
+                "lvrgb_knn_small_noalloc: point count must be in 1..65536");
+        require(nq >= 0 && nq <= kNoAllocMaxQueries, LVRGB_ERR_INVALID_ARGUMENT,
+                "lvrgb_knn_small_noalloc: query count must be in 0..65536");
+        require(k >= 1 && k <= kNoAllocMaxK, LVRGB_ERR_INVALID_ARGUMENT,
+                "lvrgb_knn_small_noalloc: k must be in 1..96");
+        require(points && (nq == 0 || (queries && idx && dist)), LVRGB_ERR_INVALID_ARGUMENT,
+                "lvrgb_knn_small_noalloc: NULL array");
+        cudaStream_t st = as_stream(stream);
+        Carver C{noalloc_scratch()};
+        const int np = int(n), nb = (np + kNoAllocBucket - 1) / kNoAllocBucket;
+        LbvhBuffers B;
+        B.pts = C.take<float4>(size_t(np));
+        B.inv = C.take<uint32_t>(size_t(np));
+        B.nodes = C.take<TreeNode>(size_t(nb > 1 ? nb - 1 : 1));
+        B.bkeys = C.take<uint32_t>(size_t(nb));
+        B.bparent = C.take<int>(size_t(nb));
+        B.counters = C.take<int>(size_t(nb > 1 ? nb - 1 : 1));
+        B.codes = C.take<uint32_t>(size_t(np));
+        B.codes2 = C.take<uint32_t>(size_t(np));
+        B.idx = C.take<uint32_t>(size_t(np));
+        B.idx2 = C.take<uint32_t>(size_t(np));
+        B.sort_tmp = C.take<unsigned char>(radix_sort_temp_bytes<uint32_t>(size_t(np)));
+        B.box_tmp = C.take<unsigned char>(bbox_temp_bytes(size_t(np)));
+        B.box = C.take<float>(8);
+        B.err = C.take<int>(4);
+        float4* qs = C.take<float4>(size_t(nq > 0 ? nq : 1));
+        // The array keeps the previous call's contents: clear what must start at zero.
+        LVRGB_CUDA(cudaMemsetAsync(B.err, 0, 4 * sizeof(int), st));
+        Lbvh T;
+        lbvh_build_into(points, np, kNoAllocBucket, B, T, st);
+        // Morton frame of the tree for the search seeds: one 24-byte read of the box.
+        float h[6];
+        LVRGB_CUDA(cudaMemcpyAsync(h, B.box, sizeof(h), cudaMemcpyDeviceToHost, st));
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+        const float ext = std::max(std::max(h[3] - h[0], h[4] - h[1]), h[5] - h[2]);
+        for (int a = 0; a < 3; a++) T.mn[a] = h[a];
+        T.scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+        T.seed_radius = 1;
+        if (nq == 0) return;
+        pack_queries_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(queries, int(nq), qs);
+        LVRGB_LAUNCH_CHECK();
+        knn_rows_smem(T, qs, int(nq), k, idx, dist, nullptr, B.err, st);
+        int herr = 0;
+        LVRGB_CUDA(cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+        require(herr == 0, LVRGB_ERR_KERNEL, "kNN traversal reported an internal limit");
+    });
 }
 
 const char* lvrgb_last_error(void) { return g_last_error.c_str(); }

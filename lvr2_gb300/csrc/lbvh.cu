@@ -196,4 +196,37 @@ void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::s
     LVRGB_LAUNCH_CHECK();
 }
 
+void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, Lbvh& T, cudaStream_t s) {
+    if (bucket < 1 || bucket > 32) bucket = 32;
+    T.n = n;
+    T.bucket = bucket;
+    T.nbuckets = n > 0 ? (n + bucket - 1) / bucket : 0;
+    T.pts = B.pts;
+    T.inv = B.inv;
+    T.nodes = B.nodes;
+    T.bkeys = B.bkeys;
+    if (n == 0) return;
+    const int nb = T.nbuckets;
+    bbox_float3(xyz, size_t(n), 3, B.box, B.box_tmp, s);
+    morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, B.box, B.codes, B.idx);
+    LVRGB_LAUNCH_CHECK();
+    bool alt = radix_sort_pairs<uint32_t>(B.codes, B.idx, B.codes2, B.idx2, size_t(n), 0, 30, B.sort_tmp, s);
+    const uint32_t* scodes = alt ? B.codes2 : B.codes;
+    const uint32_t* sidx = alt ? B.idx2 : B.idx;
+    gather_sorted_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, sidx, n, B.pts, B.inv);
+    LVRGB_LAUNCH_CHECK();
+    bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(scodes, bucket, nb, B.bkeys);
+    LVRGB_LAUNCH_CHECK();
+    if (nb == 1) {
+        LVRGB_CUDA(cudaMemsetAsync(B.bparent, 0xff, sizeof(int), s));
+        return;
+    }
+    LVRGB_CUDA(cudaMemsetAsync(B.counters, 0, sizeof(int) * size_t(nb - 1), s));
+    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(scodes, bucket, nb, B.nodes, B.bparent);
+    LVRGB_LAUNCH_CHECK();
+    bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(B.pts, n, bucket, nb, B.nodes, B.bparent, B.counters,
+                                                                 B.err);
+    LVRGB_LAUNCH_CHECK();
+}
+
 }  // namespace lvrgb

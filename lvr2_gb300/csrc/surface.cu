@@ -2,6 +2,7 @@
 // calculateSurfaceNormals), normal interpolation, kNN rows and
 // getInterpolatedNormal, all on the warp-cooperative LBVH traversal.
 #include <algorithm>
+#include <stdexcept>
 
 #include "primitives.cuh"
 #include "surface.h"
@@ -671,6 +672,31 @@ void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, flo
     A.gheap = P.gheap;
     set_smem(rows_kernel, P.smem);
     rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void knn_rows_smem(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
+                   int* d_err, cudaStream_t s) {
+    if (nq == 0 || k <= 0) return;
+    if (k > kSmemHeapMax) throw std::invalid_argument("k exceeds the shared-memory heap limit");
+    RowsArgs A;
+    A.T = T;
+    A.K = k;
+    A.qs = qs;
+    A.nq = nq;
+    A.idx = idx;
+    A.dist = dist;
+    A.count = count;
+    A.normals = nullptr;
+    A.nout = nullptr;
+    A.err = d_err;
+    A.gheap = nullptr;
+    const size_t smem = size_t(kWarpsPerBlock) * 64 * sizeof(float4) +
+                        size_t(kWarpsPerBlock) * size_t(k) * 32 * sizeof(unsigned long long);
+    const int tiles = (nq + 31) / 32;
+    const int blocks = (tiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    set_smem(rows_kernel, smem);
+    rows_kernel<<<blocks, kWarpsPerBlock * 32, smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }
 

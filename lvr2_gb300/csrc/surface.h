@@ -44,6 +44,11 @@ void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Worksp
 void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
               Workspace& ws, int* d_err, cudaStream_t s);
 
+// knn_rows with the heaps in shared memory only (k <= kSmemHeapMax) and no
+// workspace: allocates nothing.
+void knn_rows_smem(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
+                   int* d_err, cudaStream_t s);
+
 // PointsetSurface::getInterpolatedNormal for sorted queries; out rows float3.
 void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, const float4* qs, int nq,
                               float* out, Workspace& ws, int* d_err, cudaStream_t s);
