@@ -37,6 +37,11 @@ KN = KI = KD = 20
 VOXELSIZE = 0.005
 NEM = 3
 CPU_SAMPLE_FRACTION = 0.02
+# DRAM bytes (read + write) per unit of the two kNN kernels, from one ncu
+# capture of the 2M-point case (profiles/normals_kernel_spheres_tori_2M.md,
+# profiles/sdf_kernel_spheres_tori_2M.md); the normal kernel's traffic is
+# per-point I/O (the neighbour gathers hit L2), so it scales with the points.
+NCU_DRAM_BYTES_PER_NORMAL = (47.096576e6 + 152.642304e6) / 2_000_000
 
 
 def parse():
@@ -288,9 +293,9 @@ def run_gpu(args):
     normals_ms, sdf_ms = float(stage[1]), float(stage[4])
     if normals_ms >= sdf_ms:
         dom = {"kernel": "normals_kernel<3> (fused kNN + PCA + flip, all adaptive rounds)",
-               "bytes": nb, "ms": normals_ms}
+               "bytes": nb, "ms": normals_ms, "traffic": NCU_DRAM_BYTES_PER_NORMAL * n}
     else:
-        dom = {"kernel": "sdf_kernel (kd-nearest signed distance)", "bytes": sb, "ms": sdf_ms}
+        dom = {"kernel": "sdf_kernel (kd-nearest signed distance)", "bytes": sb, "ms": sdf_ms, "traffic": None}
     achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "normals/s", "n_gpus": world, "steps": args.steps,
@@ -313,7 +318,10 @@ def run_gpu(args):
                    "normals_push_rounds_per_warp": float(stats[12]) / max(1.0, n / 32.0)},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes": int(dom["bytes"]), "traffic": None},
+                     "algorithmic_bytes": int(dom["bytes"]),
+                     "traffic": int(dom["traffic"]) if dom["traffic"] else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2M-point capture, "
+                                       "scaled per point"},
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "e2e": e2e,
