@@ -66,6 +66,30 @@ def build(verbose=False, ptxas_info=False, jobs=None):
     return LIB
 
 
+CPP = PKG / "cpp"
+CLI = PKG / "lvr2gb_reconstruct"
+
+
+def cpp_compile(src, out, extra=()):
+    """Compiles a C++ host program against include/lvrgb.h and liblvrgb.so."""
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I", str(PKG.parent / "include"), "-I", str(CPP), str(src),
+           "-L", str(PKG), "-llvrgb", "-Wl,-rpath," + str(PKG), "-o", str(out)] + list(extra)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for %s:\n%s" % (src, r.stderr))
+    return out
+
+
+def build_cli():
+    """The lvr2gb_reconstruct command-line tool (lvr2_gb300/cpp)."""
+    src = CPP / "lvr2gb_reconstruct.cpp"
+    deps = [src, CPP / "lvr2gb.hpp", PKG.parent / "include" / "lvrgb.h", LIB]
+    if CLI.exists() and CLI.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+        return CLI
+    return cpp_compile(src, CLI)
+
+
 if __name__ == "__main__":
     build(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    build_cli()
     print(LIB)

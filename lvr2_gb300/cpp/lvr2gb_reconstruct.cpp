@@ -1,0 +1,263 @@
+// lvr2gb_reconstruct -- the reconstruction part of lvr2_reconstruct
+// (src/tools/lvr2_reconstruct/Main.cpp:238-610) on the GB300 path: read a
+// point cloud, estimate and interpolate normals, build the grid, evaluate the
+// signed distance and extract the (P)MC mesh, with lvr2_reconstruct's flag
+// names and defaults (Options.cpp:60-125).
+//
+//   lvr2gb_reconstruct scan.pts -v 10 --kn 10 --ki 10 --kd 5 --flipPoint 0 0 0
+//
+// Input: ASCII .pts/.xyz/.3d (x y z [extra columns]) or PLY with float x,y,z
+// (and nx,ny,nz, used unless --recalcNormals).  Output: binary PLY mesh
+// (triangle_mesh.ply, or --outputFile), and with --exportPointNormals the
+// points with their normals (pointnormals.ply).
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "lvr2gb.hpp"
+
+namespace {
+
+struct Options {
+    std::string input;
+    std::string output = "triangle_mesh.ply";
+    float voxelsize = 10.0f;
+    int intersections = -1;
+    std::string pcm = "LVR2";
+    int nem = 0;
+    std::string decomposition = "PMC";
+    bool extrude = true;
+    int kd = 5, ki = 10, kn = 10;
+    bool flip_set = false;
+    float flip[3] = {0, 0, 0};
+    bool recalc = false;
+    bool export_normals = false;
+    int device = 0;
+};
+
+void usage() {
+    std::puts(
+        "usage: lvr2gb_reconstruct <inputFile> [--voxelsize|-v F] [--intersections|-i N] [--pcm|-p NAME]\n"
+        "       [--nem 0|2|3] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
+        "       [--flipPoint X Y Z] [--recalcNormals|-r] [--exportPointNormals|-e] [--outputFile PATH]\n"
+        "       [--useGPU] [--threads N] [--device N]");
+}
+
+Options parse(int argc, char** argv) {
+    Options o;
+    auto need = [&](int& i, int count) {
+        if (i + count >= argc) {
+            usage();
+            std::exit(2);
+        }
+    };
+    for (int i = 1; i < argc; i++) {
+        std::string a = argv[i];
+        if (a == "--help" || a == "-h") {
+            usage();
+            std::exit(0);
+        } else if (a == "--voxelsize" || a == "-v") {
+            need(i, 1); o.voxelsize = std::stof(argv[++i]);
+        } else if (a == "--intersections" || a == "-i") {
+            need(i, 1); o.intersections = std::stoi(argv[++i]);
+        } else if (a == "--pcm" || a == "-p") {
+            need(i, 1); o.pcm = argv[++i];
+        } else if (a == "--nem") {
+            need(i, 1); o.nem = std::stoi(argv[++i]);
+        } else if (a == "--decomposition" || a == "-d") {
+            need(i, 1); o.decomposition = argv[++i];
+        } else if (a == "--noExtrusion") {
+            o.extrude = false;
+        } else if (a == "--kd") {
+            need(i, 1); o.kd = std::stoi(argv[++i]);
+        } else if (a == "--ki") {
+            need(i, 1); o.ki = std::stoi(argv[++i]);
+        } else if (a == "--kn") {
+            need(i, 1); o.kn = std::stoi(argv[++i]);
+        } else if (a == "--flipPoint") {
+            need(i, 3);
+            for (int k = 0; k < 3; k++) o.flip[k] = std::stof(argv[++i]);
+            o.flip_set = true;
+        } else if (a == "--recalcNormals" || a == "-r") {
+            o.recalc = true;
+        } else if (a == "--exportPointNormals" || a == "-e") {
+            o.export_normals = true;
+        } else if (a == "--outputFile") {
+            need(i, 1); o.output = argv[++i];
+        } else if (a == "--useGPU") {
+        } else if (a == "--threads" || a == "--device") {
+            need(i, 1);
+            int v = std::stoi(argv[++i]);
+            if (a == "--device") o.device = v;
+        } else if (!a.empty() && a[0] != '-') {
+            o.input = a;
+        } else {
+            std::fprintf(stderr, "unknown option %s\n", a.c_str());
+            usage();
+            std::exit(2);
+        }
+    }
+    if (o.input.empty()) {
+        usage();
+        std::exit(2);
+    }
+    return o;
+}
+
+bool ends_with(const std::string& s, const std::string& t) {
+    return s.size() >= t.size() && s.compare(s.size() - t.size(), t.size(), t) == 0;
+}
+
+// ASCII point file: lines of >= 3 numbers; a first line with a single number
+// (point count header) is skipped.
+void read_ascii(const std::string& path, std::vector<float>& xyz) {
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("cannot open " + path);
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream ss(line);
+        float v[3];
+        if (ss >> v[0] >> v[1] >> v[2]) xyz.insert(xyz.end(), v, v + 3);
+    }
+}
+
+// PLY with vertex float properties x, y, z (and optional nx, ny, nz).
+void read_ply(const std::string& path, std::vector<float>& xyz, std::vector<float>& nrm) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw std::runtime_error("cannot open " + path);
+    std::string line, format;
+    size_t nv = 0;
+    std::vector<std::string> props;
+    bool in_vertex = false;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        std::istringstream ss(line);
+        std::string w;
+        ss >> w;
+        if (w == "format") ss >> format;
+        else if (w == "element") {
+            std::string e;
+            ss >> e;
+            in_vertex = e == "vertex";
+            if (in_vertex) ss >> nv;
+        } else if (w == "property" && in_vertex) {
+            std::string type, name;
+            ss >> type >> name;
+            if (type != "float" && type != "float32") throw std::runtime_error("PLY vertex property " + name + " is not float");
+            props.push_back(name);
+        } else if (w == "end_header") {
+            break;
+        }
+    }
+    int ix = -1, iy = -1, iz = -1, inx = -1, iny = -1, inz = -1;
+    for (int i = 0; i < int(props.size()); i++) {
+        if (props[i] == "x") ix = i;
+        if (props[i] == "y") iy = i;
+        if (props[i] == "z") iz = i;
+        if (props[i] == "nx") inx = i;
+        if (props[i] == "ny") iny = i;
+        if (props[i] == "nz") inz = i;
+    }
+    if (ix < 0 || iy < 0 || iz < 0) throw std::runtime_error("PLY has no x y z");
+    const bool has_n = inx >= 0 && iny >= 0 && inz >= 0;
+    std::vector<float> row(props.size());
+    xyz.reserve(3 * nv);
+    for (size_t v = 0; v < nv; v++) {
+        if (format == "ascii") {
+            for (auto& r : row) in >> r;
+        } else if (format == "binary_little_endian") {
+            in.read(reinterpret_cast<char*>(row.data()), std::streamsize(row.size() * sizeof(float)));
+        } else {
+            throw std::runtime_error("PLY format " + format + " is not supported");
+        }
+        xyz.push_back(row[ix]); xyz.push_back(row[iy]); xyz.push_back(row[iz]);
+        if (has_n) { nrm.push_back(row[inx]); nrm.push_back(row[iny]); nrm.push_back(row[inz]); }
+    }
+}
+
+void write_mesh_ply(const std::string& path, const lvr2gb::Mesh& m) {
+    std::ofstream out(path, std::ios::binary);
+    if (!out) throw std::runtime_error("cannot write " + path);
+    const size_t nv = m.vertices.size() / 3, nf = m.faces.size() / 3;
+    out << "ply\nformat binary_little_endian 1.0\ncomment lvr2gb_reconstruct\n"
+        << "element vertex " << nv << "\nproperty float x\nproperty float y\nproperty float z\n"
+        << "element face " << nf << "\nproperty list uchar int vertex_indices\nend_header\n";
+    out.write(reinterpret_cast<const char*>(m.vertices.data()), std::streamsize(m.vertices.size() * sizeof(float)));
+    for (size_t f = 0; f < nf; f++) {
+        const unsigned char three = 3;
+        const int32_t idx[3] = {int32_t(m.faces[3 * f]), int32_t(m.faces[3 * f + 1]), int32_t(m.faces[3 * f + 2])};
+        out.write(reinterpret_cast<const char*>(&three), 1);
+        out.write(reinterpret_cast<const char*>(idx), sizeof(idx));
+    }
+}
+
+void write_point_normals_ply(const std::string& path, const std::vector<float>& xyz, const std::vector<float>& n) {
+    std::ofstream out(path, std::ios::binary);
+    const size_t np = xyz.size() / 3;
+    out << "ply\nformat binary_little_endian 1.0\nelement vertex " << np
+        << "\nproperty float x\nproperty float y\nproperty float z\nproperty float nx\nproperty float ny\n"
+           "property float nz\nend_header\n";
+    for (size_t i = 0; i < np; i++) {
+        out.write(reinterpret_cast<const char*>(&xyz[3 * i]), 3 * sizeof(float));
+        out.write(reinterpret_cast<const char*>(&n[3 * i]), 3 * sizeof(float));
+    }
+}
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Options o = parse(argc, argv);
+    try {
+        std::vector<float> xyz, given_normals;
+        if (ends_with(o.input, ".ply")) read_ply(o.input, xyz, given_normals);
+        else read_ascii(o.input, xyz);
+        const size_t n = xyz.size() / 3;
+        std::printf("[lvr2gb_reconstruct] %zu points from %s\n", n, o.input.c_str());
+        if (o.pcm != "LVR2" && o.pcm != "FLANN" && o.pcm != "NANOFLANN" && o.pcm != "LBVH_CUDA" && o.pcm != "GB300")
+            std::printf("[lvr2gb_reconstruct] --pcm %s: using the GB300 LBVH\n", o.pcm.c_str());
+        double t0 = now_ms();
+        lvr2gb::Surface surface(xyz.data(), n, o.kn, o.ki, o.kd, o.nem, o.device);
+        auto bb = surface.getBoundingBox();
+        std::printf("[lvr2gb_reconstruct] BB of points: [%g, %g, %g] - [%g, %g, %g]\n", bb[0].x, bb[0].y, bb[0].z,
+                    bb[1].x, bb[1].y, bb[1].z);
+        // lvr2_reconstruct sets the flip point to (0,0,0) unless --flipPoint (Main.cpp:335-349)
+        surface.setFlipPoint(lvr2gb::Vec3{o.flip[0], o.flip[1], o.flip[2]});
+        const bool have_normals = given_normals.size() == xyz.size() && !given_normals.empty();
+        if (!have_normals || o.recalc) {
+            surface.calculateSurfaceNormals();
+        } else {
+            std::printf("[lvr2gb_reconstruct] Using given normals.\n");
+            surface.setNormals(given_normals.data());
+        }
+        double t1 = now_ms();
+        lvr2gb::GridOptions g;
+        g.voxelsize = o.voxelsize;
+        g.intersections = o.intersections;
+        g.extrude = o.extrude;
+        g.decomposition = o.decomposition;
+        lvr2gb::Mesh mesh = surface.reconstruct(g);
+        double t2 = now_ms();
+        std::printf("[lvr2gb_reconstruct] Grid Cells: %lld\n", (long long)mesh.info.cells_valid);
+        std::printf("[lvr2gb_reconstruct] Reconstructed mesh (vertices, faces): %lld, %lld\n",
+                    (long long)mesh.info.vertices, (long long)mesh.info.faces);
+        std::printf("[lvr2gb_reconstruct] normals %.2f ms, grid + distance + marching cubes %.2f ms\n", t1 - t0,
+                    t2 - t1);
+        write_mesh_ply(o.output, mesh);
+        if (o.export_normals) write_point_normals_ply("pointnormals.ply", xyz, surface.normals());
+        std::printf("[lvr2gb_reconstruct] wrote %s\n", o.output.c_str());
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "[lvr2gb_reconstruct] error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

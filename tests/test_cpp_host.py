@@ -1,0 +1,70 @@
+"""The C++ host side: lvr2_gb300/cpp/lvr2gb.hpp (lvr2-style classes over the
+C ABI) and the lvr2gb_reconstruct command-line tool."""
+import struct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def built(lib, tmp_path_factory):
+    from lvr2_gb300 import build as B
+    cli = B.build_cli()
+    test_bin = tmp_path_factory.mktemp("cpp") / "test_adapters"
+    B.cpp_compile(ROOT / "tests/cpp/test_adapters.cpp", test_bin)
+    return cli, test_bin
+
+
+def test_cpp_programs_compile_and_parse_flags(built):
+    cli, _ = built
+    r = subprocess.run([str(cli), "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--voxelsize" in r.stdout and "--flipPoint" in r.stdout
+    r = subprocess.run([str(cli), "/nonexistent/scan.pts"], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    r = subprocess.run([str(cli), "x.pts", "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+def read_ply_counts(path):
+    data = Path(path).read_bytes()
+    head = data[:data.index(b"end_header\n")].decode()
+    nv = int(head.split("element vertex ")[1].split()[0])
+    nf = int(head.split("element face ")[1].split()[0])
+    return nv, nf
+
+
+@pytest.mark.gpu
+def test_cpp_adapters_on_gpu(built):
+    _, test_bin = built
+    r = subprocess.run([str(test_bin)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr + r.stdout
+
+
+@pytest.mark.gpu
+def test_cli_matches_python_path(built, tmp_path):
+    """lvr2gb_reconstruct with lvr2_reconstruct's default flags gives the same
+    mesh as the same calls made through the Python mirror."""
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    cli, _ = built
+    pts, _ = synthetic.scan_scene(40_000, seed=9)
+    src = tmp_path / "scan.xyz"
+    with open(src, "w") as f:
+        f.write("%d\n" % len(pts))
+        np.savetxt(f, pts, fmt="%.9g")
+    out = tmp_path / "mesh.ply"
+    r = subprocess.run([str(cli), str(src), "-v", "10", "--outputFile", str(out), "-e"], capture_output=True,
+                       text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "Grid Cells:" in r.stdout
+    nv, nf = read_ply_counts(out)
+    pts_read = np.loadtxt(src, skiprows=1, dtype=np.float32)
+    with lvr2_gb300.Surface(pts_read, kn=10, ki=10, kd=5, nem=0, flip_point=(0, 0, 0)) as s:
+        s.calculate_normals()
+        info = s.reconstruct(voxelsize=10.0, decomposition="PMC")
+    assert (nv, nf) == (info.vertices, info.faces)
+    assert (tmp_path / "pointnormals.ply").exists()
