@@ -254,6 +254,41 @@ lvrgb_status lvrgb_kernel_launches(uint64_t* out);
 lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float* queries, int64_t nq, int32_t k,
                                      uint32_t* idx, float* dist, void* stream);
 
+/* ---- scan projects ----------------------------------------------------
+ * Normals of every scan of a scan project in one pass: the per-scan
+ * CudaSurface runs of lvr2_cuda_normals' directory mode
+ * (src/tools/lvr2_cuda_normals/Main.cpp:60-111, 166-190), with kNN restricted
+ * to each scan and a per-scan flip point, over one segmented LBVH (one sort,
+ * one tree, one normals launch per search round).  Results equal
+ * lvrgb_calculate_normals run on each scan alone. */
+typedef struct lvrgb_batch_s* lvrgb_batch;
+
+/* xyz: all scans concatenated (n x 3); scan_offsets: nscans + 1 entries,
+ * scan_offsets[0] = 0, strictly increasing; flip_points: nscans x 3 (the
+ * scanner positions).  cfg: kn, ki (<= 2 kn), nem, adaptive, bucket,
+ * seed_radius, device as for a surface (flip fields ignored).  Host arrays
+ * for offsets and flips; xyz on host or device (on_device). */
+lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xyz, const int64_t* scan_offsets,
+                                int32_t nscans, const float* flip_points, int32_t on_device, void* stream,
+                                lvrgb_batch* out);
+lvrgb_status lvrgb_batch_destroy(lvrgb_batch b);
+
+/* Builds the segmented LBVH and computes (and interpolates) all normals.
+ * use_graph != 0: the first call runs once and captures the whole launch
+ * sequence in a CUDA graph; later calls replay it.  Synchronous. */
+lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, void* stream);
+
+/* Normals of all scans in input order (n x 3). */
+lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_device, void* stream);
+
+/* Times the pipeline for each candidate (LBVH bucket 16/32, seed radius 1/2)
+ * on this project and keeps the fastest; returns the choice. */
+lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_radius, void* stream);
+
+/* Counters of the last run (layout of lvrgb_normal_stats) and device ms:
+ * ms[0] tree, ms[1] normals, ms[2] interpolation (eager runs), ms[3] total. */
+lvrgb_status lvrgb_batch_stats(lvrgb_batch b, uint32_t counters[16], float ms[4]);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* lvrgb_last_error(void);
 

@@ -7,6 +7,6 @@ Python mirror of lvr2's PointsetSurface / CudaSurface calls; the C++ mirror is
 in lvr2_gb300/cpp.
 """
 from ._lib import LvrgbError, load
-from .surface import Surface
+from .surface import Batch, Surface
 
-__all__ = ["Surface", "LvrgbError", "load"]
+__all__ = ["Surface", "Batch", "LvrgbError", "load"]

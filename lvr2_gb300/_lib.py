@@ -27,6 +27,8 @@ EXPORTS = [
     "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance", "lvrgb_grid_distances",
     "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
     "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches", "lvrgb_knn_small_noalloc",
+    "lvrgb_batch_create", "lvrgb_batch_destroy", "lvrgb_batch_calculate_normals", "lvrgb_batch_get_normals",
+    "lvrgb_batch_autotune", "lvrgb_batch_stats",
     "lvrgb_last_error", "lvrgb_version",
 ]
 
@@ -98,6 +100,12 @@ def load(path=None):
     L.lvrgb_surface_timings.argtypes = [vp, vp]
     L.lvrgb_kernel_launches.argtypes = [vp]
     L.lvrgb_knn_small_noalloc.argtypes = [vp, i64, vp, i64, i32, vp, vp, vp]
+    L.lvrgb_batch_create.argtypes = [ctypes.POINTER(SurfaceConfig), vp, vp, i32, vp, i32, vp, ctypes.POINTER(vp)]
+    L.lvrgb_batch_destroy.argtypes = [vp]
+    L.lvrgb_batch_calculate_normals.argtypes = [vp, i32, vp]
+    L.lvrgb_batch_get_normals.argtypes = [vp, vp, i32, vp]
+    L.lvrgb_batch_autotune.argtypes = [vp, vp, vp, vp]
+    L.lvrgb_batch_stats.argtypes = [vp, vp, vp]
     L.lvrgb_last_error.restype = ctypes.c_char_p
     L.lvrgb_version.restype = ctypes.c_char_p
     for name in EXPORTS:

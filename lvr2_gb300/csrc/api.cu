@@ -9,6 +9,7 @@
 #include <string>
 
 #include "lvrgb.h"
+#include "batch.h"
 #include "grid.h"
 #include "lbvh_build.h"
 #include "primitives.cuh"
@@ -731,6 +732,238 @@ lvrgb_status lvrgb_kernel_launches(uint64_t* out) {
     if (!out) return fail(LVRGB_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = g_launches.load();
     return LVRGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Scan projects: normals of many scans in one pass (lvrgb_batch_*).
+// ---------------------------------------------------------------------------
+struct lvrgb_batch_s {
+    lvrgb_surface_config cfg;
+    int device = 0;
+    Workspace ws;
+    std::vector<int64_t> offsets;
+    std::vector<float> flips;
+    float* d_xyz = nullptr;
+    BatchRun R;
+    int* d_err = nullptr;
+    uint32_t* d_stats = nullptr;
+    cudaStream_t bs = nullptr;  // the batch's own stream (graphs need a non-default stream)
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec = nullptr;
+    bool ran = false;
+    float ms[4] = {0, 0, 0, 0};
+    ~lvrgb_batch_s() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (bs) cudaStreamDestroy(bs);
+    }
+};
+
+namespace {
+
+NormalsConfig batch_config(const lvrgb_batch_s* b) {
+    NormalsConfig c;
+    c.kn = b->cfg.kn;
+    c.nem = b->cfg.nem;
+    c.adaptive = b->cfg.adaptive;
+    c.gap_threshold = b->cfg.gap_threshold > 0 ? b->cfg.gap_threshold : 1e-3f;
+    return c;
+}
+
+void batch_run_eager(lvrgb_batch b, bool timed) {
+    if (b->R.prepared_bucket != b->cfg.bucket)
+        batch_prepare(b->offsets, b->flips, batch_config(b), b->cfg.ki, b->cfg.bucket, b->ws, b->R, b->bs);
+    batch_pipeline(b->d_xyz, batch_config(b), b->cfg.ki, b->cfg.seed_radius, b->ws, b->R, b->d_err, b->d_stats, b->bs,
+                   timed ? b->ev : nullptr);
+    b->ran = true;
+}
+
+// Runs the pipeline on the batch stream, ordered after `caller` and before
+// whatever the caller enqueues next.
+template <typename F>
+void on_batch_stream(lvrgb_batch b, cudaStream_t caller, F&& f) {
+    LVRGB_CUDA(cudaEventRecord(b->ev[4], caller));
+    LVRGB_CUDA(cudaStreamWaitEvent(b->bs, b->ev[4], 0));
+    f();
+    LVRGB_CUDA(cudaEventRecord(b->ev[5], b->bs));
+    LVRGB_CUDA(cudaStreamWaitEvent(caller, b->ev[5], 0));
+}
+
+void batch_check(lvrgb_batch b) {
+    int herr = 0;
+    LVRGB_CUDA(cudaStreamSynchronize(b->bs));
+    LVRGB_CUDA(cudaMemcpy(&herr, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        LVRGB_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
+        throw ApiError{LVRGB_ERR_KERNEL, "kNN traversal reported an internal limit"};
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xyz, const int64_t* scan_offsets,
+                                int32_t nscans, const float* flip_points, int32_t on_device, void* stream,
+                                lvrgb_batch* out) {
+    if (!out) return fail(LVRGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    lvrgb_batch b = nullptr;
+    lvrgb_status st = guarded([&] {
+        require(cfg && scan_offsets && flip_points, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        require(nscans >= 1 && nscans <= 65535, LVRGB_ERR_INVALID_ARGUMENT, "nscans must be in 1..65535");
+        require(cfg->kn > 0 && cfg->ki >= 0, LVRGB_ERR_INVALID_ARGUMENT, "kn must be > 0, ki >= 0");
+        require(cfg->ki <= 2 * cfg->kn, LVRGB_ERR_UNSUPPORTED,
+                "scan projects interpolate from the estimation's neighbour lists: ki must be <= 2 * kn");
+        check_nem(cfg->nem);
+        require(cfg->bucket >= 0 && cfg->bucket <= 32, LVRGB_ERR_INVALID_ARGUMENT, "bucket must be in 0..32");
+        require(scan_offsets[0] == 0, LVRGB_ERR_INVALID_ARGUMENT, "scan_offsets[0] must be 0");
+        for (int k = 0; k < nscans; k++)
+            require(scan_offsets[k + 1] > scan_offsets[k], LVRGB_ERR_INVALID_ARGUMENT,
+                    "scan offsets must be strictly increasing (no empty scan)");
+        const int64_t n = scan_offsets[nscans];
+        require(n < (int64_t(1) << 31) - 32 * int64_t(nscans), LVRGB_ERR_INVALID_ARGUMENT, "too many points");
+        require(xyz != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "xyz is NULL");
+        DeviceScope dev(cfg->device);
+        cudaStream_t st = as_stream(stream);
+        b = new lvrgb_batch_s();
+        b->cfg = *cfg;
+        if (b->cfg.bucket == 0) b->cfg.bucket = 32;
+        if (b->cfg.seed_radius == 0) b->cfg.seed_radius = 1;
+        b->device = cfg->device;
+        b->offsets.assign(scan_offsets, scan_offsets + nscans + 1);
+        b->flips.assign(flip_points, flip_points + 3 * size_t(nscans));
+        LVRGB_CUDA(cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking));
+        for (auto& e : b->ev) LVRGB_CUDA(cudaEventCreate(&e));
+        b->d_err = b->ws.get<int>("batch.err", 4);
+        b->d_stats = b->ws.get<uint32_t>("batch.stats", kNormalStats);
+        LVRGB_CUDA(cudaMemsetAsync(b->d_err, 0, 4 * sizeof(int), st));
+        b->d_xyz = b->ws.get<float>("batch.xyz", size_t(n) * 3);
+        LVRGB_CUDA(cudaMemcpyAsync(b->d_xyz, xyz, size_t(n) * 3 * sizeof(float),
+                                   on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+    if (st != LVRGB_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return LVRGB_OK;
+}
+
+lvrgb_status lvrgb_batch_destroy(lvrgb_batch b) {
+    if (!b) return LVRGB_OK;
+    return guarded([&] {
+        DeviceScope dev(b->device);
+        delete b;
+    });
+}
+
+lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, void* stream) {
+    return guarded([&] {
+        require(b != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "batch is NULL");
+        DeviceScope dev(b->device);
+        cudaStream_t caller = as_stream(stream);
+        if (!use_graph) {
+            on_batch_stream(b, caller, [&] { batch_run_eager(b, true); });
+            batch_check(b);
+            for (int i = 0; i < 3; i++) LVRGB_CUDA(cudaEventElapsedTime(&b->ms[i], b->ev[i], b->ev[i + 1]));
+            LVRGB_CUDA(cudaEventElapsedTime(&b->ms[3], b->ev[0], b->ev[3]));
+            return;
+        }
+        if (!b->exec) {
+            // An eager pass sizes every buffer and sets kernel attributes, then
+            // the same launch sequence is captured once.
+            on_batch_stream(b, caller, [&] { batch_run_eager(b, false); });
+            batch_check(b);
+            cudaGraph_t g = nullptr;
+            LVRGB_CUDA(cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeRelaxed));
+            try {
+                batch_run_eager(b, false);
+            } catch (...) {
+                cudaStreamEndCapture(b->bs, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            LVRGB_CUDA(cudaStreamEndCapture(b->bs, &g));
+            const cudaError_t e = cudaGraphInstantiate(&b->exec, g, 0);
+            cudaGraphDestroy(g);
+            LVRGB_CUDA(e);
+        }
+        on_batch_stream(b, caller, [&] {
+            LVRGB_CUDA(cudaEventRecord(b->ev[0], b->bs));
+            LVRGB_CUDA(cudaGraphLaunch(b->exec, b->bs));
+            LVRGB_CUDA(cudaEventRecord(b->ev[3], b->bs));
+        });
+        batch_check(b);
+        b->ms[0] = b->ms[1] = b->ms[2] = 0.0f;
+        LVRGB_CUDA(cudaEventElapsedTime(&b->ms[3], b->ev[0], b->ev[3]));
+    });
+}
+
+lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(b != nullptr && normals != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        require(b->ran, LVRGB_ERR_STATE, "no normals: call lvrgb_batch_calculate_normals");
+        DeviceScope dev(b->device);
+        cudaStream_t st = as_stream(stream);
+        const size_t n = size_t(b->offsets.back());
+        float* d = stage_out(b->ws, "batch.out3", normals, n * 3, on_device);
+        on_batch_stream(b, st, [&] { batch_scatter_normals(b->R, d, b->bs); });
+        finish_out(normals, d, n * 3, on_device, st);
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_radius, void* stream) {
+    return guarded([&] {
+        require(b != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "batch is NULL");
+        DeviceScope dev(b->device);
+        cudaStream_t caller = as_stream(stream);
+        // Candidate tile shapes: LBVH bucket size and seed radius.  Each runs
+        // the whole pipeline twice; the second run is timed.
+        const int cands[4][2] = {{32, 1}, {32, 2}, {16, 1}, {16, 2}};
+        float best = 1e30f;
+        int bb = b->cfg.bucket, br = b->cfg.seed_radius;
+        for (const auto& c : cands) {
+            b->cfg.bucket = c[0];
+            b->cfg.seed_radius = c[1];
+            float t = 0;
+            for (int rep = 0; rep < 2; rep++) {
+                on_batch_stream(b, caller, [&] { batch_run_eager(b, true); });
+                batch_check(b);
+                LVRGB_CUDA(cudaEventElapsedTime(&t, b->ev[0], b->ev[3]));
+            }
+            if (t < best) {
+                best = t;
+                bb = c[0];
+                br = c[1];
+            }
+        }
+        b->cfg.bucket = bb;
+        b->cfg.seed_radius = br;
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        on_batch_stream(b, caller, [&] { batch_run_eager(b, false); });
+        batch_check(b);
+        if (bucket) *bucket = bb;
+        if (seed_radius) *seed_radius = br;
+    });
+}
+
+lvrgb_status lvrgb_batch_stats(lvrgb_batch b, uint32_t counters[16], float ms[4]) {
+    return guarded([&] {
+        require(b != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "batch is NULL");
+        DeviceScope dev(b->device);
+        if (counters) LVRGB_CUDA(cudaMemcpy(counters, b->d_stats, kNormalStats * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (ms)
+            for (int i = 0; i < 4; i++) ms[i] = b->ms[i];
+    });
 }
 
 }  // extern "C"

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_kernel(SdfArgs A) {
         if (active) {
             heap.sort_ascending();
             float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
-            const int cnt = min(A.K, A.T.n);
+            const int cnt = heap.real;
 #pragma unroll 4
             for (int s = 0; s < cnt; s++) {
                 const unsigned long long key = heap.at(s);

@@ -1,6 +1,9 @@
 // lbvh.cu -- LBVH construction: bounding box, 30-bit Morton codes, device
 // radix sort, Karras radix tree over point buckets, bottom-up child boxes.
 #include "lbvh_build.h"
+
+#include <stdexcept>
+#include <vector>
 #include "primitives.cuh"
 
 namespace lvrgb {
@@ -145,6 +148,154 @@ __global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket,
     }
 }
 
+// ---- segmented (multi-scan) construction --------------------------------
+
+// Scan of position i from sorted offsets off[0..S] (binary search).
+__device__ __forceinline__ int scan_of(const int* __restrict__ off, int S, int i) {
+    int lo = 0, hi = S;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// One block per scan: the scan's bounding box.
+__global__ void seg_bbox_kernel(const float* __restrict__ xyz, const int* __restrict__ off, float* __restrict__ box) {
+    const int s = blockIdx.x;
+    const int a = off[s], b = off[s + 1];
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x)
+        for (int c = 0; c < 3; c++) {
+            const float v = xyz[3 * size_t(i) + c];
+            mn[c] = fminf(mn[c], v);
+            mx[c] = fmaxf(mx[c], v);
+        }
+    __shared__ float sh[32][6];
+    for (int c = 0; c < 3; c++)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[c] = fminf(mn[c], __shfl_down_sync(kFull, mn[c], o));
+            mx[c] = fmaxf(mx[c], __shfl_down_sync(kFull, mx[c], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; c++) { sh[threadIdx.x >> 5][c] = mn[c]; sh[threadIdx.x >> 5][3 + c] = mx[c]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        float v = sh[0][threadIdx.x];
+        for (int w = 1; w < int(blockDim.x >> 5); w++)
+            v = threadIdx.x < 3 ? fminf(v, sh[w][threadIdx.x]) : fmaxf(v, sh[w][threadIdx.x]);
+        box[6 * s + threadIdx.x] = v;
+    }
+}
+
+__global__ void seg_morton_kernel(const float* __restrict__ xyz, int n, const int* __restrict__ off, int S,
+                                  const float* __restrict__ box, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = scan_of(off, S, i);
+    const float* bx = box + 6 * s;
+    const float ext = fmaxf(fmaxf(bx[3] - bx[0], bx[4] - bx[1]), bx[5] - bx[2]);
+    const float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    const uint32_t cx = uint32_t(fminf(fmaxf((xyz[3 * size_t(i)] - bx[0]) * scale, 0.0f), 1023.0f));
+    const uint32_t cy = uint32_t(fminf(fmaxf((xyz[3 * size_t(i) + 1] - bx[1]) * scale, 0.0f), 1023.0f));
+    const uint32_t cz = uint32_t(fminf(fmaxf((xyz[3 * size_t(i) + 2] - bx[2]) * scale, 0.0f), 1023.0f));
+    keys[i] = (uint64_t(s) << 30) | (spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2));
+    idx[i] = uint32_t(i);
+}
+
+// Sorted position j -> padded position pad_off[s] + (j - off[s]).
+__global__ void seg_gather_kernel(const float* __restrict__ xyz, const uint64_t* __restrict__ skeys,
+                                  const uint32_t* __restrict__ sidx, int n, const int* __restrict__ off,
+                                  const int* __restrict__ pad_off, float4* __restrict__ pts, uint32_t* __restrict__ inv,
+                                  uint64_t* __restrict__ pkeys) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint64_t key = skeys[j];
+    const int s = int(key >> 30);
+    const uint32_t o = sidx[j];
+    const int pp = pad_off[s] + (j - off[s]);
+    pts[pp] = make_float4(xyz[3 * size_t(o)], xyz[3 * size_t(o) + 1], xyz[3 * size_t(o) + 2], __uint_as_float(o));
+    inv[o] = uint32_t(pp);
+    pkeys[pp] = key;
+}
+
+// Padding after each scan's points: NaN coordinates (never within any bound)
+// and index 0xffffffff.
+__global__ void seg_pad_kernel(int np, const int* __restrict__ off, const int* __restrict__ pad_off, int S,
+                               float4* __restrict__ pts) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int s = scan_of(pad_off, S, p);
+    if (p - pad_off[s] >= off[s + 1] - off[s]) {
+        const float nan = __int_as_float(0x7fffffff);
+        pts[p] = make_float4(nan, nan, nan, __uint_as_float(0xffffffffu));
+    }
+}
+
+__global__ void seg_bucket_keys_kernel(const uint64_t* __restrict__ pkeys, int bucket, int nb, uint64_t* __restrict__ bkeys,
+                                       uint16_t* __restrict__ bucket_scan) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const uint64_t k = pkeys[size_t(b) * bucket];
+    bkeys[b] = k;
+    bucket_scan[b] = uint16_t(k >> 30);
+}
+
+__device__ __forceinline__ int delta64(const uint64_t* __restrict__ keys, int nb, int i, int j) {
+    if (j < 0 || j >= nb) return -1;
+    const uint64_t ki = keys[i], kj = keys[j];
+    if (ki != kj) return __clzll(ki ^ kj);
+    return 64 + __clz(uint32_t(i) ^ uint32_t(j));
+}
+
+// Karras radix tree over 64-bit (scan, Morton) bucket keys.  The node whose
+// range is exactly one scan's buckets becomes that scan's root.
+__global__ void seg_karras_kernel(const uint64_t* __restrict__ keys, int nb, const uint16_t* __restrict__ bucket_scan,
+                                  TreeNode* __restrict__ nodes, int* __restrict__ bparent, SegInfo* __restrict__ segs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb - 1) return;
+    const int dir = (delta64(keys, nb, i, i + 1) - delta64(keys, nb, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta64(keys, nb, i, i - dir);
+    int lmax = 2;
+    while (delta64(keys, nb, i, i + lmax * dir) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta64(keys, nb, i, i + (l + t) * dir) > dmin) l += t;
+    const int j = i + l * dir;
+    const int dnode = delta64(keys, nb, i, j);
+    int s = 0;
+    int div = 2;
+    int t = (l + div - 1) / div;
+    while (true) {
+        if (delta64(keys, nb, i, i + (s + t) * dir) > dnode) s += t;
+        if (t == 1) break;
+        div <<= 1;
+        t = (l + div - 1) / div;
+    }
+    const int gamma = i + s * dir + (dir < 0 ? -1 : 0);
+    const int lo = min(i, j), hi = max(i, j);
+    int left, right;
+    if (lo == gamma) {
+        left = -1 - gamma;
+        bparent[gamma] = (i << 1) | 0;
+    } else {
+        left = gamma;
+        nodes[gamma].d.z = (i << 1) | 0;
+    }
+    if (hi == gamma + 1) {
+        right = -1 - (gamma + 1);
+        bparent[gamma + 1] = (i << 1) | 1;
+    } else {
+        right = gamma + 1;
+        nodes[gamma + 1].d.z = (i << 1) | 1;
+    }
+    nodes[i].d.x = left;
+    nodes[i].d.y = right;
+    if (i == 0) nodes[0].d.z = -1;
+    const int sc = bucket_scan[lo];
+    if (segs[sc].blo == lo && segs[sc].bhi == hi) segs[sc].root = i;
+}
+
 }  // namespace
 
 void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::string& tag, Lbvh& T,
@@ -226,6 +377,102 @@ void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, 
     LVRGB_LAUNCH_CHECK();
     bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(B.pts, n, bucket, nb, B.nodes, B.bparent, B.counters,
                                                                  B.err);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void lbvh_segmented_prepare(const std::vector<int64_t>& offsets, const std::vector<float>& flips, int bucket,
+                            Workspace& ws, const std::string& tag, SegTree& out, cudaStream_t s) {
+    if (bucket < 1 || bucket > 32) bucket = 32;
+    const int S = int(offsets.size()) - 1;
+    if (S < 1 || S > 65535) throw std::invalid_argument("scan count must be in 1..65535");
+    const int n = int(offsets[size_t(S)]);
+    std::vector<int> off(size_t(S) + 1), pad_off(size_t(S) + 1);
+    std::vector<SegInfo> segs(static_cast<size_t>(S));
+    int np = 0, nb = 0;
+    for (int k = 0; k < S; k++) {
+        const int64_t a = offsets[size_t(k)], b = offsets[size_t(k) + 1];
+        if (b <= a) throw std::invalid_argument("scan offsets must be strictly increasing");
+        off[size_t(k)] = int(a);
+        pad_off[size_t(k)] = np;
+        const int nbk = int((b - a + bucket - 1) / bucket);
+        segs[size_t(k)].blo = nb;
+        segs[size_t(k)].bhi = nb + nbk - 1;
+        segs[size_t(k)].root = nbk == 1 ? -1 - nb : 0;  // multi-bucket roots come from the tree
+        segs[size_t(k)].n = int(b - a);
+        segs[size_t(k)].fx = flips[3 * size_t(k)];
+        segs[size_t(k)].fy = flips[3 * size_t(k) + 1];
+        segs[size_t(k)].fz = flips[3 * size_t(k) + 2];
+        segs[size_t(k)].pad = 0;
+        nb += nbk;
+        np += nbk * bucket;
+    }
+    off[size_t(S)] = n;
+    pad_off[size_t(S)] = np;
+    int sbits = 0;
+    while ((1 << sbits) < S) sbits++;
+    out.nscans = S;
+    out.npoints = n;
+    out.npadded = np;
+    out.nbuckets = nb;
+    out.bucket = bucket;
+    out.sbits = sbits;
+    out.d_off = ws.get<int>(tag + ".off", size_t(S) + 1);
+    out.d_pad = ws.get<int>(tag + ".padoff", size_t(S) + 1);
+    out.segs = ws.get<SegInfo>(tag + ".segs", size_t(S));
+    LVRGB_CUDA(cudaMemcpyAsync(out.d_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, s));
+    LVRGB_CUDA(cudaMemcpyAsync(out.d_pad, pad_off.data(), sizeof(int) * pad_off.size(), cudaMemcpyHostToDevice, s));
+    LVRGB_CUDA(cudaMemcpyAsync(out.segs, segs.data(), sizeof(SegInfo) * segs.size(), cudaMemcpyHostToDevice, s));
+    // the host vectors go out of scope: finish the uploads now
+    LVRGB_CUDA(cudaStreamSynchronize(s));
+    // size every buffer of the build here so that lbvh_segmented_build allocates nothing
+    out.T.pts = ws.get<float4>(tag + ".pts", size_t(np));
+    out.T.inv = ws.get<uint32_t>(tag + ".inv", size_t(n));
+    out.T.nodes = ws.get<TreeNode>(tag + ".nodes", size_t(nb > 1 ? nb - 1 : 1));
+    out.bucket_scan = ws.get<uint16_t>(tag + ".bscan", size_t(nb));
+    out.box = ws.get<float>(tag + ".segbox", size_t(S) * 6);
+    out.keys = ws.get<uint64_t>(tag + ".keys", size_t(n));
+    out.keys2 = ws.get<uint64_t>(tag + ".keys2", size_t(n));
+    out.idx = ws.get<uint32_t>(tag + ".idx", size_t(n));
+    out.idx2 = ws.get<uint32_t>(tag + ".idx2", size_t(n));
+    out.sort_tmp = ws.get<unsigned char>(tag + ".sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(n)));
+    out.pkeys = ws.get<uint64_t>(tag + ".pkeys", size_t(np));
+    out.bkeys = ws.get<uint64_t>(tag + ".bkeys", size_t(nb));
+    out.bparent = ws.get<int>(tag + ".bparent", size_t(nb));
+    out.counters = ws.get<int>(tag + ".counters", size_t(nb > 1 ? nb - 1 : 1));
+    out.T.n = np;
+    out.T.bucket = bucket;
+    out.T.nbuckets = nb;
+    out.T.bkeys = nullptr;
+}
+
+void lbvh_segmented_build(const float* xyz, SegTree& out, int* d_err, cudaStream_t s) {
+    const int S = out.nscans, n = out.npoints, np = out.npadded, nb = out.nbuckets, bucket = out.bucket;
+    float4* pts = const_cast<float4*>(out.T.pts);
+    uint32_t* inv = const_cast<uint32_t*>(out.T.inv);
+    TreeNode* nodes = const_cast<TreeNode*>(out.T.nodes);
+    seg_bbox_kernel<<<S, 1024, 0, s>>>(xyz, out.d_off, out.box);
+    LVRGB_LAUNCH_CHECK();
+    seg_morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, out.d_off, S, out.box, out.keys, out.idx);
+    LVRGB_LAUNCH_CHECK();
+    const bool alt = radix_sort_pairs<uint64_t>(out.keys, out.idx, out.keys2, out.idx2, size_t(n), 0,
+                                                30 + out.sbits, out.sort_tmp, s);
+    seg_pad_kernel<<<ceil_div(np, 256), 256, 0, s>>>(np, out.d_off, out.d_pad, S, pts);
+    LVRGB_LAUNCH_CHECK();
+    seg_gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, alt ? out.keys2 : out.keys, alt ? out.idx2 : out.idx, n,
+                                                      out.d_off, out.d_pad, pts, inv, out.pkeys);
+    LVRGB_LAUNCH_CHECK();
+    seg_bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(out.pkeys, bucket, nb, out.bkeys, out.bucket_scan);
+    LVRGB_LAUNCH_CHECK();
+    if (nb == 1) {
+        LVRGB_CUDA(cudaMemsetAsync(out.bparent, 0xff, sizeof(int), s));
+        return;
+    }
+    LVRGB_CUDA(cudaMemsetAsync(out.counters, 0, sizeof(int) * size_t(nb - 1), s));
+    seg_karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(out.bkeys, nb, out.bucket_scan, nodes, out.bparent,
+                                                            out.segs);
+    LVRGB_LAUNCH_CHECK();
+    bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, np, bucket, nb, nodes, out.bparent,
+                                                                 out.counters, d_err);
     LVRGB_LAUNCH_CHECK();
 }
 

@@ -29,6 +29,16 @@ struct __align__(16) TreeNode {
     int4 d;    // child0, child1 (>= 0 internal node, < 0 bucket -1-b), parent word, unused
 };
 
+// One scan of a segmented tree: its subtree root (< 0: single bucket -1-root),
+// its bucket range and its flip point.
+struct SegInfo {
+    int root;
+    int blo, bhi;
+    int n;
+    float fx, fy, fz;
+    int pad;
+};
+
 struct Lbvh {
     const float4* pts = nullptr;
     const uint32_t* inv = nullptr;
@@ -60,12 +70,14 @@ struct LaneHeap {
     unsigned long long* h;
     int K;
     int fill;
+    int real;  // real (non-sentinel) entries once finished
     unsigned long long top;
 
     __device__ __forceinline__ void init(unsigned long long* lane_base, int k) {
         h = lane_base;
         K = k;
         fill = 0;
+        real = 0;
         top = kKeyEmpty;
     }
     __device__ __forceinline__ float tau() const { return key_d2(top); }
@@ -101,6 +113,7 @@ struct LaneHeap {
     }
     // Completes the heap when fewer than K keys were offered (sentinels).
     __device__ __forceinline__ void finish() {
+        real = fill;
         if (fill < K) {
             for (int s = fill; s < K; s++) h[s * 32] = kKeyEmpty;
             fill = K;
@@ -224,10 +237,10 @@ __device__ __forceinline__ int seed_bucket_for(const Lbvh& T, float x, float y, 
 // small before the tree walk; the walk skips them.
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
                                              LaneHeap& heap, float4* stage, int* err, TravStats& st,
-                                             int seed = -1) {
+                                             int seed = -1, int root = 0, int blo = 0, int bhi = 0x7fffffff) {
     const int lane = threadIdx.x & 31;
     if (T.nbuckets <= 0) {
-        heap.finish();
+        if (active) heap.finish();
         return;
     }
     // warp query box and an empty, NaN-padded candidate buffer
@@ -252,21 +265,25 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         for (int a = 0; a < 3; a++) { W.lo[a] = v[a]; W.hi[a] = v[3 + a]; }
         __syncwarp();
     }
-    if (T.nbuckets == 1) {
-        add_bucket(T, 0, W, qx, qy, qz, active, heap, st);
-        if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
-        heap.finish();
-        return;
-    }
+    // A root < 0 is a single bucket (-1 - root): a one-bucket tree or segment.
+    if (T.nbuckets == 1) root = -1;
+    bhi = min(bhi, T.nbuckets - 1);
     int skip_lo = 1, skip_hi = 0;  // empty range
     if (seed >= 0) {
-        skip_lo = max(0, seed - T.seed_radius);
-        skip_hi = min(T.nbuckets - 1, seed + T.seed_radius);
+        skip_lo = max(blo, seed - T.seed_radius);
+        skip_hi = min(bhi, seed + T.seed_radius);
         for (int b = skip_lo; b <= skip_hi; b++) add_bucket(T, b, W, qx, qy, qz, active, heap, st);
+    }
+    if (root < 0) {
+        const int b = -1 - root;
+        if (b < skip_lo || b > skip_hi) add_bucket(T, b, W, qx, qy, qz, active, heap, st);
+        if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
+        if (active) heap.finish();
+        return;
     }
     int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
     int sp = 0;
-    int node = 0;  // root
+    int node = root;
     // A tree over nb buckets has nb - 1 internal nodes; each is expanded at
     // most once per warp.  The bound only guards against a malformed tree.
     int budget = T.nbuckets + 1;
@@ -351,7 +368,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         }
     }
     if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
-    heap.finish();
+    if (active) heap.finish();
 }
 
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,

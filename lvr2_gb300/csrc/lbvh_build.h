@@ -1,6 +1,7 @@
 // lbvh_build.h -- host entry of the LBVH construction (lbvh.cu).
 #pragma once
 #include <string>
+#include <vector>
 
 #include "lbvh.cuh"
 #include "workspace.h"
@@ -36,5 +37,32 @@ struct LbvhBuffers {
 // Same construction as lbvh_build, into caller-provided buffers (no
 // allocation).
 void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, Lbvh& T, cudaStream_t s);
+
+// A segmented LBVH over the scans of a scan project: one radix sort of
+// (scan, Morton) keys, each scan's points padded to whole buckets (padding:
+// NaN coordinates, index 0xffffffff), one Karras tree whose per-scan subtrees
+// are the scans' search roots.  T.n counts the padded positions.
+struct SegTree {
+    Lbvh T;
+    int nscans = 0, npoints = 0, npadded = 0, nbuckets = 0, bucket = 32, sbits = 0;
+    SegInfo* segs = nullptr;           // device, per scan
+    uint16_t* bucket_scan = nullptr;   // device, per bucket
+    int* d_off = nullptr;              // device scan offsets
+    int* d_pad = nullptr;              // device padded offsets
+    float* box = nullptr;
+    uint64_t *keys = nullptr, *keys2 = nullptr, *pkeys = nullptr, *bkeys = nullptr;
+    uint32_t *idx = nullptr, *idx2 = nullptr;
+    void* sort_tmp = nullptr;
+    int *bparent = nullptr, *counters = nullptr;
+};
+
+// Uploads the scan layout (offsets, padding, per-scan info and flip points)
+// and sizes every buffer; synchronises the stream.  Run when the layout or the
+// bucket size changes.
+void lbvh_segmented_prepare(const std::vector<int64_t>& offsets, const std::vector<float>& flips, int bucket,
+                            Workspace& ws, const std::string& tag, SegTree& out, cudaStream_t s);
+// Builds the tree from device points: kernels and device-side copies only (no
+// allocation, no host transfer), so it can be captured in a CUDA graph.
+void lbvh_segmented_build(const float* xyz, SegTree& out, int* d_err, cudaStream_t s);
 
 }  // namespace lvrgb

@@ -141,6 +141,11 @@ struct NormalsArgs {
     uint32_t* stats;
     uint32_t* nbr;  // optional: first ki neighbours (Morton positions), column s at nbr[s * n]
     int ki;
+    // Segmented (multi-scan) mode: per-bucket scan id and per-scan search
+    // root, bucket range and flip point; nq_dev replaces nq when given.
+    const SegInfo* segs;
+    const uint16_t* bucket_scan;
+    const uint32_t* nq_dev;
 };
 
 // BaseVector::normalize with IEEE operations (null vector unchanged).
@@ -294,23 +299,46 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
     const unsigned lt = (1u << lane) - 1u;
-    const int cnt = min(A.K, A.T.n);
+    const int nq = A.nq_dev ? int(*A.nq_dev) : A.nq;
     TravStats st;
-    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
+    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < nq;
          tile += gridDim.x * kWarpsPerBlock) {
         const int qi = tile * 32 + lane;
-        const bool active = qi < A.nq;
+        bool active = qi < nq;
         const int pos = active ? (A.list ? int(A.list[qi]) : qi) : 0;
         const float4 q = __ldg(A.T.pts + pos);
+        // padding after each scan of a segmented tree is not a query
+        if (A.segs && __float_as_uint(q.w) == 0xffffffffu) active = false;
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
-        const int seed = __shfl_sync(kFull, pos, 0) / A.T.bucket;
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
+        float fx = A.fx, fy = A.fy, fz = A.fz;
+        if (A.segs) {
+            // One search per scan present in the warp; each lane searches its own scan's tree.
+            const int sc = active ? int(A.bucket_scan[pos / A.T.bucket]) : -1;
+            unsigned remaining = __ballot_sync(kFull, active);
+            while (remaining) {
+                const int leader = __ffs(remaining) - 1;
+                const int s = __shfl_sync(kFull, sc, leader);
+                const unsigned grp = __ballot_sync(kFull, active && sc == s);
+                remaining &= ~grp;
+                const SegInfo g = A.segs[s];
+                const int seed = __shfl_sync(kFull, pos, leader) / A.T.bucket;
+                knn_traverse(A.T, q.x, q.y, q.z, (grp >> lane) & 1u, heap, ctx.stage, A.err, st, seed, g.root,
+                             g.blo, g.bhi);
+            }
+            if (active) {
+                fx = A.segs[sc].fx; fy = A.segs[sc].fy; fz = A.segs[sc].fz;
+            }
+        } else {
+            const int seed = __shfl_sync(kFull, pos, 0) / A.T.bucket;
+            knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
+        }
         bool retry = false;
         if (active) {
             // Ascending order puts the real entries first (fewer points than K)
             // and gives the interpolation its ki nearest in lvr2's order.
-            if (A.T.n < A.K || A.nbr) heap.sort_ascending();
+            const int cnt = heap.real;
+            if (cnt < A.K || A.nbr) heap.sort_ascending();
             NbrPass P;
             neighbour_pass<kNem>(A.T, heap, cnt, q, P);
             bool fit = true;
@@ -327,7 +355,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
                 bool fp64;
                 fit_plane<kNem>(A, heap, cnt, q, P, n, fp64);
                 // Flip toward the flip point; Normal::operator-() re-normalises.
-                const float tx = __fsub_rn(A.fx, q.x), ty = __fsub_rn(A.fy, q.y), tz = __fsub_rn(A.fz, q.z);
+                const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
                 const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
                 if (dot < 0.0f) {
                     n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
@@ -357,7 +385,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     }
     unsigned pushes = st.pushes;
     for (int o = 16; o > 0; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
-
     if (lane == 0 && st.nodes) {
         atomicAdd(A.stats + 8, st.buckets);
         atomicAdd(A.stats + 9, st.nodes);
@@ -370,9 +397,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
 // interpolateSurfaceNormals from stored neighbour lists: the same sums as
 // interpolate_kernel, in the same order, without a second search.
 __global__ void interpolate_lists_kernel(const float4* __restrict__ in, const uint32_t* __restrict__ nbr, int n,
-                                         int ki, float4* __restrict__ out) {
+                                         int ki, float4* __restrict__ out, const float4* __restrict__ pad_pts) {
     const int pos = blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= n) return;
+    if (pad_pts && __float_as_uint(pad_pts[pos].w) == 0xffffffffu) {
+        out[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
     const float4 m = in[pos];
     float x = m.x, y = m.y, z = m.z;
     const int cnt = min(ki, n);
@@ -413,7 +444,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) interpolate_kernel(Interp
             heap.sort_ascending();
             float4 m = A.in[pos];
             float x = m.x, y = m.y, z = m.z;
-            const int cnt = min(A.K, A.T.n);
+            const int cnt = heap.real;
 #pragma unroll 4
             for (int s = 0; s < cnt; s++) {
                 const unsigned long long key = heap.at(s);
@@ -587,6 +618,9 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.stats = d_stats;
         A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
         A.ki = ki;
+        A.segs = nullptr;
+        A.bucket_scan = nullptr;
+        A.nq_dev = nullptr;
         HeapPlan P = plan_heap(nq, K, ws);
         A.gheap = P.gheap;
         const int threads = kWarpsPerBlock * 32;
@@ -614,6 +648,69 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
     }
 }
 
+void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
+                               const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
+                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki) {
+    const int n = T.n;
+    if (n == 0) return;
+    if (g_num_sms == 0) {
+        int dev = 0;
+        LVRGB_CUDA(cudaGetDevice(&dev));
+        LVRGB_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    uint32_t* lists[2] = {ws.get<uint32_t>("segn.listA", size_t(n)), ws.get<uint32_t>("segn.listB", size_t(n))};
+    uint32_t* counters = ws.get<uint32_t>("segn.counters", 8);
+    LVRGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s));
+    const int rounds = cfg.adaptive ? 5 : 1;
+    size_t k = size_t(cfg.kn);
+    for (int round = 1; round <= rounds; round++) {
+        k *= 2;  // the reference doubles k before every search
+        const int K = int(std::min<size_t>(k, size_t(1) << 20));
+        NormalsArgs A;
+        A.T = T;
+        A.K = K;
+        A.nem = cfg.nem;
+        A.adaptive = cfg.adaptive;
+        A.last_round = round == rounds;
+        A.round = round;
+        A.list = round == 1 ? nullptr : lists[round & 1];
+        A.nq = n;
+        A.nq_dev = round == 1 ? nullptr : counters + (round - 2);
+        A.fx = cfg.flip[0]; A.fy = cfg.flip[1]; A.fz = cfg.flip[2];
+        A.gap_thr = cfg.gap_threshold;
+        A.normals = normals;
+        A.kused = kused;
+        A.retry = lists[(round + 1) & 1];
+        A.retry_count = counters + (round - 1);
+        A.err = d_err;
+        A.stats = d_stats;
+        A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
+        A.ki = ki;
+        A.segs = segs;
+        A.bucket_scan = bucket_scan;
+        // Later rounds read their query count on the device: launch a fixed
+        // grid that strides over however many queries the previous round left.
+        HeapPlan P = plan_heap(round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), K, ws);
+        A.gheap = P.gheap;
+        const int threads = kWarpsPerBlock * 32;
+        switch (cfg.nem) {
+            case 2:
+                set_smem(normals_kernel<2>, P.smem);
+                normals_kernel<2><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+            case 3:
+                set_smem(normals_kernel<3>, P.smem);
+                normals_kernel<3><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+            default:
+                set_smem(normals_kernel<0>, P.smem);
+                normals_kernel<0><<<P.blocks, threads, P.smem, s>>>(A);
+                break;
+        }
+        LVRGB_LAUNCH_CHECK();
+    }
+}
+
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,
                          cudaStream_t s) {
     if (T.n == 0) return;
@@ -634,9 +731,10 @@ void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, W
     LVRGB_LAUNCH_CHECK();
 }
 
-void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s) {
+void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s,
+                            const float4* pad_pts) {
     if (n == 0) return;
-    interpolate_lists_kernel<<<ceil_div(n, 256), 256, 0, s>>>(in, nbr, n, ki, out);
+    interpolate_lists_kernel<<<ceil_div(n, 256), 256, 0, s>>>(in, nbr, n, ki, out, pad_pts);
     LVRGB_LAUNCH_CHECK();
 }
 

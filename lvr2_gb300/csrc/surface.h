@@ -29,7 +29,18 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
                      int* d_err, uint32_t* d_stats, cudaStream_t s, uint32_t* nbr = nullptr, int ki = 0);
 
 // Interpolation from the neighbour lists written by compute_normals.
-void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s);
+// pad_pts (optional): the tree's points, whose padding positions get a zero
+// normal.
+void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in, float4* out, cudaStream_t s,
+                            const float4* pad_pts = nullptr);
+
+// compute_normals over a segmented tree (one search tree per scan, per-scan
+// flip points).  All rounds are launched without host synchronisation: each
+// later round reads the previous round's retry count on the device, so the
+// sequence can be captured in a CUDA graph.
+void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
+                               const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
+                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki);
 
 // out_i = normalize(in_i + sum_{j in kNN_ki(p_i)} in_j), Morton order.
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,

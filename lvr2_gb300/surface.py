@@ -243,6 +243,73 @@ class Surface:
         return a, v
 
 
+class Batch:
+    """Normals for every scan of a scan project in one pass (lvrgb_batch_*):
+    the per-scan CudaSurface runs of lvr2_cuda_normals' directory mode, with
+    kNN restricted to each scan and each scan flipped toward its own point."""
+
+    def __init__(self, scans, flip_points, kn=10, ki=10, nem=3, adaptive=True, bucket=32, seed_radius=1,
+                 gap_threshold=1e-3, device=0, stream=None):
+        L = _lib.load()
+        cfg = SurfaceConfig()
+        L.lvrgb_surface_config_default(ctypes.byref(cfg))
+        cfg.kn, cfg.ki, cfg.nem = int(kn), int(ki), int(nem)
+        cfg.adaptive = int(bool(adaptive))
+        cfg.bucket, cfg.seed_radius = int(bucket), int(seed_radius)
+        cfg.gap_threshold = float(gap_threshold)
+        cfg.device = int(device)
+        if isinstance(scans, (list, tuple)):
+            sizes = [len(s) for s in scans]
+            pts = np.ascontiguousarray(np.concatenate([np.asarray(s, np.float32).reshape(-1, 3) for s in scans]))
+            on_dev = 0
+        else:
+            raise ValueError("scans must be a list of (n_i, 3) arrays")
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.flips = np.ascontiguousarray(flip_points, np.float32).reshape(-1, 3)
+        self.n = int(self.offsets[-1])
+        self._stream = _stream_ptr(stream)
+        self._h = ctypes.c_void_p()
+        check(L.lvrgb_batch_create(ctypes.byref(cfg), _ptr(pts), _ptr(self.offsets), len(sizes), _ptr(self.flips),
+                                   on_dev, self._stream, ctypes.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().lvrgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def calculate_normals(self, use_graph=False):
+        check(_lib.load().lvrgb_batch_calculate_normals(self._h, int(bool(use_graph)), self._stream))
+
+    def normals(self):
+        out = np.empty((self.n, 3), np.float32)
+        check(_lib.load().lvrgb_batch_get_normals(self._h, _ptr(out), 0, self._stream))
+        return out
+
+    def autotune(self):
+        b = np.zeros(1, np.int32)
+        r = np.zeros(1, np.int32)
+        check(_lib.load().lvrgb_batch_autotune(self._h, _ptr(b), _ptr(r), self._stream))
+        return int(b[0]), int(r[0])
+
+    def stats(self):
+        c = np.zeros(16, np.uint32)
+        ms = np.zeros(4, np.float32)
+        check(_lib.load().lvrgb_batch_stats(self._h, _ptr(c), _ptr(ms)))
+        return c, ms
+
+
 def kernel_launches():
     """Kernels launched by liblvrgb.so in this process."""
     out = np.zeros(1, np.uint64)
@@ -250,4 +317,4 @@ def kernel_launches():
     return int(out[0])
 
 
-__all__ = ["Surface", "LvrgbError", "kernel_launches"]
+__all__ = ["Surface", "Batch", "LvrgbError", "kernel_launches"]
