@@ -407,9 +407,10 @@ __global__ void interpolate_lists_kernel(const float4* __restrict__ in, const ui
     const float4 m = in[pos];
     float x = m.x, y = m.y, z = m.z;
     const int cnt = min(ki, n);
-#pragma unroll 4
     for (int s = 0; s < cnt; s++) {
-        const float4 nj = __ldg(in + __ldg(nbr + size_t(s) * n + pos));
+        const uint32_t j = __ldg(nbr + size_t(s) * n + pos);
+        if (j == 0xffffffffu) break;  // fewer neighbours than ki (a small scan)
+        const float4 nj = __ldg(in + j);
         x = __fadd_rn(x, nj.x);
         y = __fadd_rn(y, nj.y);
         z = __fadd_rn(z, nj.z);
