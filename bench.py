@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--bucket", type=int, default=32, help="LBVH bucket size (tuning)")
     ap.add_argument("--seed-radius", type=int, default=1, help="seed buckets on each side (tuning)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the scan-project (batched) measurement")
+    ap.add_argument("--batched-scale", type=float, default=1.0, help="scale of the 64-scan project")
     return ap.parse_args()
 
 
@@ -148,6 +150,47 @@ def normal_bytes(stats, kn):
 
 def sdf_bytes(n_vertices, kd):
     return n_vertices * (12 + 32 * kd + 4 + 1)
+
+
+def batched_measurement(args, steps):
+    """Scan project: 64 scans, log-uniform 50k-4M points (~60M), per-scan flip
+    point at the scanner, kn = ki = 10, PCA.  The batched form (one segmented
+    LBVH, one launch per search round, CUDA graph replay, autotuned) against
+    the plain form (one surface per scan, one after the other) on the same GPU."""
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    scans, flips = synthetic.scan_project_device(64, seed=4, scale=args.batched_scale, device="cuda")
+    n = sum(int(s.shape[0]) for s in scans)
+    # plain: a surface per scan
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for rep in range(2):
+        torch.cuda.synchronize()
+        ev0.record()
+        for sc, f in zip(scans, flips):
+            with lvr2_gb300.Surface(sc, kn=10, ki=10, nem=3, flip_point=f) as s:
+                s.calculate_normals()
+        ev1.record()
+        torch.cuda.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+    with lvr2_gb300.Batch(scans, flips, kn=10, ki=10, nem=3) as b:
+        bucket, radius = b.autotune()
+        b.calculate_normals(use_graph=True)
+        times = []
+        for _ in range(max(steps, 1)):
+            b.calculate_normals(use_graph=True)
+            times.append(float(b.stats()[1][3]))
+        counters, _ = b.stats()
+        b.calculate_normals(use_graph=False)
+        _, stage = b.stats()
+    batched_ms = float(np.mean(times))
+    return {"workload": "scan_project_64", "scans": 64, "points": n, "kn": 10, "ki": 10, "nem": 3,
+            "plain_ms": plain_ms, "plain_normals_per_s": n / (plain_ms / 1000.0),
+            "batched_ms": batched_ms, "batched_normals_per_s": n / (batched_ms / 1000.0),
+            "speedup_vs_plain": plain_ms / batched_ms, "autotuned": {"bucket": bucket, "seed_radius": radius},
+            "batched_stage_ms": {"tree": float(stage[0]), "normals": float(stage[1]), "interpolation": float(stage[2])},
+            "fitted_per_round": [int(x) for x in counters[:5]], "graph": True}
 
 
 def cpu_reference_step(points, threads=0, canonical=False):
@@ -326,6 +369,8 @@ def run_gpu(args):
         "clocks": clocks.summary(),
         "e2e": e2e,
     }
+    if not args.no_batched:
+        line["batched"] = batched_measurement(args, args.steps)
     if not args.no_cpu_baseline:
         sample = cpu_sample(pts)
         dt, _ = cpu_reference_step(sample)

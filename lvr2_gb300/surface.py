@@ -258,12 +258,16 @@ class Batch:
         cfg.bucket, cfg.seed_radius = int(bucket), int(seed_radius)
         cfg.gap_threshold = float(gap_threshold)
         cfg.device = int(device)
-        if isinstance(scans, (list, tuple)):
-            sizes = [len(s) for s in scans]
+        if not isinstance(scans, (list, tuple)):
+            raise ValueError("scans must be a list of (n_i, 3) arrays")
+        sizes = [len(s) for s in scans]
+        if scans and _is_torch_cuda(scans[0]):
+            import torch
+            pts = torch.cat([s.reshape(-1, 3).float() for s in scans]).contiguous()
+            on_dev = 1
+        else:
             pts = np.ascontiguousarray(np.concatenate([np.asarray(s, np.float32).reshape(-1, 3) for s in scans]))
             on_dev = 0
-        else:
-            raise ValueError("scans must be a list of (n_i, 3) arrays")
         self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
         self.flips = np.ascontiguousarray(flip_points, np.float32).reshape(-1, 3)
         self.n = int(self.offsets[-1])

@@ -244,3 +244,71 @@ def crop(points, fraction, center=None):
             break
         side *= (fraction / max(got, 1e-9)) ** (1 / 3)
     return p[sel]
+
+
+def _raycast_torch(origin, d, boxes, cyls, ground_y):
+    import torch
+    o = origin
+    inf = torch.full((d.shape[0],), float("inf"), device=d.device, dtype=d.dtype)
+    t = inf.clone()
+    tp = (ground_y - o[1]) / d[:, 1]
+    t = torch.where(tp > 1e-6, torch.minimum(t, tp), t)
+    for b in boxes:
+        lo = torch.tensor([b[0], b[2], b[4]], device=d.device, dtype=d.dtype)
+        hi = torch.tensor([b[1], b[3], b[5]], device=d.device, dtype=d.dtype)
+        t1 = (lo - o) / d
+        t2 = (hi - o) / d
+        tn = torch.nan_to_num(torch.minimum(t1, t2), nan=-float("inf")).amax(dim=1)
+        tf = torch.nan_to_num(torch.maximum(t1, t2), nan=float("inf")).amin(dim=1)
+        hit = (tf >= tn) & (tf > 1e-6)
+        th = torch.where(tn > 1e-6, tn, tf)
+        t = torch.where(hit, torch.minimum(t, th), t)
+    for cx, cz, r, h in cyls:
+        ox, oz = o[0] - cx, o[2] - cz
+        a = d[:, 0] ** 2 + d[:, 2] ** 2
+        bq = 2 * (ox * d[:, 0] + oz * d[:, 2])
+        c = ox * ox + oz * oz - r * r
+        disc = bq * bq - 4 * a * c
+        sq = torch.sqrt(torch.clamp(disc, min=0))
+        for tc in ((-bq - sq) / (2 * a), (-bq + sq) / (2 * a)):
+            y = o[1] + tc * d[:, 1]
+            ok = (disc >= 0) & (tc > 1e-6) & (y >= ground_y) & (y <= ground_y + h)
+            t = torch.where(ok, torch.minimum(t, tc), t)
+    return t
+
+
+def scan_project_device(n_scans=64, seed=4, lo=50_000, hi=4_000_000, sigma=0.5, scale=1.0, device="cuda"):
+    """scan_project's construction evaluated with torch on a device (seeded
+    torch generator; a different random stream than scan_project), for
+    full-size projects.  Returns (list of device (n_i, 3) float32 tensors,
+    flip points (n_scans, 3) float32 numpy)."""
+    import torch
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_scans)) * scale
+    sizes = np.maximum(sizes.astype(np.int64), 16)
+    scans, flips = [], []
+    for i in range(n_scans):
+        while True:
+            pose = np.array([rng.uniform(-800, 1450), GROUND_Y + 1.5, rng.uniform(20, 790)])
+            inside = any((b[0] <= pose[0] <= b[1]) and (b[4] <= pose[2] <= b[5]) for b in BOXES)
+            inside |= any((pose[0] - c[0]) ** 2 + (pose[2] - c[1]) ** 2 <= c[2] ** 2 for c in CYLINDERS)
+            if not inside:
+                break
+        m = int(sizes[i])
+        o = torch.tensor(pose, device=device, dtype=torch.float32)
+        parts, have = [], 0
+        while have < m:
+            k = max(2 * (m - have), 50_000)
+            d = torch.randn((k, 3), generator=gen, device=device)
+            d = d / d.norm(dim=1, keepdim=True)
+            t = _raycast_torch(o, d, BOXES, CYLINDERS, GROUND_Y)
+            ok = torch.isfinite(t) & (t < 3000)
+            noise = torch.randn((int(ok.sum()),), generator=gen, device=device) * sigma
+            p = o + d[ok] * (t[ok] + noise)[:, None]
+            parts.append(p)
+            have += p.shape[0]
+        scans.append(torch.cat(parts)[:m].contiguous())
+        flips.append(pose.astype(np.float32))
+    return scans, np.array(flips, np.float32)
