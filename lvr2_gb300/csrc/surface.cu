@@ -6,6 +6,7 @@
 
 #include "primitives.cuh"
 #include "surface.h"
+#include "wide.cuh"
 
 namespace lvrgb {
 
@@ -195,31 +196,27 @@ __device__ __forceinline__ void neighbour_pass(const Lbvh& T, const LaneHeap& he
     }
 }
 
+// Mean of the neighbourhood relative to q: nem 3 includes q itself
+// (calcPlaneIPCAExact starts its incremental mean at the query point).
 template <int kNem>
-__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, int cnt, float4 q,
-                                          const NbrPass& P, float n[3], bool& fp64) {
+__device__ __forceinline__ void plane_mean(const float s[3], int cnt, float mean[3]) {
+    const float m = kNem == 3 ? float(cnt + 1) : float(cnt > 0 ? cnt : 1);
+    mean[0] = s[0] / m;
+    mean[1] = s[1] / m;
+    mean[2] = s[2] / m;
+}
+
+// Plane normal from the neighbourhood sums.
+//   nem 3: S = covariance sums about the centroid, q included (xx xy xz yy yz zz)
+//   nem 0: S = sums about the centroid (xx xz zz xy zy); mean relative to q
+//   nem 2: r = sums of (p - q)(p - q)^T in IEEE order
+template <int kNem>
+__device__ __forceinline__ void solve_plane(float gap_thr, float4 q, const float mean[3], const float S[6],
+                                            const float r[6], float n[3], bool& fp64) {
     fp64 = false;
     if (kNem == 3) {
-        // PCA of {q} and its neighbours (calcPlaneIPCAExact starts its
-        // incremental mean at the query point): covariance about the centroid,
-        // second pass, coordinates relative to q, compensated sums.
-        const float m = float(cnt + 1);
-        const float mx = P.s[0] / m, my = P.s[1] / m, mz = P.s[2] / m;
-        float S[6] = {mx * mx, mx * my, mx * mz, my * my, my * mz, mz * mz};  // the query point itself
-        float C[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 4
-        for (int s = 0; s < cnt; s++) {
-            const float4 p = neighbour_point(A.T, heap.at(s));
-            const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
-            kahan_add(S[0], C[0], ex * ex);
-            kahan_add(S[1], C[1], ex * ey);
-            kahan_add(S[2], C[2], ex * ez);
-            kahan_add(S[3], C[3], ey * ey);
-            kahan_add(S[4], C[4], ey * ez);
-            kahan_add(S[5], C[5], ez * ez);
-        }
         float v[3];
-        if (eig_smallest_f32(S, A.gap_thr, v)) {
+        if (eig_smallest_f32(S, gap_thr, v)) {
             n[0] = v[0]; n[1] = v[1]; n[2] = v[2];
         } else {
             double D[6], w[3];
@@ -231,7 +228,7 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
     } else if (kNem == 2) {
         // calcPlaneIterative: the largest of the three cofactor determinants
         // of the sums of (p - q)(p - q)^T.
-        const float xx = P.r[0], xy = P.r[1], xz = P.r[2], yy = P.r[3], yz = P.r[4], zz = P.r[5];
+        const float xx = r[0], xy = r[1], xz = r[2], yy = r[3], yz = r[4], zz = r[5];
         const float det_x = __fsub_rn(__fmul_rn(yy, zz), __fmul_rn(yz, yz));
         const float det_y = __fsub_rn(__fmul_rn(xx, zz), __fmul_rn(xz, xz));
         const float det_z = __fsub_rn(__fmul_rn(xx, yy), __fmul_rn(xy, xy));
@@ -258,19 +255,7 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
         // calcPlane (nem 0): least-squares y = C0 + C1 x + C2 z over the
         // neighbours; centred FP32 sums relative to q, 2x2 solve in FP64,
         // then the reference's two in-plane vectors at +100 offsets.
-        const float m = float(cnt > 0 ? cnt : 1);
-        const float mx = P.s[0] / m, my = P.s[1] / m, mz = P.s[2] / m;
-        float S[5] = {0, 0, 0, 0, 0}, C[5] = {0, 0, 0, 0, 0};  // xx xz zz xy zy
-#pragma unroll 4
-        for (int s = 0; s < cnt; s++) {
-            const float4 p = neighbour_point(A.T, heap.at(s));
-            const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
-            kahan_add(S[0], C[0], ex * ex);
-            kahan_add(S[1], C[1], ex * ez);
-            kahan_add(S[2], C[2], ez * ez);
-            kahan_add(S[3], C[3], ex * ey);
-            kahan_add(S[4], C[4], ez * ey);
-        }
+        const float mx = mean[0], my = mean[1], mz = mean[2];
         const double sxx = S[0], sxz = S[1], szz = S[2], sxy = S[3], szy = S[4];
         const double det = sxx * szz - sxz * sxz;
         double c1 = 0, c2 = 0;
@@ -291,6 +276,50 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
         normalize_ieee(nx, ny, nz);
         n[0] = nx; n[1] = ny; n[2] = nz;
     }
+}
+
+// Second pass over a lane's heap: the centred sums of nem 3 / nem 0.
+template <int kNem>
+__device__ __forceinline__ void centred_sums(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q,
+                                             const float mean[3], float S[6]) {
+    const float mx = mean[0], my = mean[1], mz = mean[2];
+    float C[6] = {0, 0, 0, 0, 0, 0};
+    if (kNem == 3) {
+        // the query point itself, then the neighbours
+        S[0] = mx * mx; S[1] = mx * my; S[2] = mx * mz; S[3] = my * my; S[4] = my * mz; S[5] = mz * mz;
+    } else {
+        for (int i = 0; i < 6; i++) S[i] = 0.0f;
+    }
+#pragma unroll 4
+    for (int s = 0; s < cnt; s++) {
+        const float4 p = neighbour_point(T, heap.at(s));
+        const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
+        if (kNem == 3) {
+            kahan_add(S[0], C[0], ex * ex);
+            kahan_add(S[1], C[1], ex * ey);
+            kahan_add(S[2], C[2], ex * ez);
+            kahan_add(S[3], C[3], ey * ey);
+            kahan_add(S[4], C[4], ey * ez);
+            kahan_add(S[5], C[5], ez * ez);
+        } else {
+            kahan_add(S[0], C[0], ex * ex);
+            kahan_add(S[1], C[1], ex * ez);
+            kahan_add(S[2], C[2], ez * ez);
+            kahan_add(S[3], C[3], ex * ey);
+            kahan_add(S[4], C[4], ez * ey);
+        }
+    }
+}
+
+template <int kNem>
+__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, int cnt, float4 q,
+                                          const NbrPass& P, float n[3], bool& fp64) {
+    float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0};
+    if (kNem != 2) {
+        plane_mean<kNem>(P.s, cnt, mean);
+        centred_sums<kNem>(A.T, heap, cnt, q, mean, S);
+    }
+    solve_plane<kNem>(A.gap_thr, q, mean, S, P.r, n, fp64);
 }
 
 template <int kNem>
@@ -391,6 +420,216 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         atomicAdd(A.stats + 10, pushes);
         atomicAdd(A.stats + 11, st.chunks);
         atomicAdd(A.stats + 12, st.rounds);
+    }
+}
+
+// normals_kernel for K > kSmemHeapMax: one warp per query (wide.cuh), the
+// neighbourhood sums reduced across the warp.  The neighbour set, the box
+// test and therefore the round in which a point is fitted are the same as in
+// the per-lane kernel.
+// x * 2^e, exact unless the result leaves the normal range.
+__device__ __forceinline__ float mul_pow2(float x, int e) {
+    while (e > 126) {
+        x = __fmul_rn(x, __int_as_float(253 << 23));  // 2^126
+        e -= 126;
+    }
+    while (e < -126) {
+        x = __fmul_rn(x, __int_as_float(1 << 23));  // 2^-126
+        e += 126;
+    }
+    return __fmul_rn(x, __int_as_float((e + 127) << 23));
+}
+
+// E with |p - q| < 2^E for every point p of the box [lo, hi].
+__device__ __forceinline__ int box_exponent(const float lo[3], const float hi[3], float4 q) {
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(lo[0], q.x)), fabsf(__fsub_rn(hi[0], q.x))),
+                                fmaxf(fabsf(__fsub_rn(lo[1], q.y)), fabsf(__fsub_rn(hi[1], q.y)))),
+                          fmaxf(fabsf(__fsub_rn(lo[2], q.z)), fabsf(__fsub_rn(hi[2], q.z))));
+    if (!(m > 0.0f) || !(m <= FLT_MAX)) return 0;
+    const unsigned b = __float_as_uint(m);
+    const int biased = int(b >> 23);
+    if (biased == 0) return 32 - __clz(int(b)) - 149;  // subnormal: m = b * 2^-149
+    return biased - 126;                               // m = 1.f * 2^(biased - 127)
+}
+
+// 64-bit fixed point with 40 fractional bits: terms below 4 in magnitude and
+// up to 2^20 of them stay below 2^62.
+__device__ __forceinline__ long long to_fixed(float v) {
+    return __float2ll_rn(__fmul_rn(v, 1099511627776.0f));  // 2^40
+}
+__device__ __forceinline__ float from_fixed(long long v) { return float(double(v) * (1.0 / 1099511627776.0)); }
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+constexpr int kWideWarps = 8;  // warps per block
+constexpr int kWideTile = 8;   // queries per warp tile
+
+template <int kNem>
+__global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    WideState W;
+    W.K = A.K;
+    W.cap = wide_capacity(A.K);
+    W.hist = reinterpret_cast<uint32_t*>(smem) + wib * 256;
+    W.keys = A.gheap ? A.gheap + (size_t(blockIdx.x) * kWideWarps + wib) * size_t(W.cap)
+                     : reinterpret_cast<unsigned long long*>(smem + kWideWarps * 1024) + size_t(wib) * W.cap;
+    const int nq = A.nq_dev ? int(*A.nq_dev) : A.nq;
+    const int B = A.T.bucket;
+    TravStats st;
+    for (int tile = blockIdx.x * kWideWarps + wib; tile * kWideTile < nq; tile += gridDim.x * kWideWarps) {
+        unsigned fitted = 0, retry = 0;
+        int my_pos = 0;
+        const int nt = min(kWideTile, nq - tile * kWideTile);
+        for (int j = 0; j < nt; j++) {
+            const int qi = tile * kWideTile + j;
+            const int pos = A.list ? int(__ldg(A.list + qi)) : qi;
+            const float4 q = __ldg(A.T.pts + pos);
+            int root = 0, blo = 0, bhi = 0x7fffffff;
+            float fx = A.fx, fy = A.fy, fz = A.fz;
+            if (A.segs) {
+                if (__float_as_uint(q.w) == 0xffffffffu) continue;  // padding after a scan
+                const SegInfo g = A.segs[A.bucket_scan[pos / B]];
+                root = g.root; blo = g.blo; bhi = g.bhi;
+                fx = g.fx; fy = g.fy; fz = g.fz;
+            }
+            wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, pos / B, root, blo, bhi);
+            const int cnt = W.cnt;
+            // pass 1: neighbourhood box (min / max: exact in any order)
+            float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            for (int i = lane; i < cnt; i += 32) {
+                const float4 p = neighbour_point(A.T, W.keys[i]);
+                lo[0] = fminf(p.x, lo[0]); lo[1] = fminf(p.y, lo[1]); lo[2] = fminf(p.z, lo[2]);
+                hi[0] = fmaxf(p.x, hi[0]); hi[1] = fmaxf(p.y, hi[1]); hi[2] = fmaxf(p.z, hi[2]);
+            }
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                lo[a] = warp_min_f(lo[a]);
+                hi[a] = warp_max_f(hi[a]);
+            }
+            bool fit = true;
+            if (A.adaptive && !A.last_round) {
+                // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
+                const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
+                const float e = 0.05f;
+                fit = dx >= __fmul_rn(e, dy) && dx >= __fmul_rn(e, dz) && dy >= __fmul_rn(e, dx) &&
+                      dy >= __fmul_rn(e, dz) && dz >= __fmul_rn(e, dx) && dz >= __fmul_rn(e, dy);
+            }
+            if (!fit) {
+                retry |= 1u << j;
+                if (lane == j) my_pos = pos;
+                continue;
+            }
+            // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
+            // box), accumulated in 64-bit fixed point: exact and independent
+            // of the order in which the search left the neighbours, so every
+            // tree layout of the same points gives the same normal.
+            const int E = box_exponent(lo, hi, q);
+            float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0}, r[6] = {0, 0, 0, 0, 0, 0};
+            if (kNem == 2) {
+                long long acc[6] = {0, 0, 0, 0, 0, 0};
+                for (int i = lane; i < cnt; i += 32) {
+                    const float4 p = neighbour_point(A.T, W.keys[i]);
+                    const float ux = mul_pow2(__fsub_rn(p.x, q.x), -E), uy = mul_pow2(__fsub_rn(p.y, q.y), -E),
+                                uz = mul_pow2(__fsub_rn(p.z, q.z), -E);
+                    acc[0] += to_fixed(__fmul_rn(ux, ux));
+                    acc[1] += to_fixed(__fmul_rn(ux, uy));
+                    acc[2] += to_fixed(__fmul_rn(ux, uz));
+                    acc[3] += to_fixed(__fmul_rn(uy, uy));
+                    acc[4] += to_fixed(__fmul_rn(uy, uz));
+                    acc[5] += to_fixed(__fmul_rn(uz, uz));
+                }
+#pragma unroll
+                for (int a = 0; a < 6; a++) r[a] = from_fixed(warp_sum_ll(acc[a]));
+            } else {
+                long long acc1[3] = {0, 0, 0};
+                for (int i = lane; i < cnt; i += 32) {
+                    const float4 p = neighbour_point(A.T, W.keys[i]);
+                    acc1[0] += to_fixed(mul_pow2(__fsub_rn(p.x, q.x), -E));
+                    acc1[1] += to_fixed(mul_pow2(__fsub_rn(p.y, q.y), -E));
+                    acc1[2] += to_fixed(mul_pow2(__fsub_rn(p.z, q.z), -E));
+                }
+                float su[3], mu[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++) su[a] = from_fixed(warp_sum_ll(acc1[a]));
+                plane_mean<kNem>(su, cnt, mu);
+                long long acc[6] = {0, 0, 0, 0, 0, 0};
+                for (int i = lane; i < cnt; i += 32) {
+                    const float4 p = neighbour_point(A.T, W.keys[i]);
+                    const float ex = __fsub_rn(mul_pow2(__fsub_rn(p.x, q.x), -E), mu[0]);
+                    const float ey = __fsub_rn(mul_pow2(__fsub_rn(p.y, q.y), -E), mu[1]);
+                    const float ez = __fsub_rn(mul_pow2(__fsub_rn(p.z, q.z), -E), mu[2]);
+                    if (kNem == 3) {
+                        acc[0] += to_fixed(__fmul_rn(ex, ex));
+                        acc[1] += to_fixed(__fmul_rn(ex, ey));
+                        acc[2] += to_fixed(__fmul_rn(ex, ez));
+                        acc[3] += to_fixed(__fmul_rn(ey, ey));
+                        acc[4] += to_fixed(__fmul_rn(ey, ez));
+                        acc[5] += to_fixed(__fmul_rn(ez, ez));
+                    } else {
+                        acc[0] += to_fixed(__fmul_rn(ex, ex));
+                        acc[1] += to_fixed(__fmul_rn(ex, ez));
+                        acc[2] += to_fixed(__fmul_rn(ez, ez));
+                        acc[3] += to_fixed(__fmul_rn(ex, ey));
+                        acc[4] += to_fixed(__fmul_rn(ez, ey));
+                    }
+                }
+                // nem 3: the query point's own term (its offset from the mean is -mu)
+                const float own[6] = {__fmul_rn(mu[0], mu[0]), __fmul_rn(mu[0], mu[1]), __fmul_rn(mu[0], mu[2]),
+                                      __fmul_rn(mu[1], mu[1]), __fmul_rn(mu[1], mu[2]), __fmul_rn(mu[2], mu[2])};
+#pragma unroll
+                for (int a = 0; a < 6; a++) {
+                    const long long own_fx = (kNem == 3) ? to_fixed(own[a]) : 0ll;
+                    S[a] = from_fixed(warp_sum_ll(acc[a]) + own_fx);
+                }
+                // the plane offset of nem 0 needs the mean in world units
+#pragma unroll
+                for (int a = 0; a < 3; a++) mean[a] = mul_pow2(mu[a], E);
+            }
+            float n[3];
+            bool fp64;
+            solve_plane<kNem>(A.gap_thr, q, mean, S, r, n, fp64);
+            // Flip toward the flip point; Normal::operator-() re-normalises.
+            const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
+            const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
+            if (dot < 0.0f) {
+                n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
+                normalize_ieee(n[0], n[1], n[2]);
+            }
+            if (lane == 0) {
+                A.normals[pos] = make_float4(n[0], n[1], n[2], 0.0f);
+                if (A.kused) A.kused[pos] = A.K;
+                if (fp64) atomicAdd(A.stats + 5, 1u);
+            }
+            if (A.nbr) {
+                // kNN(ki) of the interpolation = the first ki of this kNN(K >= ki)
+                const int m = min(A.ki, cnt);
+                uint32_t* col = A.nbr + pos;
+                const size_t stride = size_t(A.T.n);
+                const uint32_t* inv = A.T.inv;
+                wide_sorted_prefix(W, m, [&](int rank, unsigned long long key) {
+                    col[size_t(rank) * stride] = __ldg(inv + key_idx(key));
+                });
+                for (int t = m + lane; t < A.ki; t += 32) col[size_t(t) * stride] = 0xffffffffu;
+            }
+            fitted |= 1u << j;
+        }
+        if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
+        if (retry) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(A.retry_count, uint32_t(__popc(retry)));
+            base = __shfl_sync(kFull, base, 0);
+            if ((retry >> lane) & 1u) A.retry[base + __popc(retry & lt)] = uint32_t(my_pos);
+        }
+    }
+    if (lane == 0 && st.nodes) {
+        atomicAdd(A.stats + 8, st.buckets);
+        atomicAdd(A.stats + 9, st.nodes);
     }
 }
 
@@ -560,6 +799,12 @@ void set_smem(Kernel k, size_t bytes) {
     if (bytes > 48 * 1024) LVRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
+// Launches the normals kernel for one search round: per-lane heaps up to
+// kSmemHeapMax, one warp per query above.  grid_nq: the number of queries the
+// grid is sized for (the round's count, or a cap when the count is on the
+// device).
+void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s);
+
 }  // namespace
 
 HeapPlan plan_heap(int nq, int K, Workspace& ws) {
@@ -583,6 +828,52 @@ HeapPlan plan_heap(int nq, int K, Workspace& ws) {
     }
     return p;
 }
+
+namespace {
+
+template <int kNem>
+void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
+    if (A.K <= kSmemHeapMax) {
+        HeapPlan P = plan_heap(grid_nq, A.K, ws);
+        A.gheap = P.gheap;
+        set_smem(normals_kernel<kNem>, P.smem);
+        normals_kernel<kNem><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+        LVRGB_LAUNCH_CHECK();
+        return;
+    }
+    // one warp per query; key buffers in shared memory when they fit
+    const size_t per_warp = size_t(wide_capacity(A.K)) * sizeof(unsigned long long);
+    const int tiles = ceil_div(std::max(grid_nq, 1), kWideTile);
+    const int need = std::max(1, ceil_div(tiles, kWideWarps));
+    size_t smem = size_t(kWideWarps) * 1024;
+    int blocks = need;
+    A.gheap = nullptr;
+    if (smem + kWideWarps * per_warp <= size_t(200) * 1024) {
+        smem += kWideWarps * per_warp;
+    } else {
+        const int maxb = int(std::max<size_t>(1, (size_t(1) << 31) / (kWideWarps * per_warp)));
+        blocks = std::min({need, g_num_sms * 4, maxb});
+        A.gheap = ws.get<unsigned long long>("knn.widebuf", size_t(blocks) * kWideWarps * (per_warp / 8));
+    }
+    set_smem(normals_wide_kernel<kNem>, smem);
+    normals_wide_kernel<kNem><<<blocks, kWideWarps * 32, smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        LVRGB_CUDA(cudaGetDevice(&dev));
+        LVRGB_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    switch (A.nem) {
+        case 2: launch_normals_nem<2>(A, grid_nq, ws, s); break;
+        case 3: launch_normals_nem<3>(A, grid_nq, ws, s); break;
+        default: launch_normals_nem<0>(A, grid_nq, ws, s); break;
+    }
+}
+
+}  // namespace
 
 void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
                      int* d_err, uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki) {
@@ -622,24 +913,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.segs = nullptr;
         A.bucket_scan = nullptr;
         A.nq_dev = nullptr;
-        HeapPlan P = plan_heap(nq, K, ws);
-        A.gheap = P.gheap;
-        const int threads = kWarpsPerBlock * 32;
-        switch (cfg.nem) {
-            case 2:
-                set_smem(normals_kernel<2>, P.smem);
-                normals_kernel<2><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-            case 3:
-                set_smem(normals_kernel<3>, P.smem);
-                normals_kernel<3><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-            default:
-                set_smem(normals_kernel<0>, P.smem);
-                normals_kernel<0><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-        }
-        LVRGB_LAUNCH_CHECK();
+        launch_normals(A, nq, ws, s);
         if (last) break;
         h_count[0] = 0;
         LVRGB_CUDA(cudaMemcpyAsync(h_count, counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -691,24 +965,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.bucket_scan = bucket_scan;
         // Later rounds read their query count on the device: launch a fixed
         // grid that strides over however many queries the previous round left.
-        HeapPlan P = plan_heap(round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), K, ws);
-        A.gheap = P.gheap;
-        const int threads = kWarpsPerBlock * 32;
-        switch (cfg.nem) {
-            case 2:
-                set_smem(normals_kernel<2>, P.smem);
-                normals_kernel<2><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-            case 3:
-                set_smem(normals_kernel<3>, P.smem);
-                normals_kernel<3><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-            default:
-                set_smem(normals_kernel<0>, P.smem);
-                normals_kernel<0><<<P.blocks, threads, P.smem, s>>>(A);
-                break;
-        }
-        LVRGB_LAUNCH_CHECK();
+        launch_normals(A, round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), ws, s);
     }
 }
 

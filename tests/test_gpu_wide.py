@@ -1,0 +1,111 @@
+"""GPU parity of the large-k searches (k above the per-lane heap limit of 96),
+which run one warp per query.
+
+Points on axis-aligned planes fail lvr2's neighbourhood-box test in every
+adaptive round but the last (AdaptiveKSearchSurface.tcc:218-268), so a room
+of flat walls sends every point to k = 32 kn.  Bars as in test_gpu_parity:
+adaptive round per point identical to the oracle, normals within 0.5 degrees
+at the 99.9th percentile, interpolation bit-exact, kNN rows bit-exact.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import angle_deg
+
+pytestmark = pytest.mark.gpu
+
+ANGLE_P999_DEG = 0.5
+
+
+@pytest.fixture(scope="module")
+def gb(lib):
+    import lvr2_gb300
+    return lvr2_gb300
+
+
+def room(n, seed=0, jitter=0.0):
+    """Points on the six walls of an axis-aligned box (2 x 1.5 x 1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ext = np.array([2.0, 1.5, 1.0])
+    pts = []
+    per = n // 6
+    for axis in range(3):
+        for side in (0.0, 1.0):
+            u = rng.uniform(0, 1, (per, 3)) * ext
+            u[:, axis] = side * ext[axis]
+            pts.append(u)
+    P = np.concatenate(pts)
+    if jitter:
+        P += rng.normal(0, jitter, P.shape)
+    return P.astype(np.float32)
+
+
+def plane_and_sphere(n, seed=1):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = n // 2
+    floor = np.column_stack([rng.uniform(-1, 1, m), rng.uniform(-1, 1, m), np.zeros(m)])
+    v = rng.normal(size=(n - m, 3))
+    sphere = 0.4 * v / np.linalg.norm(v, axis=1, keepdims=True) + np.array([0, 0, 0.5])
+    return np.concatenate([floor, sphere]).astype(np.float32)
+
+
+def compare_normals(gb, oracle_mod, P, kn, nem, flip, ki=0):
+    o = oracle_mod.OracleSurface(P)
+    on, ok = o.normals(kn, nem=nem, adaptive=True, flip=np.asarray(flip, np.float32), with_k=True)
+    with gb.Surface(P, kn=kn, ki=ki, nem=nem, flip_point=flip) as s:
+        s.calculate_normals()
+        gn, gk = s.raw_normals()
+        final = s.normals()
+        stats = s.normal_stats()
+    assert (gk == ok).all(), "adaptive k differs at %d points" % int((gk != ok).sum())
+    assert stats[:5].sum() == len(P)
+    good = np.isfinite(on).all(1) & np.isfinite(gn).all(1)
+    if nem == 0:
+        good &= np.abs(on[:, 1]) > 0.42  # y = f(x, z) needs a normal away from horizontal
+    ang = angle_deg(gn[good], on[good])
+    assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG, np.percentile(ang, [50, 99, 99.9, 100])
+    if ki:
+        assert np.array_equal(final, o.interpolate(gn, ki), equal_nan=True)
+    return gk
+
+
+@pytest.mark.parametrize("nem", [3, 2, 0])
+def test_room_walls_reach_last_round(gb, oracle_mod, nem):
+    P = room(24_000, seed=3)
+    flip = np.array([1.0, 0.75, 0.5], np.float32)  # inside the room
+    gk = compare_normals(gb, oracle_mod, P, kn=10, nem=nem, flip=flip, ki=10)
+    assert (gk == 320).mean() > 0.5  # points away from the edges need k = 32 kn
+
+
+@pytest.mark.parametrize("kn,ki", [(4, 8), (5, 10), (20, 40), (6, 13)])
+def test_floor_and_sphere(gb, oracle_mod, kn, ki):
+    """k = 128, 160, 640 and 192 in the last round; a sphere fitted earlier."""
+    P = plane_and_sphere(30_000)
+    gk = compare_normals(gb, oracle_mod, P, kn=kn, nem=3, flip=(0.0, 0.0, 0.5), ki=ki)
+    assert (gk == 32 * kn).any() and (gk == 2 * kn).any()
+
+
+def test_noisy_room(gb, oracle_mod):
+    P = room(30_000, seed=5, jitter=3e-4)
+    compare_normals(gb, oracle_mod, P, kn=10, nem=3, flip=(1.0, 0.75, 0.5), ki=20)
+
+
+def test_fewer_points_than_k(gb, oracle_mod):
+    """A flat patch of 150 points: the last round's k = 320 exceeds n."""
+    rng = np.random.Generator(np.random.PCG64(8))
+    P = np.column_stack([rng.uniform(0, 1, 150), rng.uniform(0, 1, 150), np.zeros(150)]).astype(np.float32)
+    gk = compare_normals(gb, oracle_mod, P, kn=10, nem=3, flip=(0.0, 0.0, 1.0), ki=10)
+    assert (gk == 320).all()
+
+
+@pytest.mark.parametrize("bucket", [32, 16])
+def test_room_bucket_sizes(gb, oracle_mod, bucket):
+    P = room(12_000, seed=11)
+    o = oracle_mod.OracleSurface(P)
+    on, ok = o.normals(10, nem=3, adaptive=True, flip=np.array([1.0, 0.75, 0.5], np.float32), with_k=True)
+    with gb.Surface(P, kn=10, ki=0, nem=3, flip_point=(1.0, 0.75, 0.5), bucket=bucket) as s:
+        s.calculate_normals()
+        gn, gk = s.raw_normals()
+    assert (gk == ok).all()
+    ang = angle_deg(gn, on)
+    assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG
