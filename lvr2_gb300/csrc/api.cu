@@ -247,7 +247,7 @@ void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, c
     // Morton frame of the tree (used to seed searches of arbitrary positions)
     const float ext = std::max(std::max(h[3] - h[0], h[4] - h[1]), h[5] - h[2]);
     for (int a = 0; a < 3; a++) s->T.mn[a] = h[a];
-    s->T.scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    s->T.scale = morton_scale(ext);
     check_kernel_error(s, st);
     s->normals = s->ws.get<float4>("api.normals", size_t(n));
     s->raw_normals = s->ws.get<float4>("api.raw_normals", size_t(n));
@@ -1051,14 +1051,14 @@ lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float
         B.pts = C.take<float4>(size_t(np));
         B.inv = C.take<uint32_t>(size_t(np));
         B.nodes = C.take<TreeNode>(size_t(nb > 1 ? nb - 1 : 1));
-        B.bkeys = C.take<uint32_t>(size_t(nb));
+        B.bkeys = C.take<uint64_t>(size_t(nb));
         B.bparent = C.take<int>(size_t(nb));
         B.counters = C.take<int>(size_t(nb > 1 ? nb - 1 : 1));
-        B.codes = C.take<uint32_t>(size_t(np));
-        B.codes2 = C.take<uint32_t>(size_t(np));
+        B.codes = C.take<uint64_t>(size_t(np));
+        B.codes2 = C.take<uint64_t>(size_t(np));
         B.idx = C.take<uint32_t>(size_t(np));
         B.idx2 = C.take<uint32_t>(size_t(np));
-        B.sort_tmp = C.take<unsigned char>(radix_sort_temp_bytes<uint32_t>(size_t(np)));
+        B.sort_tmp = C.take<unsigned char>(radix_sort_temp_bytes<uint64_t>(size_t(np)));
         B.box_tmp = C.take<unsigned char>(bbox_temp_bytes(size_t(np)));
         B.box = C.take<float>(8);
         B.err = C.take<int>(4);
@@ -1073,7 +1073,7 @@ lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float
         LVRGB_CUDA(cudaStreamSynchronize(st));
         const float ext = std::max(std::max(h[3] - h[0], h[4] - h[1]), h[5] - h[2]);
         for (int a = 0; a < 3; a++) T.mn[a] = h[a];
-        T.scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
+        T.scale = morton_scale(ext);
         T.seed_radius = 1;
         if (nq == 0) return;
         pack_queries_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(queries, int(nq), qs);

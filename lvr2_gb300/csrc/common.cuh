@@ -69,16 +69,8 @@ __device__ __forceinline__ float box_dist2(float qx, float qy, float qz, float l
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// 10-bit Morton spread (30-bit codes for the point LBVH).
-__device__ __forceinline__ uint32_t spread10(uint32_t v) {
-    v &= 0x3ffu;
-    v = (v | (v << 16)) & 0x030000ffu;
-    v = (v | (v << 8)) & 0x0300f00fu;
-    v = (v | (v << 4)) & 0x030c30c3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-}
-// 3-D Morton spread/compact of up to 21 bits per axis (lattice keys use 20).
+// 3-D Morton spread/compact of up to 21 bits per axis (lattice keys use 20,
+// the point LBVH 21).
 __host__ __device__ __forceinline__ uint64_t spread20(uint64_t v) {
     v &= 0x1fffffull;
     v = (v | (v << 32)) & 0x1f00000000ffffull;

@@ -1,7 +1,8 @@
-// lbvh.cu -- LBVH construction: bounding box, 30-bit Morton codes, device
+// lbvh.cu -- LBVH construction: bounding box, 63-bit Morton codes, device
 // radix sort, Karras radix tree over point buckets, bottom-up child boxes.
 #include "lbvh_build.h"
 
+#include <algorithm>
 #include <stdexcept>
 #include <vector>
 #include "primitives.cuh"
@@ -11,19 +12,12 @@ namespace lvrgb {
 namespace {
 
 __global__ void morton_kernel(const float* __restrict__ xyz, int n, const float* __restrict__ box,
-                              uint32_t* __restrict__ codes, uint32_t* __restrict__ idx) {
+                              uint64_t* __restrict__ codes, uint32_t* __restrict__ idx) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float mnx = box[0], mny = box[1], mnz = box[2];
-    float ext = fmaxf(fmaxf(box[3] - mnx, box[4] - mny), box[5] - mnz);
-    float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
-    float fx = (xyz[3 * i] - mnx) * scale;
-    float fy = (xyz[3 * i + 1] - mny) * scale;
-    float fz = (xyz[3 * i + 2] - mnz) * scale;
-    uint32_t cx = uint32_t(fminf(fmaxf(fx, 0.0f), 1023.0f));
-    uint32_t cy = uint32_t(fminf(fmaxf(fy, 0.0f), 1023.0f));
-    uint32_t cz = uint32_t(fminf(fmaxf(fz, 0.0f), 1023.0f));
-    codes[i] = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    const float ext = fmaxf(fmaxf(box[3] - box[0], box[4] - box[1]), box[5] - box[2]);
+    codes[i] = morton63(xyz[3 * size_t(i)], xyz[3 * size_t(i) + 1], xyz[3 * size_t(i) + 2], box[0], box[1], box[2],
+                        morton_scale(ext));
     idx[i] = uint32_t(i);
 }
 
@@ -36,33 +30,42 @@ __global__ void gather_sorted_kernel(const float* __restrict__ xyz, const uint32
     inv[o] = uint32_t(j);
 }
 
-// Longest common prefix of bucket keys i and j, with the bucket index as
-// tie-break for equal keys (Karras 2012).
-__device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, int bucket, int nb, int i, int j) {
+// Common-prefix length of buckets i and j in the key [scan id: sbits bits]
+// [first point's 63-bit Morton code] [bucket index: 32 bits] -- the bucket
+// index breaks ties between equal codes (Karras 2012).  Without per-bucket
+// scan ids (bscan == nullptr) sbits is 0.
+__device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, const uint16_t* __restrict__ bscan, int sbits,
+                                     int nb, int i, int j) {
     if (j < 0 || j >= nb) return -1;
-    uint32_t ki = codes[size_t(i) * bucket], kj = codes[size_t(j) * bucket];
-    if (ki != kj) return __clz(ki ^ kj);
-    return 32 + __clz(uint32_t(i) ^ uint32_t(j));
+    if (bscan) {
+        const unsigned si = bscan[i], sj = bscan[j];
+        if (si != sj) return __clz(int(si ^ sj)) - (32 - sbits);
+    }
+    const uint64_t ki = keys[i], kj = keys[j];
+    if (ki != kj) return sbits + __clzll((long long)(ki ^ kj)) - 1;
+    return sbits + 63 + __clz(int(uint32_t(i) ^ uint32_t(j)));
 }
 
-__global__ void karras_kernel(const uint32_t* __restrict__ codes, int bucket, int nb, TreeNode* __restrict__ nodes,
-                              int* __restrict__ bparent) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Karras radix tree over the nb bucket keys.  With per-bucket scan ids, the
+// node whose range is exactly one scan's buckets becomes that scan's root.
+__global__ void karras_kernel(const uint64_t* __restrict__ keys, const uint16_t* __restrict__ bscan, int sbits, int nb,
+                              TreeNode* __restrict__ nodes, int* __restrict__ bparent, SegInfo* __restrict__ segs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nb - 1) return;
-    const int dir = (delta(codes, bucket, nb, i, i + 1) - delta(codes, bucket, nb, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = delta(codes, bucket, nb, i, i - dir);
+    const int dir = (delta(keys, bscan, sbits, nb, i, i + 1) - delta(keys, bscan, sbits, nb, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, bscan, sbits, nb, i, i - dir);
     int lmax = 2;
-    while (delta(codes, bucket, nb, i, i + lmax * dir) > dmin) lmax <<= 1;
+    while (delta(keys, bscan, sbits, nb, i, i + lmax * dir) > dmin) lmax <<= 1;
     int l = 0;
     for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (delta(codes, bucket, nb, i, i + (l + t) * dir) > dmin) l += t;
+        if (delta(keys, bscan, sbits, nb, i, i + (l + t) * dir) > dmin) l += t;
     const int j = i + l * dir;
-    const int dnode = delta(codes, bucket, nb, i, j);
+    const int dnode = delta(keys, bscan, sbits, nb, i, j);
     int s = 0;
     int div = 2;
     int t = (l + div - 1) / div;
     while (true) {
-        if (delta(codes, bucket, nb, i, i + (s + t) * dir) > dnode) s += t;
+        if (delta(keys, bscan, sbits, nb, i, i + (s + t) * dir) > dnode) s += t;
         if (t == 1) break;
         div <<= 1;
         t = (l + div - 1) / div;
@@ -87,9 +90,13 @@ __global__ void karras_kernel(const uint32_t* __restrict__ codes, int bucket, in
     nodes[i].d.x = left;
     nodes[i].d.y = right;
     if (i == 0) nodes[0].d.z = -1;
+    if (segs) {
+        const int sc = bscan[lo];
+        if (segs[sc].blo == lo && segs[sc].bhi == hi) segs[sc].root = i;
+    }
 }
 
-__global__ void bucket_keys_kernel(const uint32_t* __restrict__ codes, int bucket, int nb, uint32_t* __restrict__ bkeys) {
+__global__ void bucket_keys_kernel(const uint64_t* __restrict__ codes, int bucket, int nb, uint64_t* __restrict__ bkeys) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nb) bkeys[b] = codes[size_t(b) * bucket];
 }
@@ -124,9 +131,9 @@ __global__ void bounds_kernel(const float4* __restrict__ pts, int n, int bucket,
         }
     if (lane != 0 || nb == 1) return;
     int pw = bparent[b];
-    // The path to the root of a radix tree over 30-bit keys with index
-    // tie-breaks has fewer than 64 + 32 links; the bound only guards against a
-    // malformed parent chain.
+    // The path to the root of a radix tree over (16-bit scan id, 63-bit code,
+    // 32-bit index) keys has fewer than 16 + 63 + 32 links; the bound only
+    // guards against a malformed parent chain.
     for (int hops = 0; pw >= 0; hops++) {
         if (hops > 128) {
             atomicOr(err, kErrWalk);
@@ -188,6 +195,8 @@ __global__ void seg_bbox_kernel(const float* __restrict__ xyz, const int* __rest
     }
 }
 
+// Morton code of every point in its own scan's frame (sorted first; the
+// stable sort by scan id that follows groups the scans).
 __global__ void seg_morton_kernel(const float* __restrict__ xyz, int n, const int* __restrict__ off, int S,
                                   const float* __restrict__ box, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -195,28 +204,37 @@ __global__ void seg_morton_kernel(const float* __restrict__ xyz, int n, const in
     const int s = scan_of(off, S, i);
     const float* bx = box + 6 * s;
     const float ext = fmaxf(fmaxf(bx[3] - bx[0], bx[4] - bx[1]), bx[5] - bx[2]);
-    const float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
-    const uint32_t cx = uint32_t(fminf(fmaxf((xyz[3 * size_t(i)] - bx[0]) * scale, 0.0f), 1023.0f));
-    const uint32_t cy = uint32_t(fminf(fmaxf((xyz[3 * size_t(i) + 1] - bx[1]) * scale, 0.0f), 1023.0f));
-    const uint32_t cz = uint32_t(fminf(fmaxf((xyz[3 * size_t(i) + 2] - bx[2]) * scale, 0.0f), 1023.0f));
-    keys[i] = (uint64_t(s) << 30) | (spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2));
+    keys[i] = morton63(xyz[3 * size_t(i)], xyz[3 * size_t(i) + 1], xyz[3 * size_t(i) + 2], bx[0], bx[1], bx[2],
+                       morton_scale(ext));
     idx[i] = uint32_t(i);
 }
 
-// Sorted position j -> padded position pad_off[s] + (j - off[s]).
-__global__ void seg_gather_kernel(const float* __restrict__ xyz, const uint64_t* __restrict__ skeys,
-                                  const uint32_t* __restrict__ sidx, int n, const int* __restrict__ off,
-                                  const int* __restrict__ pad_off, float4* __restrict__ pts, uint32_t* __restrict__ inv,
-                                  uint64_t* __restrict__ pkeys) {
+// Scan id of every Morton-sorted point, and its position as the value.
+__global__ void seg_scan_ids_kernel(const uint32_t* __restrict__ sidx, int n, const int* __restrict__ off, int S,
+                                    uint32_t* __restrict__ sid, uint32_t* __restrict__ pos) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const uint64_t key = skeys[j];
-    const int s = int(key >> 30);
+    sid[j] = uint32_t(scan_of(off, S, int(sidx[j])));
+    pos[j] = uint32_t(j);
+}
+
+// Final position t (scan-grouped, Morton order within a scan) -> padded
+// position pad_off[s] + (t - off[s]).  perm: Morton-sorted position of t
+// (identity when null).
+__global__ void seg_gather_kernel(const float* __restrict__ xyz, const uint64_t* __restrict__ scodes,
+                                  const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sid,
+                                  const uint32_t* __restrict__ perm, int n, const int* __restrict__ off,
+                                  const int* __restrict__ pad_off, float4* __restrict__ pts, uint32_t* __restrict__ inv,
+                                  uint64_t* __restrict__ pkeys) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t j = perm ? perm[t] : uint32_t(t);
+    const int s = int(sid[t]);
     const uint32_t o = sidx[j];
-    const int pp = pad_off[s] + (j - off[s]);
+    const int pp = pad_off[s] + (t - off[s]);
     pts[pp] = make_float4(xyz[3 * size_t(o)], xyz[3 * size_t(o) + 1], xyz[3 * size_t(o) + 2], __uint_as_float(o));
     inv[o] = uint32_t(pp);
-    pkeys[pp] = key;
+    pkeys[pp] = scodes[j];
 }
 
 // Padding after each scan's points: NaN coordinates (never within any bound)
@@ -232,68 +250,13 @@ __global__ void seg_pad_kernel(int np, const int* __restrict__ off, const int* _
     }
 }
 
-__global__ void seg_bucket_keys_kernel(const uint64_t* __restrict__ pkeys, int bucket, int nb, uint64_t* __restrict__ bkeys,
+__global__ void seg_bucket_keys_kernel(const uint64_t* __restrict__ pkeys, int bucket, int nb,
+                                       const int* __restrict__ pad_off, int S, uint64_t* __restrict__ bkeys,
                                        uint16_t* __restrict__ bucket_scan) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
-    const uint64_t k = pkeys[size_t(b) * bucket];
-    bkeys[b] = k;
-    bucket_scan[b] = uint16_t(k >> 30);
-}
-
-__device__ __forceinline__ int delta64(const uint64_t* __restrict__ keys, int nb, int i, int j) {
-    if (j < 0 || j >= nb) return -1;
-    const uint64_t ki = keys[i], kj = keys[j];
-    if (ki != kj) return __clzll(ki ^ kj);
-    return 64 + __clz(uint32_t(i) ^ uint32_t(j));
-}
-
-// Karras radix tree over 64-bit (scan, Morton) bucket keys.  The node whose
-// range is exactly one scan's buckets becomes that scan's root.
-__global__ void seg_karras_kernel(const uint64_t* __restrict__ keys, int nb, const uint16_t* __restrict__ bucket_scan,
-                                  TreeNode* __restrict__ nodes, int* __restrict__ bparent, SegInfo* __restrict__ segs) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb - 1) return;
-    const int dir = (delta64(keys, nb, i, i + 1) - delta64(keys, nb, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = delta64(keys, nb, i, i - dir);
-    int lmax = 2;
-    while (delta64(keys, nb, i, i + lmax * dir) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (delta64(keys, nb, i, i + (l + t) * dir) > dmin) l += t;
-    const int j = i + l * dir;
-    const int dnode = delta64(keys, nb, i, j);
-    int s = 0;
-    int div = 2;
-    int t = (l + div - 1) / div;
-    while (true) {
-        if (delta64(keys, nb, i, i + (s + t) * dir) > dnode) s += t;
-        if (t == 1) break;
-        div <<= 1;
-        t = (l + div - 1) / div;
-    }
-    const int gamma = i + s * dir + (dir < 0 ? -1 : 0);
-    const int lo = min(i, j), hi = max(i, j);
-    int left, right;
-    if (lo == gamma) {
-        left = -1 - gamma;
-        bparent[gamma] = (i << 1) | 0;
-    } else {
-        left = gamma;
-        nodes[gamma].d.z = (i << 1) | 0;
-    }
-    if (hi == gamma + 1) {
-        right = -1 - (gamma + 1);
-        bparent[gamma + 1] = (i << 1) | 1;
-    } else {
-        right = gamma + 1;
-        nodes[gamma + 1].d.z = (i << 1) | 1;
-    }
-    nodes[i].d.x = left;
-    nodes[i].d.y = right;
-    if (i == 0) nodes[0].d.z = -1;
-    const int sc = bucket_scan[lo];
-    if (segs[sc].blo == lo && segs[sc].bhi == hi) segs[sc].root = i;
+    bkeys[b] = pkeys[size_t(b) * bucket];
+    bucket_scan[b] = uint16_t(scan_of(pad_off, S, b * bucket));
 }
 
 }  // namespace
@@ -316,19 +279,19 @@ void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::s
     void* btmp = ws.get<unsigned char>("lbvh.boxtmp", bbox_temp_bytes(size_t(n)));
     bbox_float3(xyz, size_t(n), 3, d_box, btmp, s);
 
-    uint32_t* codes = ws.get<uint32_t>("lbvh.codes", size_t(n));
-    uint32_t* codes2 = ws.get<uint32_t>("lbvh.codes2", size_t(n));
+    uint64_t* codes = ws.get<uint64_t>("lbvh.codes", size_t(n));
+    uint64_t* codes2 = ws.get<uint64_t>("lbvh.codes2", size_t(n));
     uint32_t* idx = ws.get<uint32_t>("lbvh.idx", size_t(n));
     uint32_t* idx2 = ws.get<uint32_t>("lbvh.idx2", size_t(n));
     morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, d_box, codes, idx);
     LVRGB_LAUNCH_CHECK();
-    void* stmp = ws.get<unsigned char>("lbvh.sorttmp", radix_sort_temp_bytes<uint32_t>(size_t(n)));
-    bool alt = radix_sort_pairs<uint32_t>(codes, idx, codes2, idx2, size_t(n), 0, 30, stmp, s);
-    const uint32_t* scodes = alt ? codes2 : codes;
+    void* stmp = ws.get<unsigned char>("lbvh.sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(n)));
+    bool alt = radix_sort_pairs<uint64_t>(codes, idx, codes2, idx2, size_t(n), 0, 63, stmp, s);
+    const uint64_t* scodes = alt ? codes2 : codes;
     const uint32_t* sidx = alt ? idx2 : idx;
     gather_sorted_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, sidx, n, pts, inv);
     LVRGB_LAUNCH_CHECK();
-    uint32_t* bkeys = ws.get<uint32_t>(tag + ".bkeys", size_t(nb));
+    uint64_t* bkeys = ws.get<uint64_t>(tag + ".bkeys", size_t(nb));
     T.bkeys = bkeys;
     bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(scodes, bucket, nb, bkeys);
     LVRGB_LAUNCH_CHECK();
@@ -340,7 +303,7 @@ void lbvh_build(const float* xyz, int n, int bucket, Workspace& ws, const std::s
     }
     int* counters = ws.get<int>("lbvh.counters", size_t(nb - 1));
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, sizeof(int) * size_t(nb - 1), s));
-    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(scodes, bucket, nb, nodes, bparent);
+    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(bkeys, nullptr, 0, nb, nodes, bparent, nullptr);
     LVRGB_LAUNCH_CHECK();
     bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, n, bucket, nb, nodes, bparent, counters,
                                                                  d_err);
@@ -361,8 +324,8 @@ void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, 
     bbox_float3(xyz, size_t(n), 3, B.box, B.box_tmp, s);
     morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, B.box, B.codes, B.idx);
     LVRGB_LAUNCH_CHECK();
-    bool alt = radix_sort_pairs<uint32_t>(B.codes, B.idx, B.codes2, B.idx2, size_t(n), 0, 30, B.sort_tmp, s);
-    const uint32_t* scodes = alt ? B.codes2 : B.codes;
+    bool alt = radix_sort_pairs<uint64_t>(B.codes, B.idx, B.codes2, B.idx2, size_t(n), 0, 63, B.sort_tmp, s);
+    const uint64_t* scodes = alt ? B.codes2 : B.codes;
     const uint32_t* sidx = alt ? B.idx2 : B.idx;
     gather_sorted_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, sidx, n, B.pts, B.inv);
     LVRGB_LAUNCH_CHECK();
@@ -373,7 +336,7 @@ void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, 
         return;
     }
     LVRGB_CUDA(cudaMemsetAsync(B.counters, 0, sizeof(int) * size_t(nb - 1), s));
-    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(scodes, bucket, nb, B.nodes, B.bparent);
+    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(B.bkeys, nullptr, 0, nb, B.nodes, B.bparent, nullptr);
     LVRGB_LAUNCH_CHECK();
     bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(B.pts, n, bucket, nb, B.nodes, B.bparent, B.counters,
                                                                  B.err);
@@ -434,7 +397,12 @@ void lbvh_segmented_prepare(const std::vector<int64_t>& offsets, const std::vect
     out.keys2 = ws.get<uint64_t>(tag + ".keys2", size_t(n));
     out.idx = ws.get<uint32_t>(tag + ".idx", size_t(n));
     out.idx2 = ws.get<uint32_t>(tag + ".idx2", size_t(n));
-    out.sort_tmp = ws.get<unsigned char>(tag + ".sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(n)));
+    out.sort_tmp = ws.get<unsigned char>(tag + ".sorttmp", std::max(radix_sort_temp_bytes<uint64_t>(size_t(n)),
+                                                                     radix_sort_temp_bytes<uint32_t>(size_t(n))));
+    out.sid = ws.get<uint32_t>(tag + ".sid", size_t(n));
+    out.sid2 = ws.get<uint32_t>(tag + ".sid2", size_t(n));
+    out.perm = ws.get<uint32_t>(tag + ".perm", size_t(n));
+    out.perm2 = ws.get<uint32_t>(tag + ".perm2", size_t(n));
     out.pkeys = ws.get<uint64_t>(tag + ".pkeys", size_t(np));
     out.bkeys = ws.get<uint64_t>(tag + ".bkeys", size_t(nb));
     out.bparent = ws.get<int>(tag + ".bparent", size_t(nb));
@@ -454,22 +422,37 @@ void lbvh_segmented_build(const float* xyz, SegTree& out, int* d_err, cudaStream
     LVRGB_LAUNCH_CHECK();
     seg_morton_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, n, out.d_off, S, out.box, out.keys, out.idx);
     LVRGB_LAUNCH_CHECK();
-    const bool alt = radix_sort_pairs<uint64_t>(out.keys, out.idx, out.keys2, out.idx2, size_t(n), 0,
-                                                30 + out.sbits, out.sort_tmp, s);
+    // Morton order over all points, then a stable sort by scan id: each scan
+    // contiguous and Morton-ordered within.
+    const bool alt = radix_sort_pairs<uint64_t>(out.keys, out.idx, out.keys2, out.idx2, size_t(n), 0, 63,
+                                                out.sort_tmp, s);
+    const uint64_t* scodes = alt ? out.keys2 : out.keys;
+    const uint32_t* sidx = alt ? out.idx2 : out.idx;
+    seg_scan_ids_kernel<<<ceil_div(n, 256), 256, 0, s>>>(sidx, n, out.d_off, S, out.sid, out.perm);
+    LVRGB_LAUNCH_CHECK();
+    const uint32_t* sid = out.sid;
+    const uint32_t* perm = nullptr;
+    if (out.sbits > 0) {
+        const bool alt2 = radix_sort_pairs<uint32_t>(out.sid, out.perm, out.sid2, out.perm2, size_t(n), 0, out.sbits,
+                                                     out.sort_tmp, s);
+        sid = alt2 ? out.sid2 : out.sid;
+        perm = alt2 ? out.perm2 : out.perm;
+    }
     seg_pad_kernel<<<ceil_div(np, 256), 256, 0, s>>>(np, out.d_off, out.d_pad, S, pts);
     LVRGB_LAUNCH_CHECK();
-    seg_gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, alt ? out.keys2 : out.keys, alt ? out.idx2 : out.idx, n,
-                                                      out.d_off, out.d_pad, pts, inv, out.pkeys);
+    seg_gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(xyz, scodes, sidx, sid, perm, n, out.d_off, out.d_pad, pts,
+                                                      inv, out.pkeys);
     LVRGB_LAUNCH_CHECK();
-    seg_bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(out.pkeys, bucket, nb, out.bkeys, out.bucket_scan);
+    seg_bucket_keys_kernel<<<ceil_div(nb, 256), 256, 0, s>>>(out.pkeys, bucket, nb, out.d_pad, S, out.bkeys,
+                                                            out.bucket_scan);
     LVRGB_LAUNCH_CHECK();
     if (nb == 1) {
         LVRGB_CUDA(cudaMemsetAsync(out.bparent, 0xff, sizeof(int), s));
         return;
     }
     LVRGB_CUDA(cudaMemsetAsync(out.counters, 0, sizeof(int) * size_t(nb - 1), s));
-    seg_karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(out.bkeys, nb, out.bucket_scan, nodes, out.bparent,
-                                                            out.segs);
+    karras_kernel<<<ceil_div(nb - 1, 256), 256, 0, s>>>(out.bkeys, out.bucket_scan, out.sbits, nb, nodes,
+                                                        out.bparent, out.segs);
     LVRGB_LAUNCH_CHECK();
     bounds_kernel<<<ceil_div(size_t(nb) * 32, 256), 256, 0, s>>>(pts, np, bucket, nb, nodes, out.bparent,
                                                                  out.counters, d_err);

@@ -43,7 +43,7 @@ struct Lbvh {
     const float4* pts = nullptr;
     const uint32_t* inv = nullptr;
     const TreeNode* nodes = nullptr;
-    const uint32_t* bkeys = nullptr;  // Morton code of each bucket's first point
+    const uint64_t* bkeys = nullptr;  // Morton code of each bucket's first point
     int n = 0;
     int nbuckets = 0;
     int bucket = 32;
@@ -52,8 +52,25 @@ struct Lbvh {
     int seed_radius = 1;      // buckets scanned on each side of the seed bucket
 };
 
-constexpr int kStackMax = 64;  // two register entries per lane
-constexpr int kErrStack = 1;   // traversal stack would overflow (never for depth <= 63)
+// Morton codes of the point LBVH: 21 bits per axis (63-bit codes) over the
+// cube of the longest bounding-box side.  Scans are far denser near the
+// scanner than at range; 10 bits per axis would put hundreds of thousands of
+// points of one scan into one code and their buckets would overlap.
+constexpr float kMortonCells = 2097152.0f;  // 2^21
+__host__ __device__ inline float morton_scale(float extent) { return extent > 0.0f ? kMortonCells / extent : 0.0f; }
+__device__ __forceinline__ uint64_t morton63(float x, float y, float z, float mnx, float mny, float mnz, float scale) {
+    const float top = kMortonCells - 1.0f;
+    const uint32_t cx = uint32_t(fminf(fmaxf(__fmul_rn(__fsub_rn(x, mnx), scale), 0.0f), top));
+    const uint32_t cy = uint32_t(fminf(fmaxf(__fmul_rn(__fsub_rn(y, mny), scale), 0.0f), top));
+    const uint32_t cz = uint32_t(fminf(fmaxf(__fmul_rn(__fsub_rn(z, mnz), scale), 0.0f), top));
+    return spread20(cx) | (spread20(cy) << 1) | (spread20(cz) << 2);
+}
+
+// Traversal stack: three register entries per lane.  A root-to-leaf path of a
+// Karras tree over 63-bit codes with 32-bit index tie-breaks has fewer than
+// 63 + 32 = 95 nodes, and the stack never holds more entries than that depth.
+constexpr int kStackMax = 96;
+constexpr int kErrStack = 1;   // traversal stack would overflow (never for depth <= 95)
 constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can have
 
 // Traversal counters of one warp (nodes, buckets) and one lane (heap
@@ -213,10 +230,7 @@ __device__ __forceinline__ void add_bucket(const Lbvh& T, int b, WarpCand& W, fl
 // inputs and result).
 __device__ __forceinline__ int seed_bucket_for(const Lbvh& T, float x, float y, float z) {
     const int lane = threadIdx.x & 31;
-    const uint32_t cx = uint32_t(fminf(fmaxf((x - T.mn[0]) * T.scale, 0.0f), 1023.0f));
-    const uint32_t cy = uint32_t(fminf(fmaxf((y - T.mn[1]) * T.scale, 0.0f), 1023.0f));
-    const uint32_t cz = uint32_t(fminf(fmaxf((z - T.mn[2]) * T.scale, 0.0f), 1023.0f));
-    const uint32_t code = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    const uint64_t code = morton63(x, y, z, T.mn[0], T.mn[1], T.mn[2], T.scale);
     int lo = 0, hi = T.nbuckets;  // answer in [lo, hi)
     while (hi - lo > 1) {
         const int step = (hi - lo + 31) / 32;
@@ -281,7 +295,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         if (active) heap.finish();
         return;
     }
-    int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
+    int stk0 = 0, stk1 = 0, stk2 = 0;  // lane l holds stack entries l, l + 32, l + 64
     int sp = 0;
     int node = root;
     // A tree over nb buckets has nb - 1 internal nodes; each is expanded at
@@ -320,7 +334,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                 break;
             }
             if (lane == (sp & 31)) {
-                if (sp < 32) stk0 = ref; else stk1 = ref;
+                if (sp < 32) stk0 = ref; else if (sp < 64) stk1 = ref; else stk2 = ref;
             }
             sp++;
         } else if (m0) {
@@ -346,7 +360,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
                 break;
             }
             sp--;
-            const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+            const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : (sp < 64 ? stk1 : stk2), sp & 31);
             const TreeNode* pn = T.nodes + (ref >> 1);
             const int side = ref & 1;
             float lx, ly, lz, hx, hy, hz;

@@ -21,14 +21,14 @@ struct LbvhBuffers {
     float4* pts;
     uint32_t* inv;
     TreeNode* nodes;     // max(1, nb - 1)
-    uint32_t* bkeys;     // nb
+    uint64_t* bkeys;     // nb
     int* bparent;        // nb
     int* counters;       // max(1, nb - 1), cleared by lbvh_build_into
-    uint32_t* codes;
-    uint32_t* codes2;
+    uint64_t* codes;
+    uint64_t* codes2;
     uint32_t* idx;
     uint32_t* idx2;
-    void* sort_tmp;      // radix_sort_temp_bytes<uint32_t>(n)
+    void* sort_tmp;      // radix_sort_temp_bytes<uint64_t>(n)
     void* box_tmp;       // bbox_temp_bytes(n)
     float* box;          // 6 floats
     int* err;
@@ -38,8 +38,9 @@ struct LbvhBuffers {
 // allocation).
 void lbvh_build_into(const float* xyz, int n, int bucket, const LbvhBuffers& B, Lbvh& T, cudaStream_t s);
 
-// A segmented LBVH over the scans of a scan project: one radix sort of
-// (scan, Morton) keys, each scan's points padded to whole buckets (padding:
+// A segmented LBVH over the scans of a scan project: a radix sort of the
+// points' Morton codes (each in its scan's frame) and a stable sort by scan
+// id, each scan's points padded to whole buckets (padding:
 // NaN coordinates, index 0xffffffff), one Karras tree whose per-scan subtrees
 // are the scans' search roots.  T.n counts the padded positions.
 struct SegTree {
@@ -52,6 +53,7 @@ struct SegTree {
     float* box = nullptr;
     uint64_t *keys = nullptr, *keys2 = nullptr, *pkeys = nullptr, *bkeys = nullptr;
     uint32_t *idx = nullptr, *idx2 = nullptr;
+    uint32_t *sid = nullptr, *sid2 = nullptr, *perm = nullptr, *perm2 = nullptr;
     void* sort_tmp = nullptr;
     int *bparent = nullptr, *counters = nullptr;
 };

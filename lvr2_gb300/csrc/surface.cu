@@ -771,16 +771,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
 }
 
 __global__ void query_morton_kernel(const float* __restrict__ q, int nq, const float* __restrict__ box,
-                                    uint32_t* __restrict__ codes, uint32_t* __restrict__ idx) {
+                                    uint64_t* __restrict__ codes, uint32_t* __restrict__ idx) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
-    const float mnx = box[0], mny = box[1], mnz = box[2];
-    float ext = fmaxf(fmaxf(box[3] - mnx, box[4] - mny), box[5] - mnz);
-    float scale = ext > 0.0f ? 1024.0f / ext : 0.0f;
-    uint32_t cx = uint32_t(fminf(fmaxf((q[3 * i] - mnx) * scale, 0.0f), 1023.0f));
-    uint32_t cy = uint32_t(fminf(fmaxf((q[3 * i + 1] - mny) * scale, 0.0f), 1023.0f));
-    uint32_t cz = uint32_t(fminf(fmaxf((q[3 * i + 2] - mnz) * scale, 0.0f), 1023.0f));
-    codes[i] = spread10(cx) | (spread10(cy) << 1) | (spread10(cz) << 2);
+    const float ext = fmaxf(fmaxf(box[3] - box[0], box[4] - box[1]), box[5] - box[2]);
+    codes[i] = morton63(q[3 * size_t(i)], q[3 * size_t(i) + 1], q[3 * size_t(i) + 2], box[0], box[1], box[2],
+                        morton_scale(ext));
     idx[i] = uint32_t(i);
 }
 
@@ -998,14 +994,14 @@ void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in
 
 void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Workspace& ws, cudaStream_t s) {
     if (nq == 0) return;
-    uint32_t* codes = ws.get<uint32_t>("q.codes", size_t(nq));
-    uint32_t* codes2 = ws.get<uint32_t>("q.codes2", size_t(nq));
+    uint64_t* codes = ws.get<uint64_t>("q.codes", size_t(nq));
+    uint64_t* codes2 = ws.get<uint64_t>("q.codes2", size_t(nq));
     uint32_t* idx = ws.get<uint32_t>("q.idx", size_t(nq));
     uint32_t* idx2 = ws.get<uint32_t>("q.idx2", size_t(nq));
     query_morton_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(q, nq, d_box, codes, idx);
     LVRGB_LAUNCH_CHECK();
-    void* tmp = ws.get<unsigned char>("q.sorttmp", radix_sort_temp_bytes<uint32_t>(size_t(nq)));
-    bool alt = radix_sort_pairs<uint32_t>(codes, idx, codes2, idx2, size_t(nq), 0, 30, tmp, s);
+    void* tmp = ws.get<unsigned char>("q.sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(nq)));
+    bool alt = radix_sort_pairs<uint64_t>(codes, idx, codes2, idx2, size_t(nq), 0, 63, tmp, s);
     query_gather_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(q, alt ? idx2 : idx, nq, qs);
     LVRGB_LAUNCH_CHECK();
 }

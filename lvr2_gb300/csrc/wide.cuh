@@ -210,7 +210,7 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
         wide_shrink(W);
         return;
     }
-    int stk0 = 0, stk1 = 0;  // lane l holds stack entries l and l + 32
+    int stk0 = 0, stk1 = 0, stk2 = 0;  // lane l holds stack entries l, l + 32, l + 64
     int sp = 0;
     int node = root;
     int budget = T.nbuckets + 1;
@@ -241,7 +241,7 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
             }
             const int ref = (node << 1) | (first1 ? 0 : 1);
             if (lane == (sp & 31)) {
-                if (sp < 32) stk0 = ref; else stk1 = ref;
+                if (sp < 32) stk0 = ref; else if (sp < 64) stk1 = ref; else stk2 = ref;
             }
             sp++;
         } else if (n0) {
@@ -266,7 +266,7 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
                 break;
             }
             sp--;
-            const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+            const int ref = __shfl_sync(kFull, sp < 32 ? stk0 : (sp < 64 ? stk1 : stk2), sp & 31);
             const TreeNode* pn = T.nodes + (ref >> 1);
             float lx, ly, lz, hx, hy, hz;
             int child;
