@@ -27,8 +27,9 @@ __device__ __forceinline__ int pick_smallest(double e0, double e1, double e2) {
     return 2;
 }
 
-// Cyclic Jacobi eigen-decomposition in double; smallest eigenvector.
-__device__ void jacobi3_smallest(const double Ain[6], double v_out[3]) {
+// Cyclic Jacobi eigen-decomposition in double; smallest eigenvector.  The
+// rare fallback of the FP32 solve: kept out of line.
+__device__ __noinline__ void jacobi3_smallest(const double Ain[6], double v_out[3]) {
     double A[3][3] = {{Ain[0], Ain[1], Ain[2]}, {Ain[1], Ain[3], Ain[4]}, {Ain[2], Ain[4], Ain[5]}};
     double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     for (int sweep = 0; sweep < 50; sweep++) {

@@ -60,8 +60,9 @@ __device__ __forceinline__ float warp_max_f(float v) {
 
 // The r-th smallest (1-based, 1 <= r <= cnt) of cnt distinct keys, by a warp
 // most-significant-digit radix select with 8-bit digits.  Stops as soon as the
-// digit prefix identifies a single key.
-__device__ __forceinline__ unsigned long long warp_select(const unsigned long long* keys, int cnt, int r,
+// digit prefix identifies a single key.  Not inlined: the search calls it from
+// several places, and one copy keeps the kernel within the instruction cache.
+__device__ __noinline__ unsigned long long warp_select(const unsigned long long* keys, int cnt, int r,
                                                           uint32_t* hist) {
     const int lane = threadIdx.x & 31;
     unsigned long long prefix = 0, mask = 0;
@@ -139,7 +140,7 @@ __device__ __forceinline__ unsigned long long warp_select(const unsigned long lo
 }
 
 // Keeps the keys <= kth (order preserved), in place; returns their number.
-__device__ __forceinline__ int warp_compact_le(unsigned long long* keys, int cnt, unsigned long long kth) {
+__device__ __noinline__ int warp_compact_le(unsigned long long* keys, int cnt, unsigned long long kth) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     int out = 0;
