@@ -63,24 +63,25 @@ __device__ __noinline__ void jacobi3_smallest(const double Ain[6], double v_out[
     for (int k = 0; k < 3; k++) v_out[k] = V[k][m] / n;
 }
 
-// Smallest eigenvector of a symmetric 3x3 matrix in FP32 by the closed-form
-// trigonometric eigenvalues (Smith 1961) and a cross product of two rows of
-// (A - lambda I).  Returns false when the result is not trustworthy in FP32
-// (relative eigengap below gap_thr or nearly parallel rows); the caller then
-// solves in FP64.
-__device__ bool eig_smallest_f32(const float A[6], float gap_thr, float v[3]) {
-    const float a00 = A[0], a01 = A[1], a02 = A[2], a11 = A[3], a12 = A[4], a22 = A[5];
+// Smallest eigenvector of a symmetric 3x3 matrix (a00 a01 a02 a11 a12 a22)
+// in FP32 by the closed-form trigonometric eigenvalues (Smith 1961) and a
+// cross product of two rows of (A - lambda I).  w = 0 when the result is not
+// trustworthy in FP32 (relative eigengap below gap_thr or nearly parallel
+// rows); the caller then solves in FP64.  Out of line: with its trigonometric
+// functions it would otherwise dominate the code size of the kernels that
+// inline it.
+__device__ __noinline__ float4 eig_smallest_f32(float a00, float a01, float a02, float a11, float a12, float a22,
+                                                float gap_thr) {
     const float p1 = a01 * a01 + a02 * a02 + a12 * a12;
     if (p1 == 0.0f) {
         int m = pick_smallest(a00, a11, a22);
-        v[0] = m == 0; v[1] = m == 1; v[2] = m == 2;
-        return true;
+        return make_float4(m == 0, m == 1, m == 2, 1.0f);
     }
     const float q = (a00 + a11 + a22) * (1.0f / 3.0f);
     const float b00 = a00 - q, b11 = a11 - q, b22 = a22 - q;
     const float p2 = b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * p1;
     const float p = sqrtf(p2 * (1.0f / 6.0f));
-    if (!(p > 0.0f)) return false;
+    if (!(p > 0.0f)) return make_float4(0, 0, 0, 0);
     const float ip = 1.0f / p;
     const float c00 = b00 * ip, c11 = b11 * ip, c22 = b22 * ip;
     const float c01 = a01 * ip, c02 = a02 * ip, c12 = a12 * ip;
@@ -91,7 +92,7 @@ __device__ bool eig_smallest_f32(const float A[6], float gap_thr, float v[3]) {
     const float l3 = q + 2.0f * p * cosf(phi + 2.0943951023931953f);
     const float l2 = 3.0f * q - l1 - l3;
     const float scale = fmaxf(fabsf(l1), 1e-30f);
-    if ((l2 - l3) < gap_thr * scale) return false;
+    if ((l2 - l3) < gap_thr * scale) return make_float4(0, 0, 0, 0);
     const float r0[3] = {a00 - l3, a01, a02};
     const float r1[3] = {a01, a11 - l3, a12};
     const float r2[3] = {a02, a12, a22 - l3};
@@ -115,12 +116,9 @@ __device__ bool eig_smallest_f32(const float A[6], float gap_thr, float v[3]) {
     const float rn = fmaxf(fmaxf(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2],
                                  r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]),
                            r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
-    if (!(best > 1e-10f * rn * rn)) return false;
+    if (!(best > 1e-10f * rn * rn)) return make_float4(0, 0, 0, 0);
     const float inv = rsqrtf(best);
-    v[0] = x[bi][0] * inv;
-    v[1] = x[bi][1] * inv;
-    v[2] = x[bi][2] * inv;
-    return true;
+    return make_float4(x[bi][0] * inv, x[bi][1] * inv, x[bi][2] * inv, 1.0f);
 }
 
 struct NormalsArgs {
@@ -136,8 +134,7 @@ struct NormalsArgs {
     float gap_thr;
     float4* normals;
     int32_t* kused;
-    uint32_t* retry;
-    uint32_t* retry_count;
+    uint8_t* flags;  // per query of the round: 1 = search again with a larger k
     unsigned long long* gheap;
     int* err;
     uint32_t* stats;
@@ -216,9 +213,9 @@ __device__ __forceinline__ void solve_plane(float gap_thr, float4 q, const float
                                             const float r[6], float n[3], bool& fp64) {
     fp64 = false;
     if (kNem == 3) {
-        float v[3];
-        if (eig_smallest_f32(S, gap_thr, v)) {
-            n[0] = v[0]; n[1] = v[1]; n[2] = v[2];
+        const float4 v = eig_smallest_f32(S[0], S[1], S[2], S[3], S[4], S[5], gap_thr);
+        if (v.w != 0.0f) {
+            n[0] = v.x; n[1] = v.y; n[2] = v.z;
         } else {
             double D[6], w[3];
             for (int i = 0; i < 6; i++) D[i] = double(S[i]);
@@ -404,14 +401,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
             }
         }
         const unsigned fitted = __ballot_sync(kFull, active && !retry);
-        const unsigned rm = __ballot_sync(kFull, retry);
         if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
-        if (rm) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(A.retry_count, uint32_t(__popc(rm)));
-            base = __shfl_sync(kFull, base, 0);
-            if (retry) A.retry[base + __popc(rm & lt)] = uint32_t(pos);
-        }
+        if (qi < nq) A.flags[qi] = retry ? 1 : 0;
     }
     unsigned pushes = st.pushes;
     for (int o = 16; o > 0; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
@@ -470,10 +461,9 @@ constexpr int kWideWarps = 8;  // warps per block
 constexpr int kWideTile = 8;   // queries per warp tile
 
 template <int kNem>
-__global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsArgs A) {
+__global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(NormalsArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
     WideState W;
     W.K = A.K;
     W.cap = wide_capacity(A.K);
@@ -485,7 +475,6 @@ __global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsAr
     TravStats st;
     for (int tile = blockIdx.x * kWideWarps + wib; tile * kWideTile < nq; tile += gridDim.x * kWideWarps) {
         unsigned fitted = 0, retry = 0;
-        int my_pos = 0;
         const int nt = min(kWideTile, nq - tile * kWideTile);
         for (int j = 0; j < nt; j++) {
             const int qi = tile * kWideTile + j;
@@ -500,6 +489,7 @@ __global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsAr
                 fx = g.fx; fy = g.fy; fz = g.fz;
             }
             wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, pos / B, root, blo, bhi);
+            st.rounds++;
             const int cnt = W.cnt;
             // pass 1: neighbourhood box (min / max: exact in any order)
             float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
@@ -523,7 +513,6 @@ __global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsAr
             }
             if (!fit) {
                 retry |= 1u << j;
-                if (lane == j) my_pos = pos;
                 continue;
             }
             // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
@@ -621,16 +610,14 @@ __global__ void __launch_bounds__(kWideWarps * 32) normals_wide_kernel(NormalsAr
             fitted |= 1u << j;
         }
         if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
-        if (retry) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(A.retry_count, uint32_t(__popc(retry)));
-            base = __shfl_sync(kFull, base, 0);
-            if ((retry >> lane) & 1u) A.retry[base + __popc(retry & lt)] = uint32_t(my_pos);
-        }
+        if (lane < nt) A.flags[tile * kWideTile + lane] = uint8_t((retry >> lane) & 1u);
     }
     if (lane == 0 && st.nodes) {
         atomicAdd(A.stats + 8, st.buckets);
         atomicAdd(A.stats + 9, st.nodes);
+        atomicAdd(A.stats + 13, st.pushes);
+        atomicAdd(A.stats + 14, st.chunks);
+        atomicAdd(A.stats + 15, st.rounds);
     }
 }
 
@@ -789,6 +776,56 @@ __global__ void query_gather_kernel(const float* __restrict__ q, const uint32_t*
     qs[j] = make_float4(q[3 * size_t(o)], q[3 * size_t(o) + 1], q[3 * size_t(o) + 2], __uint_as_float(o));
 }
 
+// Ordered compaction of a round's retry flags into the next round's query
+// list: the list stays in Morton order (consecutive queries of a warp stay
+// close in space) and does not depend on the order in which warps finished.
+// The query count may live on the device (nq_dev); nq bounds it.
+constexpr int kCompactBlock = 1024;
+
+__device__ __forceinline__ int round_count(int nq, const uint32_t* nq_dev) { return nq_dev ? int(*nq_dev) : nq; }
+
+__global__ void __launch_bounds__(kCompactBlock) flag_count_kernel(const uint8_t* __restrict__ flags, int nq,
+                                                                   const uint32_t* __restrict__ nq_dev,
+                                                                   uint32_t* __restrict__ counts) {
+    __shared__ uint32_t part[kCompactBlock / 32];
+    const int m = round_count(nq, nq_dev);
+    const int i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const unsigned b = __ballot_sync(kFull, i < m && flags[i] != 0);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = part[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+        if (threadIdx.x == 0) counts[blockIdx.x] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kCompactBlock) flag_scatter_kernel(const uint8_t* __restrict__ flags,
+                                                                     const uint32_t* __restrict__ list, int nq,
+                                                                     const uint32_t* __restrict__ nq_dev,
+                                                                     const uint32_t* __restrict__ offsets,
+                                                                     uint32_t* __restrict__ out) {
+    __shared__ uint32_t part[kCompactBlock / 32];
+    const int m = round_count(nq, nq_dev);
+    const int i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool f = i < m && flags[i] != 0;
+    const unsigned b = __ballot_sync(kFull, f);
+    if (lane == 0) part[w] = __popc(b);
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t v = part[lane];
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        part[lane] = incl - v;
+    }
+    __syncthreads();
+    if (f) out[offsets[blockIdx.x] + part[w] + __popc(b & ((1u << lane) - 1u))] = list ? list[i] : uint32_t(i);
+}
+
 int g_num_sms = 0;
 
 template <typename Kernel>
@@ -857,6 +894,21 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
     LVRGB_LAUNCH_CHECK();
 }
 
+// next[0, *d_count) = the list entries (or, without a list, the indices) of
+// [0, count) whose flag is set, in order.  count = *nq_dev when given (then
+// nq bounds it), else nq.
+void compact_retry(const uint8_t* flags, const uint32_t* list, int nq, const uint32_t* nq_dev, uint32_t* next,
+                   uint32_t* d_count, Workspace& ws, cudaStream_t s) {
+    const int blocks = std::max(1, ceil_div(nq, kCompactBlock));
+    uint32_t* counts = ws.get<uint32_t>("normals.flagcounts", size_t(blocks));
+    void* tmp = ws.get<unsigned char>("normals.flagscan", scan_temp_bytes(size_t(blocks)));
+    flag_count_kernel<<<blocks, kCompactBlock, 0, s>>>(flags, nq, nq_dev, counts);
+    LVRGB_LAUNCH_CHECK();
+    exclusive_scan_u32(counts, counts, size_t(blocks), tmp, d_count, s);
+    flag_scatter_kernel<<<blocks, kCompactBlock, 0, s>>>(flags, list, nq, nq_dev, counts, next);
+    LVRGB_LAUNCH_CHECK();
+}
+
 void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
     if (g_num_sms == 0) {
         int dev = 0;
@@ -878,6 +930,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
     if (n == 0) return;
     uint32_t* lists[2] = {ws.get<uint32_t>("normals.listA", size_t(n)), ws.get<uint32_t>("normals.listB", size_t(n))};
     uint32_t* counter = ws.get<uint32_t>("normals.counter", 2);
+    uint8_t* flags = ws.get<uint8_t>("normals.flags", size_t(n));
     uint64_t* h_count = ws.pinned();
     int nq = n;
     const uint32_t* list = nullptr;
@@ -887,7 +940,6 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
         const int last = (!cfg.adaptive || round == 5) ? 1 : 0;
         uint32_t* retry = lists[round & 1];
-        LVRGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), s));
         NormalsArgs A;
         A.T = T;
         A.K = K;
@@ -901,8 +953,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.gap_thr = cfg.gap_threshold;
         A.normals = normals;
         A.kused = kused;
-        A.retry = retry;
-        A.retry_count = counter;
+        A.flags = flags;
         A.err = d_err;
         A.stats = d_stats;
         A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
@@ -912,6 +963,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.nq_dev = nullptr;
         launch_normals(A, nq, ws, s);
         if (last) break;
+        compact_retry(flags, list, nq, nullptr, retry, counter, ws, s);
         h_count[0] = 0;
         LVRGB_CUDA(cudaMemcpyAsync(h_count, counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         LVRGB_CUDA(cudaStreamSynchronize(s));
@@ -932,6 +984,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
     }
     uint32_t* lists[2] = {ws.get<uint32_t>("segn.listA", size_t(n)), ws.get<uint32_t>("segn.listB", size_t(n))};
     uint32_t* counters = ws.get<uint32_t>("segn.counters", 8);
+    uint8_t* flags = ws.get<uint8_t>("segn.flags", size_t(n));
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s));
     const int rounds = cfg.adaptive ? 5 : 1;
     size_t k = size_t(cfg.kn);
@@ -952,8 +1005,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.gap_thr = cfg.gap_threshold;
         A.normals = normals;
         A.kused = kused;
-        A.retry = lists[(round + 1) & 1];
-        A.retry_count = counters + (round - 1);
+        A.flags = flags;
         A.err = d_err;
         A.stats = d_stats;
         A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
@@ -963,6 +1015,8 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         // Later rounds read their query count on the device: launch a fixed
         // grid that strides over however many queries the previous round left.
         launch_normals(A, round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), ws, s);
+        if (round < rounds)
+            compact_retry(flags, A.list, n, A.nq_dev, lists[(round + 1) & 1], counters + (round - 1), ws, s);
     }
 }
 

@@ -17,7 +17,10 @@ struct NormalsConfig {
 //   [0..4] number of points whose plane was fitted in search round 1..5,
 //   [5]    number of PCA eigensolves that fell back to FP64,
 //   [8]    buckets scanned (per warp), [9] tree nodes expanded (per warp),
-//   [10]   heap insertions (per query), [11] 32-candidate chunks scanned (per warp).
+//   [10]   heap insertions (per query), [11] 32-candidate chunks scanned (per warp),
+//   [12]   warp insertion rounds,
+//   [13..15] searches with k > kSmemHeapMax (one warp per query): candidates
+//          buffered, buffer compactions, queries.
 constexpr int kNormalStats = 16;
 
 // Normals in Morton order (float4, w = 0).  kused (optional, Morton order)

@@ -159,8 +159,9 @@ __device__ __noinline__ int warp_compact_le(unsigned long long* keys, int cnt, u
 }
 
 // Cuts the buffer to its K smallest keys and tightens the bound.
-__device__ __forceinline__ void wide_shrink(WideState& W) {
+__device__ __forceinline__ void wide_shrink(WideState& W, TravStats& st) {
     if (W.cnt <= W.K) return;
+    st.chunks++;
     const unsigned long long kth = warp_select(W.keys, W.cnt, W.K, W.hist);
     W.cnt = warp_compact_le(W.keys, W.cnt, kth);
     W.thr = kth;
@@ -184,7 +185,8 @@ __device__ __forceinline__ void wide_add_bucket(const Lbvh& T, int b, WideState&
     const unsigned m = __ballot_sync(kFull, acc);
     if (acc) W.keys[W.cnt + __popc(m & ((1u << lane) - 1u))] = key;
     W.cnt += __popc(m);
-    if (W.cnt > W.cap - 32) wide_shrink(W);
+    st.pushes += __popc(m);
+    if (W.cnt > W.cap - 32) wide_shrink(W, st);
 }
 
 // The K nearest keys of one query (warp-uniform arguments).  On return
@@ -204,11 +206,11 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
     const int half = ((W.K + T.bucket - 1) / T.bucket + 1) / 2;
     const int skip_lo = max(blo, seed - half), skip_hi = min(bhi, seed + half);
     for (int b = skip_lo; b <= skip_hi; b++) wide_add_bucket(T, b, W, qx, qy, qz, st);
-    wide_shrink(W);
+    wide_shrink(W, st);
     if (root < 0) {
         const int b = -1 - root;
         if (b < skip_lo || b > skip_hi) wide_add_bucket(T, b, W, qx, qy, qz, st);
-        wide_shrink(W);
+        wide_shrink(W, st);
         return;
     }
     int stk0 = 0, stk1 = 0, stk2 = 0;  // lane l holds stack entries l, l + 32, l + 64
@@ -286,7 +288,7 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
             next = child;
         }
     }
-    wide_shrink(W);
+    wide_shrink(W, st);
 }
 
 // Hands the m smallest of the W.cnt buffered keys to emit(rank, key), rank
