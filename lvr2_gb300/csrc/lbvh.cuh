@@ -76,7 +76,7 @@ constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can
 // Traversal counters of one warp (nodes, buckets) and one lane (heap
 // insertions); kernels that do not report them let the compiler drop them.
 struct TravStats {
-    unsigned nodes = 0, buckets = 0, chunks = 0, pushes = 0, rounds = 0;
+    unsigned nodes = 0, buckets = 0, chunks = 0, pushes = 0, rounds = 0, retries = 0;
 };
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at

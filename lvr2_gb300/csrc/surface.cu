@@ -135,6 +135,9 @@ struct NormalsArgs {
     float4* normals;
     int32_t* kused;
     uint8_t* flags;  // per query of the round: 1 = search again with a larger k
+    // Squared distance of the k-th neighbour of every point that searches
+    // again (by Morton position): written by a round, read by the next one.
+    float* kth_d2;
     unsigned long long* gheap;
     int* err;
     uint32_t* stats;
@@ -398,6 +401,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
                 if (fp64) atomicAdd(A.stats + 5, 1u);
             } else {
                 retry = true;
+                if (A.kth_d2) A.kth_d2[pos] = cnt == A.K ? heap.tau() : __int_as_float(0x7f800000);
             }
         }
         const unsigned fitted = __ballot_sync(kFull, active && !retry);
@@ -458,6 +462,9 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 }
 
 constexpr int kWideWarps = 8;  // warps per block
+// Growth of the squared k-th neighbour distance when k doubles: 2 on a
+// surface, 4 along a line; above 2 most searches need no second pass.
+constexpr float kBoundGrowth = 2.5f;
 constexpr int kWideTile = 8;   // queries per warp tile
 
 template <int kNem>
@@ -488,7 +495,20 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
                 root = g.root; blo = g.blo; bhi = g.bhi;
                 fx = g.fx; fy = g.fy; fz = g.fz;
             }
-            wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, pos / B, root, blo, bhi);
+            // The previous round's k-th distance, scaled for twice the k, bounds
+            // the search; when fewer than K points lie within the bound the
+            // search runs again without one.  Either way the result is exact.
+            float bound = __int_as_float(0x7f800000);
+            if (A.round > 1 && A.kth_d2) {
+                const float prev = A.kth_d2[pos];
+                if (prev < FLT_MAX) bound = __fmul_rn(prev, kBoundGrowth);
+            }
+            for (int attempt = 0; attempt < 2; attempt++) {
+                wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, pos / B, root, blo, bhi, bound);
+                if (W.cnt >= W.K || !(bound < FLT_MAX)) break;
+                bound = __int_as_float(0x7f800000);
+                st.retries++;
+            }
             st.rounds++;
             const int cnt = W.cnt;
             // pass 1: neighbourhood box (min / max: exact in any order)
@@ -513,6 +533,14 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
             }
             if (!fit) {
                 retry |= 1u << j;
+                if (A.kth_d2) {
+                    // the K-th key is the largest one kept
+                    unsigned long long mx = 0;
+                    for (int i = lane; i < cnt; i += 32) mx = max(mx, W.keys[i]);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+                    if (lane == 0) A.kth_d2[pos] = cnt == A.K ? key_d2(mx) : __int_as_float(0x7f800000);
+                }
                 continue;
             }
             // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
@@ -613,6 +641,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
         if (lane < nt) A.flags[tile * kWideTile + lane] = uint8_t((retry >> lane) & 1u);
     }
     if (lane == 0 && st.nodes) {
+        atomicAdd(A.stats + 6, st.retries);
         atomicAdd(A.stats + 8, st.buckets);
         atomicAdd(A.stats + 9, st.nodes);
         atomicAdd(A.stats + 13, st.pushes);
@@ -931,6 +960,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
     uint32_t* lists[2] = {ws.get<uint32_t>("normals.listA", size_t(n)), ws.get<uint32_t>("normals.listB", size_t(n))};
     uint32_t* counter = ws.get<uint32_t>("normals.counter", 2);
     uint8_t* flags = ws.get<uint8_t>("normals.flags", size_t(n));
+    float* kth_d2 = cfg.adaptive ? ws.get<float>("normals.kth", size_t(n)) : nullptr;
     uint64_t* h_count = ws.pinned();
     int nq = n;
     const uint32_t* list = nullptr;
@@ -954,6 +984,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.normals = normals;
         A.kused = kused;
         A.flags = flags;
+        A.kth_d2 = kth_d2;
         A.err = d_err;
         A.stats = d_stats;
         A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;
@@ -985,6 +1016,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
     uint32_t* lists[2] = {ws.get<uint32_t>("segn.listA", size_t(n)), ws.get<uint32_t>("segn.listB", size_t(n))};
     uint32_t* counters = ws.get<uint32_t>("segn.counters", 8);
     uint8_t* flags = ws.get<uint8_t>("segn.flags", size_t(n));
+    float* kth_d2 = cfg.adaptive ? ws.get<float>("segn.kth", size_t(n)) : nullptr;
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s));
     const int rounds = cfg.adaptive ? 5 : 1;
     size_t k = size_t(cfg.kn);
@@ -1006,6 +1038,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.normals = normals;
         A.kused = kused;
         A.flags = flags;
+        A.kth_d2 = kth_d2;
         A.err = d_err;
         A.stats = d_stats;
         A.nbr = (nbr && ki > 0 && ki <= K) ? nbr : nullptr;

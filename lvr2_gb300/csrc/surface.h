@@ -16,6 +16,7 @@ struct NormalsConfig {
 // Device counters written by compute_normals (uint32[16]):
 //   [0..4] number of points whose plane was fitted in search round 1..5,
 //   [5]    number of PCA eigensolves that fell back to FP64,
+//   [6]    bounded large-k searches that found fewer than k points and ran again,
 //   [8]    buckets scanned (per warp), [9] tree nodes expanded (per warp),
 //   [10]   heap insertions (per query), [11] 32-candidate chunks scanned (per warp),
 //   [12]   warp insertion rounds,

@@ -190,15 +190,16 @@ __device__ __forceinline__ void wide_add_bucket(const Lbvh& T, int b, WideState&
 }
 
 // The K nearest keys of one query (warp-uniform arguments).  On return
-// W.keys[0, W.cnt) holds them (unordered); W.cnt < K only when the tree (or
-// the segment [blo, bhi]) has fewer points.  seed: the query's bucket.
+// W.keys[0, W.cnt) holds them (unordered).  seed: the query's bucket.
+// bound: squared radius that limits the search (+inf: none); W.cnt < K when
+// fewer than K points lie within it, or when the tree (or the segment
+// [blo, bhi]) has fewer points.
 __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, float qz, WideState& W, int* err,
-                                         TravStats& st, int seed, int root = 0, int blo = 0,
-                                         int bhi = 0x7fffffff) {
+                                         TravStats& st, int seed, int root, int blo, int bhi, float bound) {
     const int lane = threadIdx.x & 31;
     W.cnt = 0;
-    W.thr = kKeyEmpty;
-    W.tau = __int_as_float(0x7f800000);
+    W.tau = bound;
+    W.thr = bound < __int_as_float(0x7f800000) ? make_key(bound, 0xffffffffu) : kKeyEmpty;
     if (T.nbuckets <= 0) return;
     if (T.nbuckets == 1) root = -1;
     bhi = min(bhi, T.nbuckets - 1);
