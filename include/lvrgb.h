@@ -165,6 +165,35 @@ lvrgb_status lvrgb_grid_distances(lvrgb_surface s, const float* q, int64_t nq, f
 lvrgb_status lvrgb_interpolated_normal(lvrgb_surface s, const float* q, int64_t nq, float* out,
                                        int32_t on_device, void* stream);
 
+/* Reverse mode of lvrgb_distance (AdaptiveKSearchSurface::distance,
+ * AdaptiveKSearchSurface.tcc:414-457).  No lvr2 counterpart: lvr2 has no
+ * gradients; this is the adjoint form of its signed distance for
+ * optimisation and learning pipelines.  Each position's kd nearest points are
+ * held fixed (the distance is piecewise smooth in q).  With c = mean point,
+ * m = mean normal, nh = m/|m|, r = q - c, d = r.nh, e = |r| and upstream
+ * gradients gd = grad_projected[i], ge = grad_euclidean[i] (either array may
+ * be NULL = 0):
+ *   grad_q[i]          = gd nh + ge r/e
+ *   grad_points[j]    += -grad_q[i] / kd       for each neighbour j of q_i
+ *   grad_normals[j]   += gd (r - d nh) / (kd |m|)
+ * grad_points / grad_normals (n x 3, input point order) are written (sums
+ * over all queries; float atomics, so their last bits depend on summation
+ * order).  projected / euclidean (may be NULL) equal lvrgb_distance's bit for
+ * bit.  Any output may be NULL. */
+lvrgb_status lvrgb_distance_adjoint(lvrgb_surface s, const float* q, int64_t nq, const float* grad_projected,
+                                    const float* grad_euclidean, float* projected, float* euclidean, float* grad_q,
+                                    float* grad_points, float* grad_normals, int32_t on_device, void* stream);
+
+/* Newton projection of nv positions onto the zero level of the signed
+ * distance: `steps` (1..64) updates x <- x - d(x) nh(x), each with the kd
+ * nearest points of the current x; out_normals = nh of the last step (the
+ * analytic gradient of d, a vertex normal for mesh vertices).  No lvr2
+ * counterpart (lvr2 places marching-cubes vertices by linear interpolation
+ * only); used to refine lvrgb_get_mesh vertices.  out_positions or
+ * out_normals may be NULL. */
+lvrgb_status lvrgb_project_to_surface(lvrgb_surface s, const float* v, int64_t nv, int32_t steps,
+                                      float* out_positions, float* out_normals, int32_t on_device, void* stream);
+
 /* Grid and marching-cubes parameters: the lvr2_reconstruct flags --voxelsize,
  * --intersections, --noExtrusion, --decomposition (Options.cpp:69-74). */
 typedef struct lvrgb_grid_config {

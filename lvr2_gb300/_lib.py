@@ -24,7 +24,8 @@ EXPORTS = [
     "lvrgb_surface_config_default", "lvrgb_surface_create", "lvrgb_surface_destroy", "lvrgb_surface_set_k",
     "lvrgb_surface_set_flip_point", "lvrgb_surface_set_method", "lvrgb_surface_bounding_box",
     "lvrgb_surface_num_points", "lvrgb_calculate_normals", "lvrgb_get_normals", "lvrgb_get_raw_normals",
-    "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance", "lvrgb_grid_distances",
+    "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance",
+    "lvrgb_distance_adjoint", "lvrgb_project_to_surface", "lvrgb_grid_distances",
     "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
     "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches", "lvrgb_knn_small_noalloc",
     "lvrgb_batch_create", "lvrgb_batch_destroy", "lvrgb_batch_calculate_normals", "lvrgb_batch_get_normals",
@@ -90,6 +91,8 @@ def load(path=None):
     L.lvrgb_normal_stats.argtypes = [vp, vp]
     L.lvrgb_knn.argtypes = [vp, vp, i64, i32, vp, vp, vp, i32, vp]
     L.lvrgb_distance.argtypes = [vp, vp, i64, vp, vp, i32, vp]
+    L.lvrgb_distance_adjoint.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp]
+    L.lvrgb_project_to_surface.argtypes = [vp, vp, i64, i32, vp, vp, i32, vp]
     L.lvrgb_grid_distances.argtypes = [vp, vp, i64, f32, vp, vp, i32, vp]
     L.lvrgb_interpolated_normal.argtypes = [vp, vp, i64, vp, i32, vp]
     L.lvrgb_reconstruct.argtypes = [vp, ctypes.POINTER(GridConfig), ctypes.POINTER(MeshInfo), vp]

@@ -10,6 +10,7 @@
 
 #include "lvrgb.h"
 #include "batch.h"
+#include "adjoint.h"
 #include "grid.h"
 #include "lbvh_build.h"
 #include "primitives.cuh"
@@ -133,6 +134,13 @@ void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
         throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack) ? "kNN traversal exceeded its stack depth"
                                                             : "tree walk exceeded its bound (malformed tree)"};
     }
+}
+
+// Rows of AoS positions as float4 (xyz, row index bits), in the given order.
+__global__ void pack_queries_kernel(const float* __restrict__ q, int nq, float4* __restrict__ qs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    qs[i] = make_float4(q[3 * size_t(i)], q[3 * size_t(i) + 1], q[3 * size_t(i) + 2], __uint_as_float(uint32_t(i)));
 }
 
 __global__ void morton_to_aos_kernel(const float4* __restrict__ v, const float4* __restrict__ pts, int n,
@@ -514,6 +522,75 @@ lvrgb_status lvrgb_distance(lvrgb_surface s, const float* q, int64_t nq, float* 
         signed_distance_rows(s->T, s->normals, s->cfg.kd, qs, int(nq), 1.0f, dp, de, nullptr, s->ws, s->d_err, st);
         finish_out(projected, dp, size_t(nq), on_device, st);
         if (euclidean) finish_out(euclidean, de, size_t(nq), on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_distance_adjoint(lvrgb_surface s, const float* q, int64_t nq, const float* grad_projected,
+                                    const float* grad_euclidean, float* projected, float* euclidean, float* grad_q,
+                                    float* grad_points, float* grad_normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(nq == 0 || q, LVRGB_ERR_INVALID_ARGUMENT, "NULL query array");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const int n = s->T.n;
+        // gradients w.r.t. points and normals start at zero
+        float4* gp = grad_points ? s->ws.get<float4>("adj.gp", size_t(n)) : nullptr;
+        float4* gn = grad_normals ? s->ws.get<float4>("adj.gn", size_t(n)) : nullptr;
+        if (gp && n) LVRGB_CUDA(cudaMemsetAsync(gp, 0, sizeof(float4) * size_t(n), st));
+        if (gn && n) LVRGB_CUDA(cudaMemsetAsync(gn, 0, sizeof(float4) * size_t(n), st));
+        AdjointOut o;
+        if (nq > 0) {
+            const float4* qs = prepare_queries(s, q, nq, on_device, st);
+            o.gdist = grad_projected ? stage_in(s->ws, "adj.gd", grad_projected, size_t(nq), on_device, st) : nullptr;
+            o.geucl = grad_euclidean ? stage_in(s->ws, "adj.ge", grad_euclidean, size_t(nq), on_device, st) : nullptr;
+            o.dist = projected ? stage_out(s->ws, "adj.d", projected, size_t(nq), on_device) : nullptr;
+            o.eucl = euclidean ? stage_out(s->ws, "adj.e", euclidean, size_t(nq), on_device) : nullptr;
+            o.gq = grad_q ? stage_out(s->ws, "adj.gq", grad_q, size_t(nq) * 3, on_device) : nullptr;
+            o.gp = gp;
+            o.gn = gn;
+            distance_adjoint(s->T, s->normals, s->cfg.kd, qs, int(nq), o, s->ws, s->d_err, st);
+            if (projected) finish_out(projected, o.dist, size_t(nq), on_device, st);
+            if (euclidean) finish_out(euclidean, o.eucl, size_t(nq), on_device, st);
+            if (grad_q) finish_out(grad_q, o.gq, size_t(nq) * 3, on_device, st);
+        }
+        // Morton order -> input order
+        for (int t = 0; t < 2; t++) {
+            float* host = t == 0 ? grad_points : grad_normals;
+            const float4* acc = t == 0 ? gp : gn;
+            if (!host || n == 0) continue;
+            float* d = stage_out(s->ws, t == 0 ? "adj.gpo" : "adj.gno", host, size_t(n) * 3, on_device);
+            morton_to_aos_kernel<<<ceil_div(n, 256), 256, 0, st>>>(acc, s->T.pts, n, d);
+            LVRGB_LAUNCH_CHECK();
+            finish_out(host, d, size_t(n) * 3, on_device, st);
+        }
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_project_to_surface(lvrgb_surface s, const float* v, int64_t nv, int32_t steps,
+                                      float* out_positions, float* out_normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nv >= 0 && nv < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "position count out of range");
+        require(steps >= 1 && steps <= 64, LVRGB_ERR_INVALID_ARGUMENT, "steps must be in 1..64");
+        require(nv == 0 || v, LVRGB_ERR_INVALID_ARGUMENT, "NULL position array");
+        if (nv == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float* dv = stage_in(s->ws, "proj.v", v, size_t(nv) * 3, on_device, st);
+        float4* qs = s->ws.get<float4>("proj.qs", size_t(nv));
+        pack_queries_kernel<<<ceil_div(nv, 256), 256, 0, st>>>(dv, int(nv), qs);
+        LVRGB_LAUNCH_CHECK();
+        float* op = out_positions ? stage_out(s->ws, "proj.op", out_positions, size_t(nv) * 3, on_device) : nullptr;
+        float* on = out_normals ? stage_out(s->ws, "proj.on", out_normals, size_t(nv) * 3, on_device) : nullptr;
+        project_to_surface(s->T, s->normals, s->cfg.kd, qs, int(nv), steps, op, on, s->ws, s->d_err, st);
+        if (op) finish_out(out_positions, op, size_t(nv) * 3, on_device, st);
+        if (on) finish_out(out_normals, on, size_t(nv) * 3, on_device, st);
         if (!on_device) check_kernel_error(s, st);
     });
 }
@@ -1023,11 +1100,6 @@ struct Carver {
     }
 };
 
-__global__ void pack_queries_kernel(const float* __restrict__ q, int nq, float4* __restrict__ qs) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nq) return;
-    qs[i] = make_float4(q[3 * size_t(i)], q[3 * size_t(i) + 1], q[3 * size_t(i) + 2], __uint_as_float(uint32_t(i)));
-}
 
 }  // namespace
 

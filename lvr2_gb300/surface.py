@@ -187,6 +187,53 @@ class Surface:
         check(_lib.load().lvrgb_distance(self._h, _ptr(q), len(q), _ptr(proj), _ptr(eucl), 0, self._stream))
         return proj, eucl
 
+    def distance_adjoint(self, queries, grad_projected=None, grad_euclidean=None, want_points=True,
+                         want_normals=True):
+        """Reverse mode of distance(): returns (projected, euclidean, grad_q,
+        grad_points, grad_normals) for upstream gradients of the projected
+        and Euclidean distances (None = 0).  Host numpy arrays or CUDA
+        tensors (all outputs then on the device)."""
+        q, on_dev = _f32x3(queries)
+        nq = len(q)
+        n = self.n
+        if on_dev:
+            import torch
+            dev = q.device
+
+            def empty(*shape):
+                return torch.empty(shape, dtype=torch.float32, device=dev)
+
+            def vec(a):
+                return None if a is None else a.to(device=dev, dtype=torch.float32).contiguous()
+        else:
+            def empty(*shape):
+                return np.empty(shape, np.float32)
+
+            def vec(a):
+                return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+        gd, ge = vec(grad_projected), vec(grad_euclidean)
+        proj, eucl, gq = empty(nq), empty(nq), empty(nq, 3)
+        gp = empty(n, 3) if want_points else None
+        gn = empty(n, 3) if want_normals else None
+        check(_lib.load().lvrgb_distance_adjoint(self._h, _ptr(q), nq, _ptr(gd), _ptr(ge), _ptr(proj), _ptr(eucl),
+                                                 _ptr(gq), _ptr(gp), _ptr(gn), on_dev, self._stream))
+        return proj, eucl, gq, gp, gn
+
+    def project_to_surface(self, positions, steps=3):
+        """Newton steps x <- x - d(x) n(x) onto the zero level; returns
+        (positions, unit normals)."""
+        v, on_dev = _f32x3(positions)
+        if on_dev:
+            import torch
+            pos = torch.empty_like(v)
+            nrm = torch.empty_like(v)
+        else:
+            pos = np.empty_like(v)
+            nrm = np.empty_like(v)
+        check(_lib.load().lvrgb_project_to_surface(self._h, _ptr(v), len(v), int(steps), _ptr(pos), _ptr(nrm), on_dev,
+                                                   self._stream))
+        return pos, nrm
+
     def grid_distances(self, queries, voxel_size):
         q, on_dev = _f32x3(queries)
         if on_dev:
