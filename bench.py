@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--seed-radius", type=int, default=1, help="seed buckets on each side (tuning)")
     ap.add_argument("--no-batched", action="store_true", help="skip the scan-project (batched) measurement")
     ap.add_argument("--batched-scale", type=float, default=1.0, help="scale of the 64-scan project")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the terrain adjoint measurement")
+    ap.add_argument("--adjoint-scale", type=float, default=1.0, help="scale of the 30M-point terrain")
     return ap.parse_args()
 
 
@@ -191,6 +193,56 @@ def batched_measurement(args, steps):
             "speedup_vs_plain": plain_ms / batched_ms, "autotuned": {"bucket": bucket, "seed_radius": radius},
             "batched_stage_ms": {"tree": float(stage[0]), "normals": float(stage[1]), "interpolation": float(stage[2])},
             "fitted_per_round": [int(x) for x in counters[:5]], "graph": True}
+
+
+def adjoint_measurement(args, steps):
+    """Adjoint form on terrain: 30M points on a value-noise heightfield
+    (sigma 0.2), kd = 10, voxel size 0.5.  The grid's vertices go through the
+    signed distance (forward, the reconstruct stage) and its adjoint
+    (forward + gradients w.r.t. queries, points and normals through
+    lvrgb_distance_adjoint, device buffers); the mesh vertices through three
+    Newton steps onto the zero level (lvrgb_project_to_surface)."""
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    n = int(30_000_000 * args.adjoint_scale)
+    pts = synthetic.terrain_device(n, seed=5)
+    out = {"workload": "terrain_30M" if args.adjoint_scale == 1.0 else "terrain_%d" % n, "points": n, "kd": 10,
+           "voxelsize": 0.5, "kn": 10, "ki": 10, "nem": 3}
+    with lvr2_gb300.Surface(pts, kn=10, ki=10, kd=10, nem=3, flip_point=(500.0, 500.0, 500.0)) as s:
+        s.calculate_normals()
+        info = s.reconstruct(voxelsize=0.5, decomposition="PMC")
+        sdf_ms = float(s.timings()[4])
+        _, pos, _, _ = s.grid()
+        v, _, _ = s.mesh(with_edges=False)
+        q = torch.from_numpy(pos).cuda()
+        vt = torch.from_numpy(v).cuda()
+        nq = q.shape[0]
+        gd = torch.ones(nq, device="cuda", dtype=torch.float32)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            ev[0].record()
+            for _ in range(max(steps, 1)):
+                fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            return ev[0].elapsed_time(ev[1]) / max(steps, 1)
+
+        fwd_ms = timed(lambda: s.distance_adjoint(q, None, None, want_points=False, want_normals=False))
+        adj_ms = timed(lambda: s.distance_adjoint(q, gd, None, want_points=True, want_normals=True))
+        proj_ms = timed(lambda: s.project_to_surface(vt, steps=3))
+    out.update({"grid_vertices": int(nq), "mesh_vertices": int(v.shape[0]), "cells_valid": int(info.cells_valid),
+                "sdf_stage_ms": sdf_ms, "sdf_evals_per_s_stage": nq / (sdf_ms / 1000.0),
+                "forward_api_ms": fwd_ms, "forward_evals_per_s": nq / (fwd_ms / 1000.0),
+                "adjoint_api_ms": adj_ms, "adjoint_evals_per_s": nq / (adj_ms / 1000.0),
+                "adjoint_over_forward": adj_ms / fwd_ms,
+                "projection_3_steps_ms": proj_ms, "projected_vertices_per_s": v.shape[0] / (proj_ms / 1000.0),
+                "note": "API timings include the Morton sort of the queries; device buffers"})
+    return out
 
 
 def cpu_reference_step(points, threads=0, canonical=False):
@@ -371,6 +423,8 @@ def run_gpu(args):
     }
     if not args.no_batched:
         line["batched"] = batched_measurement(args, args.steps)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_measurement(args, args.steps)
     if not args.no_cpu_baseline:
         sample = cpu_sample(pts)
         dt, _ = cpu_reference_step(sample)

@@ -231,6 +231,36 @@ def terrain(n=30_000_000, seed=5, size=1000.0, sigma=0.2, octaves=8):
     return np.stack([x, y, z], axis=1).astype(np.float32)
 
 
+def terrain_device(n=30_000_000, seed=5, size=1000.0, sigma=0.2, octaves=8, device="cuda"):
+    """terrain()'s heightfield (same value-noise lattices) evaluated with torch
+    on a device, positions from a seeded torch generator (a different random
+    stream than terrain()).  Returns a contiguous float32 (n, 3) tensor."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    x = torch.rand(n, generator=gen, device=device, dtype=torch.float64) * size
+    y = torch.rand(n, generator=gen, device=device, dtype=torch.float64) * size
+    h = torch.zeros(n, device=device, dtype=torch.float64)
+    amp, freq = 60.0, 1.0 / 200.0
+    for o in range(octaves):
+        rng = np.random.Generator(np.random.PCG64(seed * 100 + o))
+        gx = int(math.ceil(1000 * freq)) + 2
+        lat = torch.from_numpy(rng.uniform(-1, 1, (gx, gx))).to(device)
+        fx, fy = x * freq, y * freq
+        ix, iy = torch.floor(fx), torch.floor(fy)
+        tx, ty = fx - ix, fy - iy
+        sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
+        ix = ix.long().clamp(0, gx - 2)
+        iy = iy.long().clamp(0, gx - 2)
+        a = lat[ix, iy] * (1 - sx) + lat[ix + 1, iy] * sx
+        b = lat[ix, iy + 1] * (1 - sx) + lat[ix + 1, iy + 1] * sx
+        h += amp * (a * (1 - sy) + b * sy)
+        amp *= 0.5
+        freq *= 2.0
+    z = h + torch.randn(n, generator=gen, device=device, dtype=torch.float64) * sigma
+    return torch.stack([x, y, z], dim=1).to(torch.float32).contiguous()
+
+
 def crop(points, fraction, center=None):
     """Spatial crop keeping about `fraction` of the points at unchanged density."""
     p = np.asarray(points)
