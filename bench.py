@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--batched-scale", type=float, default=1.0, help="scale of the 64-scan project")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the terrain adjoint measurement")
     ap.add_argument("--adjoint-scale", type=float, default=1.0, help="scale of the 30M-point terrain")
+    ap.add_argument("--no-precision", action="store_true", help="skip the folded-sheets precision measurement")
+    ap.add_argument("--precision-scale", type=float, default=1.0, help="scale of the 20M-point folded sheets")
     return ap.parse_args()
 
 
@@ -245,6 +247,56 @@ def adjoint_measurement(args, steps):
     return out
 
 
+def precision_measurement(args, steps):
+    """Precision stress: folded thin sheets offset by +1e5, 20M points,
+    sigma_normal 1e-4, kn = 50, nem 3 (FP32 with FP64 fallback below a
+    relative eigengap of 1e-3): normals/s and the angle to float64 PCA of the
+    same neighbourhoods on a 2000-point sample (p50, p99.9)."""
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    n = int(20_000_000 * args.precision_scale)
+    pts, vs = synthetic.folded_sheets(n, seed=3)
+    flip = (pts.astype(np.float64).mean(0) + np.array([0.0, 0.0, 1e3])).astype(np.float32)
+    d = torch.from_numpy(pts).cuda()
+    with lvr2_gb300.Surface(d, kn=50, ki=0, nem=3, flip_point=flip) as s:
+        s.calculate_normals()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(max(steps, 1)):
+            s.calculate_normals()
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / max(steps, 1)
+        gn, gk = s.raw_normals()
+        stats = s.normal_stats()
+        rng = np.random.Generator(np.random.PCG64(4))
+        sel = rng.choice(n, 2000, replace=False)
+        idx, nbr = [], []
+        for k in np.unique(gk[sel]):
+            m = sel[gk[sel] == k]
+            i, _, _ = s.knn(pts[m], int(k))
+            idx.append(m)
+            nbr.extend(i)
+    idx = np.concatenate(idx)
+    P = pts.astype(np.float64)
+    ref = np.empty((len(idx), 3))
+    for r, (qi, nb) in enumerate(zip(idx, nbr)):
+        S = np.concatenate([P[qi:qi + 1], P[nb[nb != 0xFFFFFFFF].astype(np.int64)]])
+        w, V = np.linalg.eigh(np.cov(S.T, bias=True))
+        ref[r] = V[:, 0] if np.dot(V[:, 0], flip - P[qi]) >= 0 else -V[:, 0]
+    a = gn[idx].astype(np.float64)
+    a /= np.linalg.norm(a, axis=1, keepdims=True)
+    ang = np.degrees(np.arccos(np.clip(np.sum(a * ref, 1), -1, 1)))
+    return {"workload": "folded_sheets_offset_1e5_%dM" % round(n / 1e6), "points": n, "kn": 50, "nem": 3,
+            "voxelsize": vs, "normals_ms": ms, "normals_per_s": n / (ms / 1000.0),
+            "fitted_per_round": [int(x) for x in stats[:5]], "fp64_eigensolves": int(stats[5]),
+            "angle_deg_vs_fp64": {"p50": float(np.percentile(ang, 50)), "p99.9": float(np.percentile(ang, 99.9)),
+                                  "max": float(ang.max()), "sample": len(idx)}}
+
+
 def cpu_reference_step(points, threads=0, canonical=False):
     """One pass of the reference algorithm on the host (oracle/)."""
     from oracle import oracle as O
@@ -425,6 +477,8 @@ def run_gpu(args):
         line["batched"] = batched_measurement(args, args.steps)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(args, args.steps)
+    if not args.no_precision:
+        line["precision"] = precision_measurement(args, args.steps)
     if not args.no_cpu_baseline:
         sample = cpu_sample(pts)
         dt, _ = cpu_reference_step(sample)
