@@ -138,6 +138,7 @@ struct NormalsArgs {
     // Squared distance of the k-th neighbour of every point that searches
     // again (by Morton position): written by a round, read by the next one.
     float* kth_d2;
+    int wide_tile;  // queries per warp tile of the one-warp-per-query kernel (1..32)
     unsigned long long* gheap;
     int* err;
     uint32_t* stats;
@@ -465,7 +466,7 @@ constexpr int kWideWarps = 8;  // warps per block
 // Growth of the squared k-th neighbour distance when k doubles: 2 on a
 // surface, 4 along a line; above 2 most searches need no second pass.
 constexpr float kBoundGrowth = 2.5f;
-constexpr int kWideTile = 8;   // queries per warp tile
+constexpr int kWideTileMax = 32;  // queries per warp tile (consecutive queries chain their bounds)
 
 template <int kNem>
 __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(NormalsArgs A) {
@@ -480,37 +481,69 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
     const int nq = A.nq_dev ? int(*A.nq_dev) : A.nq;
     const int B = A.T.bucket;
     TravStats st;
-    for (int tile = blockIdx.x * kWideWarps + wib; tile * kWideTile < nq; tile += gridDim.x * kWideWarps) {
+    const int TQ = A.wide_tile;
+    for (int tile = blockIdx.x * kWideWarps + wib; tile * TQ < nq; tile += gridDim.x * kWideWarps) {
         unsigned fitted = 0, retry = 0;
-        const int nt = min(kWideTile, nq - tile * kWideTile);
+        const int nt = min(TQ, nq - tile * TQ);
+        // the previous query of this tile: position, k-th squared distance, scan
+        float cx = 0, cy = 0, cz = 0, ctau = __int_as_float(0x7f800000);
+        int cscan = -1;
         for (int j = 0; j < nt; j++) {
-            const int qi = tile * kWideTile + j;
+            const int qi = tile * TQ + j;
             const int pos = A.list ? int(__ldg(A.list + qi)) : qi;
             const float4 q = __ldg(A.T.pts + pos);
-            int root = 0, blo = 0, bhi = 0x7fffffff;
+            int root = 0, blo = 0, bhi = 0x7fffffff, scan = 0;
             float fx = A.fx, fy = A.fy, fz = A.fz;
             if (A.segs) {
                 if (__float_as_uint(q.w) == 0xffffffffu) continue;  // padding after a scan
-                const SegInfo g = A.segs[A.bucket_scan[pos / B]];
+                scan = A.bucket_scan[pos / B];
+                const SegInfo g = A.segs[scan];
                 root = g.root; blo = g.blo; bhi = g.bhi;
                 fx = g.fx; fy = g.fy; fz = g.fz;
             }
-            // The previous round's k-th distance, scaled for twice the k, bounds
-            // the search; when fewer than K points lie within the bound the
-            // search runs again without one.  Either way the result is exact.
-            float bound = __int_as_float(0x7f800000);
+            // Search bounds, each exact when at least K points lie within it:
+            //  * chain: the previous query's K points lie within
+            //    (sqrt(ctau) + |q - q_prev|) of q (triangle inequality; a
+            //    relative margin covers the float rounding), so this bound
+            //    holds them,
+            //  * estimate: the previous round's k-th distance of this point,
+            //    scaled for twice the k, which may hold fewer.
+            // A search that finds fewer than K points within its bound runs
+            // again with the next larger one, the last without a bound.
+            const float inf = __int_as_float(0x7f800000);
+            float chain = inf;
+            if (ctau < FLT_MAX && cscan == scan) {
+                const float dx = __fsub_rn(q.x, cx), dy = __fsub_rn(q.y, cy), dz = __fsub_rn(q.z, cz);
+                const float delta = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                         __fmul_rn(dz, dz)));
+                const float r = __fmul_rn(__fadd_rn(__fsqrt_rn(ctau), delta), 1.0000038f);
+                chain = __fmul_rn(__fmul_rn(r, r), 1.0000038f);
+            }
+            float estimate = inf;
             if (A.round > 1 && A.kth_d2) {
                 const float prev = A.kth_d2[pos];
-                if (prev < FLT_MAX) bound = __fmul_rn(prev, kBoundGrowth);
+                if (prev < FLT_MAX) estimate = __fmul_rn(prev, kBoundGrowth);
             }
-            for (int attempt = 0; attempt < 2; attempt++) {
+            float bound = fminf(chain, estimate);
+            for (int attempt = 0; attempt < 3; attempt++) {
                 wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, pos / B, root, blo, bhi, bound);
                 if (W.cnt >= W.K || !(bound < FLT_MAX)) break;
-                bound = __int_as_float(0x7f800000);
+                bound = (bound < chain && chain < FLT_MAX) ? chain : inf;
                 st.retries++;
             }
             st.rounds++;
             const int cnt = W.cnt;
+            // the K-th key of this query bounds the next one's search
+            ctau = inf;
+            if (cnt == W.K) {
+                unsigned long long mx = 0;
+                for (int i = lane; i < cnt; i += 32) mx = max(mx, W.keys[i]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+                ctau = key_d2(mx);
+                cx = q.x; cy = q.y; cz = q.z;
+                cscan = scan;
+            }
             // pass 1: neighbourhood box (min / max: exact in any order)
             float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
             for (int i = lane; i < cnt; i += 32) {
@@ -533,14 +566,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
             }
             if (!fit) {
                 retry |= 1u << j;
-                if (A.kth_d2) {
-                    // the K-th key is the largest one kept
-                    unsigned long long mx = 0;
-                    for (int i = lane; i < cnt; i += 32) mx = max(mx, W.keys[i]);
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
-                    if (lane == 0) A.kth_d2[pos] = cnt == A.K ? key_d2(mx) : __int_as_float(0x7f800000);
-                }
+                if (A.kth_d2 && lane == 0) A.kth_d2[pos] = ctau;
                 continue;
             }
             // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
@@ -638,7 +664,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
             fitted |= 1u << j;
         }
         if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
-        if (lane < nt) A.flags[tile * kWideTile + lane] = uint8_t((retry >> lane) & 1u);
+        if (lane < nt) A.flags[tile * TQ + lane] = uint8_t((retry >> lane) & 1u);
     }
     if (lane == 0 && st.nodes) {
         atomicAdd(A.stats + 6, st.retries);
@@ -906,7 +932,10 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
     }
     // one warp per query; key buffers in shared memory when they fit
     const size_t per_warp = size_t(wide_capacity(A.K)) * sizeof(unsigned long long);
-    const int tiles = ceil_div(std::max(grid_nq, 1), kWideTile);
+    // long tiles carry the chained bound further; shorter ones when there
+    // are too few queries to give every resident warp work
+    A.wide_tile = std::max(2, std::min(kWideTileMax, grid_nq / (g_num_sms * 128)));
+    const int tiles = ceil_div(std::max(grid_nq, 1), A.wide_tile);
     const int need = std::max(1, ceil_div(tiles, kWideWarps));
     size_t smem = size_t(kWideWarps) * 1024;
     int blocks = need;
