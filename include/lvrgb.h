@@ -230,6 +230,16 @@ lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrg
 lvrgb_status lvrgb_get_mesh(lvrgb_surface s, float* vertices, uint32_t* faces, int32_t* vertex_edges,
                             int32_t on_device, void* stream);
 
+/* BilinearFastBox::optimizePlanarFaces (BilinearFastBox.tcc:140-212), the
+ * post-pass that FastReconstruction::getMesh runs for PMC with kc = 5
+ * (FastReconstruction.tcc:158-168), on the last mesh in place: in every cell
+ * whose faces have one or two border edges, both end vertices of each such
+ * edge move to the centroid of their kc (1..96) nearest points.  lvr2 moves
+ * vertices in place in hash-map order, so a vertex on several such edges can
+ * move twice; here each moves once, from its marching-cubes position.
+ * moved (may be NULL) receives the number of moved vertices.  Synchronous. */
+lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* moved, void* stream);
+
 /* The last grid, sorted by lattice key: each grid vertex's lattice index
  * (Q x 3), position (Q x 3), projected distance and invalid flag; any
  * pointer may be NULL.  Same content as HashGrid::getQueryPoints

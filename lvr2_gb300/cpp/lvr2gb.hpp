@@ -53,6 +53,9 @@ struct GridOptions {
     int intersections = -1;
     bool extrude = true;
     std::string decomposition = "PMC";
+    // PMC meshes get BilinearFastBox::optimizePlanarFaces with kc = 5, as in
+    // FastReconstruction::getMesh (FastReconstruction.tcc:158-168)
+    bool optimizePlanarFaces = true;
 };
 
 class Surface {
@@ -174,6 +177,8 @@ class Surface {
         }
         Mesh m;
         check(lvrgb_reconstruct(h_, &g, &m.info, nullptr), "reconstruct");
+        if (g.decomposition == 1 && o.optimizePlanarFaces)
+            check(lvrgb_optimize_planar_faces(h_, 5, nullptr, nullptr), "optimizePlanarFaces");
         m.vertices.resize(size_t(3 * m.info.vertices));
         m.faces.resize(size_t(3 * m.info.faces));
         check(lvrgb_get_mesh(h_, m.vertices.data(), m.faces.data(), nullptr, 0, nullptr), "getMesh");

@@ -12,6 +12,7 @@
 #include "batch.h"
 #include "adjoint.h"
 #include "grid.h"
+#include "planar.h"
 #include "lbvh_build.h"
 #include "primitives.cuh"
 #include "surface.h"
@@ -667,6 +668,19 @@ lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrg
             info->voxelsize = s->grid.vs;
             for (int i = 0; i < 4; i++) info->stage_ms[i] = tm.ms[i];
         }
+    });
+}
+
+lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* moved, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
+        require(kc >= 1 && kc <= kSmemHeapMax, LVRGB_ERR_INVALID_ARGUMENT, "kc must be in 1..96");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const long long m = optimize_planar_faces(s->T, s->d_box, s->grid, kc, s->ws, s->d_err, st);
+        check_kernel_error(s, st);
+        if (moved) *moved = m;
     });
 }
 

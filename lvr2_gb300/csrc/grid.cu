@@ -518,6 +518,7 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     R.nfaces = (long long)nf;
     R.nverts = (long long)nv;
     R.faces = faces;
+    R.face_cell_off = foff;
     R.vert_keys = vkeys;
     R.verts = verts;
     timer.finish(timings, s);

@@ -35,6 +35,7 @@ struct GridResult {
     uint64_t* vert_keys = nullptr;   // [nverts] (corner lattice key << 2) | axis
     float* verts = nullptr;          // [nverts * 3]
     uint32_t* faces = nullptr;       // [nfaces * 3]
+    uint32_t* face_cell_off = nullptr;  // [ncells_valid + 1] faces of valid cell c: [off[c], off[c + 1])
 };
 
 // Per-stage device time (ms) of the last grid_reconstruct call when events

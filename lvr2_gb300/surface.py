@@ -266,6 +266,13 @@ class Surface:
         self.info = info
         return info
 
+    def optimize_planar_faces(self, kc=5):
+        """BilinearFastBox::optimizePlanarFaces on the last mesh (in place);
+        returns the number of moved vertices."""
+        moved = ctypes.c_int64(0)
+        check(_lib.load().lvrgb_optimize_planar_faces(self._h, int(kc), ctypes.byref(moved), self._stream))
+        return int(moved.value)
+
     def mesh(self, with_edges=True):
         info = self.info
         v = np.empty((info.vertices, 3), np.float32)

@@ -736,6 +736,7 @@ struct orc_recon {
     std::vector<EdgeKey> mv_key;
     std::vector<V3> mv_pos;
     std::vector<int32_t> faces;
+    std::vector<int64_t> cell_face_off;  // faces of valid cell c: [off[c], off[c + 1])
 };
 
 extern "C" {
@@ -848,6 +849,7 @@ orc_recon* orc_reconstruct(const orc_surface* s, const float* normals, float res
     // of an edge through neighbor_table / neighbor_vertex_table, which gives
     // the same identification.
     std::unordered_map<EdgeKey, int32_t, EdgeKeyHash> vmap;
+    r->cell_face_off.push_back(0);
     for (size_t vc : valid_cells) {
         const L3& ci = r->cells_all[vc];
         float dist[8];
@@ -903,8 +905,60 @@ orc_recon* orc_reconstruct(const orc_surface* s, const float* normals, float res
                 r->faces.push_back(vid);
             }
         }
+        r->cell_face_off.push_back(int64_t(r->faces.size() / 3));
     }
     return r;
+}
+
+// BilinearFastBox::optimizePlanarFaces (BilinearFastBox.tcc:140-212), which
+// FastReconstruction::getMesh runs on every cell with kc = 5 for PMC
+// (FastReconstruction.tcc:158-168): in a cell whose faces have one or two
+// border edges (edges of exactly one face of the mesh), both end vertices of
+// each such edge move to the centroid of the kc nearest points.  The
+// reference moves vertices in place while iterating its cell hash map, so a
+// vertex on several such edges can move more than once, in an order that
+// depends on the hash map.  Canonical form: every marked vertex moves once,
+// from its marching-cubes position.  Returns the number of moved vertices.
+int64_t orc_recon_optimize_planar(orc_recon* r, const orc_surface* s, int kc, int canonical, int threads) {
+    set_threads(threads);
+    const size_t nf = r->faces.size() / 3;
+    auto edge_key = [&](size_t f, int e) {
+        const uint64_t a = uint32_t(r->faces[3 * f + size_t(e)]);
+        const uint64_t b = uint32_t(r->faces[3 * f + size_t((e + 1) % 3)]);
+        return a < b ? (a << 32) | b : (b << 32) | a;
+    };
+    std::unordered_map<uint64_t, int> faces_of_edge;
+    for (size_t f = 0; f < nf; f++)
+        for (int e = 0; e < 3; e++) faces_of_edge[edge_key(f, e)]++;
+    std::vector<uint8_t> mark(r->mv_pos.size(), 0);
+    for (size_t c = 0; c + 1 < r->cell_face_off.size(); c++) {
+        const size_t f0 = size_t(r->cell_face_off[c]), f1 = size_t(r->cell_face_off[c + 1]);
+        int border = 0;
+        for (size_t f = f0; f < f1; f++)
+            for (int e = 0; e < 3; e++) border += faces_of_edge[edge_key(f, e)] == 1;
+        if (border != 1 && border != 2) continue;
+        for (size_t f = f0; f < f1; f++)
+            for (int e = 0; e < 3; e++)
+                if (faces_of_edge[edge_key(f, e)] == 1) {
+                    mark[size_t(r->faces[3 * f + size_t(e)])] = 1;
+                    mark[size_t(r->faces[3 * f + size_t((e + 1) % 3)])] = 1;
+                }
+    }
+    const std::vector<V3> orig = r->mv_pos;
+    int64_t moved = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : moved)
+    for (int64_t v = 0; v < int64_t(orig.size()); v++) {
+        if (!mark[size_t(v)]) continue;
+        moved++;
+        std::vector<uint32_t> id;
+        s->ksearch(orig[size_t(v)], kc, canonical != 0, id);
+        if (id.empty()) continue;
+        V3 c;
+        for (auto j : id) c += s->pts[j];
+        c /= float(id.size());
+        r->mv_pos[size_t(v)] = c;
+    }
+    return moved;
 }
 
 void orc_recon_destroy(orc_recon* r) { delete r; }

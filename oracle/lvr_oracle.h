@@ -79,6 +79,10 @@ void orc_recon_cells(const orc_recon* r, int32_t* cells_all, int32_t* cells_vali
 /* mesh: vertex keys (lattice of the edge's low corner x3, axis), positions,
  * faces as vertex indices (emission order within a cell follows the MC table). */
 void orc_recon_mesh(const orc_recon* r, int32_t* vkeys, float* vpos, int32_t* faces);
+/* BilinearFastBox::optimizePlanarFaces on the mesh of r, in canonical form
+ * (each marked vertex moves once, from its marching-cubes position); returns
+ * the number of moved vertices. */
+int64_t orc_recon_optimize_planar(orc_recon* r, const orc_surface* s, int kc, int canonical, int threads);
 
 /* Table dump (used to pin the tables against the reference headers). */
 int orc_mc_table(int32_t* out256x13);

@@ -59,6 +59,8 @@ def lib():
     L.orc_recon_grid.argtypes = [_vp, _i32p, _f32p, _f32p, _u8p]
     L.orc_recon_cells.argtypes = [_vp, _i32p, _i32p]
     L.orc_recon_mesh.argtypes = [_vp, _i32p, _f32p, _i32p]
+    L.orc_recon_optimize_planar.restype = _i64
+    L.orc_recon_optimize_planar.argtypes = [_vp, _vp, _int, _int, _int]
     L.orc_mc_table.argtypes = [_i32p]
     _lib = L
     return L
@@ -135,8 +137,10 @@ class OracleSurface:
         return out
 
     def reconstruct(self, normals, voxelsize=None, intersections=None, extrude=True, kd=5,
-                    decomposition="PMC", canonical=True, grid_override=None):
-        """PointsetGrid + calcDistanceValues + marching cubes.  Returns a dict."""
+                    decomposition="PMC", canonical=True, grid_override=None, planar_kc=0):
+        """PointsetGrid + calcDistanceValues + marching cubes (+ the PMC
+        optimizePlanarFaces post-pass with planar_kc nearest points when
+        planar_kc > 0).  Returns a dict."""
         nrm = _pts(normals)
         if intersections is not None and intersections > 0:
             res, isvs = float(intersections), 0
@@ -155,6 +159,9 @@ class OracleSurface:
         h = L.orc_reconstruct(self._h, nrm.reshape(-1), res, isvs, int(extrude), kd, dec,
                               int(canonical), *args, self.threads)
         try:
+            moved = 0
+            if planar_kc > 0:
+                moved = int(L.orc_recon_optimize_planar(h, self._h, int(planar_kc), int(canonical), self.threads))
             c = np.zeros(8, np.int64)
             f = np.zeros(4, np.float32)
             L.orc_recon_counts(h, c, f)
@@ -175,7 +182,7 @@ class OracleSurface:
             L.orc_recon_destroy(h)
         return dict(voxelsize=float(f[0]), cells_all=cells_all, cells_valid=cells_valid,
                     qp_lattice=lat, qp_pos=pos, qp_dist=dist, qp_invalid=inv,
-                    vkeys=vkeys, vpos=vpos, faces=faces)
+                    vkeys=vkeys, vpos=vpos, faces=faces, planar_moved=moved)
 
 
 def mc_table():
