@@ -366,10 +366,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
         }
         bool retry = false;
         if (active) {
-            // Ascending order puts the real entries first (fewer points than K)
-            // and gives the interpolation its ki nearest in lvr2's order.
+            // Ascending order puts the real entries first (fewer points than K),
+            // gives the interpolation its ki nearest in lvr2's order, and makes
+            // the sums below independent of the order the search met the
+            // neighbours in (any tree over the same points gives the same normal).
             const int cnt = heap.real;
-            if (cnt < A.K || A.nbr) heap.sort_ascending();
+            heap.sort_ascending();
             NbrPass P;
             neighbour_pass<kNem>(A.T, heap, cnt, q, P);
             bool fit = true;
@@ -813,6 +815,65 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
     }
 }
 
+// rows_kernel (index and distance rows) for K > kSmemHeapMax: one warp per
+// query (wide.cuh); consecutive Morton-sorted queries of a warp tile chain
+// their search bounds as in normals_wide_kernel.
+__global__ void __launch_bounds__(kWideWarps * 32, 4) rows_wide_kernel(RowsArgs A, int TQ) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WideState W;
+    W.K = A.K;
+    W.cap = wide_capacity(A.K);
+    W.hist = reinterpret_cast<uint32_t*>(smem) + wib * 256;
+    W.keys = A.gheap ? A.gheap + (size_t(blockIdx.x) * kWideWarps + wib) * size_t(W.cap)
+                     : reinterpret_cast<unsigned long long*>(smem + kWideWarps * 1024) + size_t(wib) * W.cap;
+    const float inf = __int_as_float(0x7f800000);
+    TravStats st;
+    for (int tile = blockIdx.x * kWideWarps + wib; tile * TQ < A.nq; tile += gridDim.x * kWideWarps) {
+        const int nt = min(TQ, A.nq - tile * TQ);
+        float cx = 0, cy = 0, cz = 0, ctau = inf;
+        for (int j = 0; j < nt; j++) {
+            const float4 q = A.qs[tile * TQ + j];
+            float bound = inf;
+            if (ctau < FLT_MAX) {
+                const float dx = __fsub_rn(q.x, cx), dy = __fsub_rn(q.y, cy), dz = __fsub_rn(q.z, cz);
+                const float delta = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                         __fmul_rn(dz, dz)));
+                const float r = __fmul_rn(__fadd_rn(__fsqrt_rn(ctau), delta), 1.0000038f);
+                bound = __fmul_rn(__fmul_rn(r, r), 1.0000038f);
+            }
+            const int seed = seed_bucket_for(A.T, q.x, q.y, q.z);
+            for (int attempt = 0; attempt < 2; attempt++) {
+                wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, seed, 0, 0, 0x7fffffff, bound);
+                if (W.cnt >= W.K || !(bound < FLT_MAX)) break;
+                bound = inf;
+            }
+            const int cnt = W.cnt;
+            const size_t row = __float_as_uint(q.w);
+            uint32_t* ri = A.idx + row * A.K;
+            float* rd = A.dist + row * A.K;
+            unsigned long long mx = 0;
+            for (int i = lane; i < cnt; i += 32) mx = max(mx, W.keys[i]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+            wide_sorted_prefix(W, cnt, [&](int r, unsigned long long key) {
+                ri[r] = key_idx(key);
+                rd[r] = __fsqrt_rn(key_d2(key));
+            });
+            for (int r = cnt + lane; r < A.K; r += 32) {
+                ri[r] = 0xffffffffu;
+                rd[r] = inf;
+            }
+            if (A.count && lane == 0) A.count[row] = cnt;
+            ctau = inf;
+            if (cnt == W.K) {
+                ctau = key_d2(mx);
+                cx = q.x; cy = q.y; cz = q.z;
+            }
+        }
+    }
+}
+
 __global__ void query_morton_kernel(const float* __restrict__ q, int nq, const float* __restrict__ box,
                                     uint64_t* __restrict__ codes, uint32_t* __restrict__ idx) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -920,6 +981,34 @@ HeapPlan plan_heap(int nq, int K, Workspace& ws) {
 
 namespace {
 
+// Launch plan of the one-warp-per-query kernels: key buffers in shared
+// memory when they fit (200 KB per block), else one global buffer per
+// resident warp; long warp tiles carry the chained bound further, shorter
+// ones when there are too few queries to give every resident warp work.
+struct WidePlan {
+    int blocks, tile;
+    size_t smem;
+    unsigned long long* gbuf;
+};
+WidePlan plan_wide(int grid_nq, int K, Workspace& ws) {
+    WidePlan P;
+    const size_t per_warp = size_t(wide_capacity(K)) * sizeof(unsigned long long);
+    P.tile = std::max(2, std::min(kWideTileMax, grid_nq / (g_num_sms * 128)));
+    const int tiles = ceil_div(std::max(grid_nq, 1), P.tile);
+    const int need = std::max(1, ceil_div(tiles, kWideWarps));
+    P.smem = size_t(kWideWarps) * 1024;
+    P.blocks = need;
+    P.gbuf = nullptr;
+    if (P.smem + kWideWarps * per_warp <= size_t(200) * 1024) {
+        P.smem += kWideWarps * per_warp;
+    } else {
+        const int maxb = int(std::max<size_t>(1, (size_t(1) << 31) / (kWideWarps * per_warp)));
+        P.blocks = std::min({need, g_num_sms * 4, maxb});
+        P.gbuf = ws.get<unsigned long long>("knn.widebuf", size_t(P.blocks) * kWideWarps * (per_warp / 8));
+    }
+    return P;
+}
+
 template <int kNem>
 void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
     if (A.K <= kSmemHeapMax) {
@@ -930,25 +1019,11 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
         LVRGB_LAUNCH_CHECK();
         return;
     }
-    // one warp per query; key buffers in shared memory when they fit
-    const size_t per_warp = size_t(wide_capacity(A.K)) * sizeof(unsigned long long);
-    // long tiles carry the chained bound further; shorter ones when there
-    // are too few queries to give every resident warp work
-    A.wide_tile = std::max(2, std::min(kWideTileMax, grid_nq / (g_num_sms * 128)));
-    const int tiles = ceil_div(std::max(grid_nq, 1), A.wide_tile);
-    const int need = std::max(1, ceil_div(tiles, kWideWarps));
-    size_t smem = size_t(kWideWarps) * 1024;
-    int blocks = need;
-    A.gheap = nullptr;
-    if (smem + kWideWarps * per_warp <= size_t(200) * 1024) {
-        smem += kWideWarps * per_warp;
-    } else {
-        const int maxb = int(std::max<size_t>(1, (size_t(1) << 31) / (kWideWarps * per_warp)));
-        blocks = std::min({need, g_num_sms * 4, maxb});
-        A.gheap = ws.get<unsigned long long>("knn.widebuf", size_t(blocks) * kWideWarps * (per_warp / 8));
-    }
-    set_smem(normals_wide_kernel<kNem>, smem);
-    normals_wide_kernel<kNem><<<blocks, kWideWarps * 32, smem, s>>>(A);
+    const WidePlan P = plan_wide(grid_nq, A.K, ws);
+    A.wide_tile = P.tile;
+    A.gheap = P.gbuf;
+    set_smem(normals_wide_kernel<kNem>, P.smem);
+    normals_wide_kernel<kNem><<<P.blocks, kWideWarps * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }
 
@@ -1137,6 +1212,19 @@ void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, flo
     A.normals = nullptr;
     A.nout = nullptr;
     A.err = d_err;
+    if (k > kSmemHeapMax) {
+        if (g_num_sms == 0) {
+            int dev = 0;
+            LVRGB_CUDA(cudaGetDevice(&dev));
+            LVRGB_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        }
+        const WidePlan W = plan_wide(nq, k, ws);
+        A.gheap = W.gbuf;
+        set_smem(rows_wide_kernel, W.smem);
+        rows_wide_kernel<<<W.blocks, kWideWarps * 32, W.smem, s>>>(A, W.tile);
+        LVRGB_LAUNCH_CHECK();
+        return;
+    }
     HeapPlan P = plan_heap(nq, k, ws);
     A.gheap = P.gheap;
     set_smem(rows_kernel, P.smem);

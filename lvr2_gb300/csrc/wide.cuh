@@ -292,17 +292,45 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
     wide_shrink(W, st);
 }
 
+// Sorts keys[0, cnt) ascending in place by a warp bitonic network over the
+// next power of two, padding with ~0 (the buffer holds at least that many:
+// cnt <= K and the capacity exceeds 2K).
+__device__ __noinline__ void warp_bitonic_sort(unsigned long long* keys, int cnt) {
+    const int lane = threadIdx.x & 31;
+    int P = 1;
+    while (P < cnt) P <<= 1;
+    for (int i = cnt + lane; i < P; i += 32) keys[i] = ~0ull;
+    __syncwarp();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < P; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = keys[i], b = keys[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // Hands the m smallest of the W.cnt buffered keys to emit(rank, key), rank
 // 0 = nearest; 1 <= m <= W.cnt.  The selected keys are staged in the histogram
-// area (m <= 128) and ranked among themselves; larger m are ranked in place.
+// area (m <= 128) and ranked among themselves; for larger m the buffer is
+// sorted.
 template <typename F>
 __device__ __forceinline__ void wide_sorted_prefix(WideState& W, int m, F&& emit) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     if (m <= 0) return;
-    const unsigned long long mth = m == W.cnt ? ~0ull : warp_select(W.keys, W.cnt, m, W.hist);
-    __syncwarp();
     if (m <= 128) {
+        const unsigned long long mth = m == W.cnt ? ~0ull : warp_select(W.keys, W.cnt, m, W.hist);
+        __syncwarp();
         unsigned long long* stage = reinterpret_cast<unsigned long long*>(W.hist);
         int c = 0;
         for (int base = 0; base < W.cnt; base += 32) {
@@ -321,15 +349,9 @@ __device__ __forceinline__ void wide_sorted_prefix(WideState& W, int m, F&& emit
             emit(rank, k);
         }
     } else {
-        for (int base = 0; base < W.cnt; base += 32) {
-            const int i = base + lane;
-            const unsigned long long k = i < W.cnt ? W.keys[i] : 0ull;
-            const bool sel = i < W.cnt && k <= mth;
-            if (__ballot_sync(kFull, sel) == 0) continue;
-            int rank = 0;
-            for (int j = 0; j < W.cnt; j++) rank += W.keys[j] < k ? 1 : 0;
-            if (sel) emit(rank, k);
-        }
+        // sort the whole buffer (the k-th selection above is not needed)
+        warp_bitonic_sort(W.keys, W.cnt);
+        for (int i = lane; i < m; i += 32) emit(i, W.keys[i]);
     }
     __syncwarp();
 }

@@ -109,3 +109,22 @@ def test_room_bucket_sizes(gb, oracle_mod, bucket):
     assert (gk == ok).all()
     ang = angle_deg(gn, on)
     assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG
+
+
+@pytest.mark.parametrize("k", [97, 200, 500])
+def test_knn_rows_large_k(gb, oracle_mod, k):
+    """kNN rows with k > 96 (one warp per query, sorted by a warp bitonic
+    sort): bit-exact, including queries outside the cloud and padding."""
+    P = plane_and_sphere(20_000)
+    rng = np.random.Generator(np.random.PCG64(6))
+    Q = np.concatenate([P[::41], rng.uniform(-2, 2, (300, 3)).astype(np.float32)])
+    o = oracle_mod.OracleSurface(P)
+    with gb.Surface(P) as s:
+        gi, gd, gc = s.knn(Q, k)
+    oi, od, oc = o.knn(Q, k)
+    assert (gc == oc).all() and (gi == oi).all() and np.array_equal(gd, od)
+    # fewer points than k: padded rows
+    with gb.Surface(P[:150]) as s:
+        gi, gd, gc = s.knn(Q[:40], k)
+    oi, od, oc = oracle_mod.OracleSurface(P[:150]).knn(Q[:40], k)
+    assert (gc == min(k, 150)).all() and (gi == oi).all() and np.array_equal(gd, od, equal_nan=True)
