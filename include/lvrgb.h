@@ -304,8 +304,9 @@ typedef struct lvrgb_batch_s* lvrgb_batch;
 
 /* xyz: all scans concatenated (n x 3); scan_offsets: nscans + 1 entries,
  * scan_offsets[0] = 0, strictly increasing; flip_points: nscans x 3 (the
- * scanner positions).  cfg: kn, ki (<= 2 kn), nem, adaptive, bucket,
- * seed_radius, device as for a surface (flip fields ignored).  Host arrays
+ * scanner positions).  cfg: kn, ki (<= 2 kn), kd (lvrgb_batch_grid_distances),
+ * nem, adaptive, bucket, seed_radius, device as for a surface (flip fields
+ * ignored).  Host arrays
  * for offsets and flips; xyz on host or device (on_device). */
 lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xyz, const int64_t* scan_offsets,
                                 int32_t nscans, const float* flip_points, int32_t on_device, void* stream,
@@ -319,6 +320,18 @@ lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, voi
 
 /* Normals of all scans in input order (n x 3). */
 lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_device, void* stream);
+
+/* Signed distance and invalid flag at the grid vertices of every scan
+ * (chunk), each against its own scan's points and normals: the GPU block of
+ * LargeScaleReconstruction::createChunk (LargeScaleReconstruction.tcc:636-688),
+ * which builds one GpuSurface per chunk, computes its normals and then
+ * GpuSurface::distances for the chunk grid's query points, for all chunks at
+ * once.  q: every chunk's query positions concatenated (host or device);
+ * q_offsets: nscans + 1 host entries, q_offsets[0] = 0, non-decreasing.
+ * Semantics per query as lvrgb_grid_distances with the batch's kd.  Needs
+ * lvrgb_batch_calculate_normals.  Synchronous for host pointers. */
+lvrgb_status lvrgb_batch_grid_distances(lvrgb_batch b, const float* q, const int64_t* q_offsets, float voxel_size,
+                                        float* distance, uint8_t* invalid, int32_t on_device, void* stream);
 
 /* Times the pipeline for each candidate (LBVH bucket 16/32, seed radius 1/2)
  * on this project and keeps the fastest; returns the choice. */

@@ -10,6 +10,7 @@
 
 #include "lvrgb.h"
 #include "batch.h"
+#include "chunks.h"
 #include "adjoint.h"
 #include "grid.h"
 #include "planar.h"
@@ -1006,6 +1007,38 @@ lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_d
         on_batch_stream(b, st, [&] { batch_scatter_normals(b->R, d, b->bs); });
         finish_out(normals, d, n * 3, on_device, st);
         if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_batch_grid_distances(lvrgb_batch b, const float* q, const int64_t* q_offsets, float voxel_size,
+                                        float* distance, uint8_t* invalid, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(b != nullptr && q_offsets != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        require(b->ran, LVRGB_ERR_STATE, "no normals: call lvrgb_batch_calculate_normals");
+        require(voxel_size > 0, LVRGB_ERR_INVALID_ARGUMENT, "voxel_size must be > 0");
+        const int S = int(b->offsets.size()) - 1;
+        require(q_offsets[0] == 0, LVRGB_ERR_INVALID_ARGUMENT, "q_offsets[0] must be 0");
+        for (int k = 0; k < S; k++)
+            require(q_offsets[k + 1] >= q_offsets[k], LVRGB_ERR_INVALID_ARGUMENT, "q_offsets must not decrease");
+        const int64_t nq = q_offsets[S];
+        require(nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(nq == 0 || (q && distance && invalid), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(b->device);
+        cudaStream_t st = as_stream(stream);
+        int64_t* d_off = b->ws.get<int64_t>("chunk.qoff", size_t(S) + 1);
+        LVRGB_CUDA(cudaMemcpyAsync(d_off, q_offsets, sizeof(int64_t) * (size_t(S) + 1), cudaMemcpyHostToDevice, st));
+        const float* dq = stage_in(b->ws, "chunk.q", q, size_t(nq) * 3, on_device, st);
+        float* dd = stage_out(b->ws, "chunk.d", distance, size_t(nq), on_device);
+        uint8_t* di = stage_out(b->ws, "chunk.inv", invalid, size_t(nq), on_device);
+        on_batch_stream(b, st, [&] {
+            chunk_grid_distances(b->R.tree, b->R.normals, b->cfg.kd, dq, d_off, int(nq), voxel_size, dd, di, b->ws,
+                                 b->d_err, b->bs);
+        });
+        finish_out(distance, dd, size_t(nq), on_device, st);
+        finish_out(invalid, di, size_t(nq), on_device, st);
+        LVRGB_CUDA(cudaStreamSynchronize(st));
+        batch_check(b);
     });
 }
 

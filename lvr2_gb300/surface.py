@@ -303,11 +303,11 @@ class Batch:
     kNN restricted to each scan and each scan flipped toward its own point."""
 
     def __init__(self, scans, flip_points, kn=10, ki=10, nem=3, adaptive=True, bucket=32, seed_radius=1,
-                 gap_threshold=1e-3, device=0, stream=None):
+                 gap_threshold=1e-3, device=0, stream=None, kd=5):
         L = _lib.load()
         cfg = SurfaceConfig()
         L.lvrgb_surface_config_default(ctypes.byref(cfg))
-        cfg.kn, cfg.ki, cfg.nem = int(kn), int(ki), int(nem)
+        cfg.kn, cfg.ki, cfg.kd, cfg.nem = int(kn), int(ki), int(kd), int(nem)
         cfg.adaptive = int(bool(adaptive))
         cfg.bucket, cfg.seed_radius = int(bucket), int(seed_radius)
         cfg.gap_threshold = float(gap_threshold)
@@ -354,6 +354,19 @@ class Batch:
         out = np.empty((self.n, 3), np.float32)
         check(_lib.load().lvrgb_batch_get_normals(self._h, _ptr(out), 0, self._stream))
         return out
+
+    def grid_distances(self, queries, voxel_size):
+        """Signed distance and invalid flag of every scan's (chunk's) grid
+        vertices against that scan: `queries` is a list of (m_i, 3) arrays,
+        one per scan.  Returns (distance, invalid) concatenated."""
+        sizes = [len(q) for q in queries]
+        q = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float32).reshape(-1, 3) for x in queries]))
+        off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        dist = np.empty(len(q), np.float32)
+        inv = np.empty(len(q), np.uint8)
+        check(_lib.load().lvrgb_batch_grid_distances(self._h, _ptr(q), _ptr(off), float(voxel_size), _ptr(dist),
+                                                     _ptr(inv), 0, self._stream))
+        return dist, inv
 
     def autotune(self):
         b = np.zeros(1, np.int32)

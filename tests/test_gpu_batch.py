@@ -70,3 +70,35 @@ def test_batch_argument_checks(lib):
     with pytest.raises(lvr2_gb300.LvrgbError) as e:
         lvr2_gb300.Batch(scans[:2] + [np.zeros((0, 3), np.float32)], flips[:3])
     assert e.value.status == 1
+
+
+def test_batch_grid_distances_equal_per_chunk_surfaces(lib):
+    """The chunk form of LargeScaleReconstruction's GPU block: every chunk's
+    grid vertices against that chunk's points and normals, in one call, equal
+    lvrgb_grid_distances of one surface per chunk bit for bit."""
+    import lvr2_gb300
+    scans, flips = project()
+    rng = np.random.Generator(np.random.PCG64(12))
+    vs = 0.25
+    queries = []
+    for p in scans:
+        lo, hi = p.min(0), p.max(0)
+        m = int(rng.integers(0, 3000))
+        # grid-like positions in and around the chunk, plus points near its surface
+        q = np.concatenate([rng.uniform(lo - vs, hi + vs, (m, 3)), p[rng.choice(len(p), min(len(p), 500))] + 0.01])
+        queries.append(q.astype(np.float32))
+    queries[1] = np.zeros((0, 3), np.float32)  # a chunk without grid vertices
+    ref_d, ref_i = [], []
+    for p, f, q in zip(scans, flips, queries):
+        with lvr2_gb300.Surface(p, kn=10, ki=10, kd=7, nem=3, flip_point=f) as s:
+            s.calculate_normals()
+            d, i = s.grid_distances(q, vs) if len(q) else (np.zeros(0, np.float32), np.zeros(0, np.uint8))
+        ref_d.append(d)
+        ref_i.append(i)
+    with lvr2_gb300.Batch(scans, flips, kn=10, ki=10, kd=7, nem=3) as b:
+        b.calculate_normals()
+        d, i = b.grid_distances(queries, vs)
+        d2, i2 = b.grid_distances(queries, vs)
+    assert np.array_equal(d, np.concatenate(ref_d)) and np.array_equal(i, np.concatenate(ref_i))
+    assert np.array_equal(d, d2) and np.array_equal(i, i2)
+    assert 0 < i.mean() < 1
