@@ -81,8 +81,13 @@ struct TravStats {
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
 // base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.  The
-// first K keys are stored without sifting and heapified once; until then the
-// bound is +inf.
+// heap is kHeapArity-ary: a sift-down is a chain of dependent shared-memory
+// loads, one level per step, and the children of a level are independent
+// loads, so a wider node halves the chain (k = 40: 3 levels instead of 6).
+// The first K keys are stored without sifting and heapified once; until then
+// the bound is +inf.
+constexpr int kHeapArity = 4;
+
 struct LaneHeap {
     unsigned long long* h;
     int K;
@@ -100,22 +105,29 @@ struct LaneHeap {
     __device__ __forceinline__ float tau() const { return key_d2(top); }
     __device__ __forceinline__ void sift_down(int i, int end, unsigned long long key) {
         while (true) {
-            int l = 2 * i + 1;
-            if (l >= end) break;
-            unsigned long long cl = h[l * 32];
-            int c = l;
-            if (l + 1 < end) {
-                unsigned long long cr = h[(l + 1) * 32];
-                if (cr > cl) { cl = cr; c = l + 1; }
+            const int c0 = kHeapArity * i + 1;
+            if (c0 >= end) break;
+            unsigned long long best = h[c0 * 32];
+            int bc = c0;
+#pragma unroll
+            for (int t = 1; t < kHeapArity; t++) {
+                const int c = c0 + t;
+                if (c < end) {
+                    const unsigned long long v = h[c * 32];
+                    if (v > best) {
+                        best = v;
+                        bc = c;
+                    }
+                }
             }
-            if (cl <= key) break;
-            h[i * 32] = cl;
-            i = c;
+            if (best <= key) break;
+            h[i * 32] = best;
+            i = bc;
         }
         h[i * 32] = key;
     }
     __device__ __forceinline__ void heapify() {
-        for (int i = K / 2 - 1; i >= 0; i--) sift_down(i, K, h[i * 32]);
+        for (int i = (K - 2) / kHeapArity; i >= 0; i--) sift_down(i, K, h[i * 32]);
         top = h[0];
     }
     // Replace the maximum by key (caller guarantees key < top).
