@@ -97,6 +97,78 @@ __global__ void assign_ids_kernel(const uint64_t* __restrict__ keys, const uint3
     }
 }
 
+// ---- dense form: when the lattice key space is small, a flag per key and a
+// scan replace sort + unique; the compacted keys come out sorted and a key's
+// scan position is its id.
+__global__ void mark_point_cells_kernel(const float4* __restrict__ pts, int n, Frame F, uint32_t* __restrict__ flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pts[i];
+    int ix = int(floorf(__fdiv_rn(p.x, F.vs)));
+    int iy = int(floorf(__fdiv_rn(p.y, F.vs)));
+    int iz = int(floorf(__fdiv_rn(p.z, F.vs)));
+    if (inside(F, cell_center(ix, F.vs), cell_center(iy, F.vs), cell_center(iz, F.vs)))
+        flags[lattice_key(uint32_t(ix - F.bx), uint32_t(iy - F.by), uint32_t(iz - F.bz))] = 1u;
+}
+
+__global__ void mark_extrude_kernel(const uint64_t* __restrict__ cells, int nc, Frame F, uint32_t* __restrict__ flags) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 27) return;
+    int c = t / 27, o = t % 27;
+    uint32_t x, y, z;
+    lattice_decode(cells[c], x, y, z);
+    int dx = o / 9 - 1, dy = (o / 3) % 3 - 1, dz = o % 3 - 1;
+    int ix = int(x) + F.bx + dx, iy = int(y) + F.by + dy, iz = int(z) + F.bz + dz;
+    if (inside(F, cell_center(ix, F.vs), cell_center(iy, F.vs), cell_center(iz, F.vs)))
+        flags[lattice_key(uint32_t(int(x) + dx), uint32_t(int(y) + dy), uint32_t(int(z) + dz))] = 1u;
+}
+
+__global__ void mark_corners_kernel(const uint64_t* __restrict__ cells, int nc, uint32_t* __restrict__ flags) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 8) return;
+    int c = t >> 3, k = t & 7;
+    uint32_t x, y, z;
+    lattice_decode(cells[c], x, y, z);
+    flags[lattice_key(x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2])] = 1u;
+}
+
+__global__ void corner_ids_kernel(const uint64_t* __restrict__ cells, int nc, const uint32_t* __restrict__ pos,
+                                  uint32_t* __restrict__ cell_corner) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 8) return;
+    int c = t >> 3, k = t & 7;
+    uint32_t x, y, z;
+    lattice_decode(cells[c], x, y, z);
+    cell_corner[t] = pos[lattice_key(x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2])];
+}
+
+__global__ void dense_compact_kernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, size_t N,
+                                     uint64_t* __restrict__ out) {
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    if (flags[i]) out[pos[i]] = uint64_t(i);
+}
+
+__global__ void mark_refs_kernel(const uint64_t* __restrict__ rk, size_t nref, uint32_t* __restrict__ flags) {
+    size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r < nref) flags[rk[r]] = 1u;
+}
+
+// Face vertex ids and vertex positions from the dense edge map (every
+// reference to an edge computes the same position, so the writes agree).
+__global__ void dense_refs_kernel(const uint64_t* __restrict__ rk, const float4* __restrict__ rp, size_t nref,
+                                  const uint32_t* __restrict__ pos, uint32_t* __restrict__ faces,
+                                  float* __restrict__ verts) {
+    size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nref) return;
+    const uint32_t id = pos[rk[r]];
+    faces[r] = id;
+    const float4 p = rp[r];
+    verts[3 * size_t(id)] = p.x;
+    verts[3 * size_t(id) + 1] = p.y;
+    verts[3 * size_t(id) + 2] = p.z;
+}
+
 __global__ void qp_pos_kernel(const uint64_t* __restrict__ keys, int n, Frame F, float4* __restrict__ pos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -315,6 +387,20 @@ size_t sort_unique(Workspace& ws, const std::string& tag, uint64_t*& keys, size_
     return u;
 }
 
+// The dense form pays a scan over the whole key space; it replaces sorts of
+// at least `nkeys` keys.
+bool use_dense(int bits, size_t nkeys) {
+    return bits <= 30 && (size_t(1) << bits) <= std::max<size_t>(size_t(1) << 24, 8 * nkeys);
+}
+
+// Scan of a dense flag map (N entries); returns the number of set flags and
+// leaves the positions in pos (N + 1 entries).
+size_t dense_scan(Workspace& ws, const uint32_t* flags, uint32_t* pos, size_t N, cudaStream_t s) {
+    void* stmp = ws.get<unsigned char>("grid.densescan", scan_temp_bytes(N));
+    exclusive_scan_u32(flags, pos, N, stmp, pos + N, s);
+    return size_t(uint32_t(read_u64(ws, pos + N, sizeof(uint32_t), s)));
+}
+
 struct StageTimer {
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     bool on = false;
@@ -390,30 +476,64 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     const int n = T.n;
 
     // ---- cells of the points, then extrusion (PointsetGrid.tcc:61-106) ----
-    uint64_t* ck = ws.get<uint64_t>("grid.cellsA", size_t(n));
-    point_cells_kernel<<<ceil_div(n, 256), 256, 0, s>>>(T.pts, n, F, ck);
-    LVRGB_LAUNCH_CHECK();
-    size_t nc = sort_unique(ws, "grid.cellsA", ck, size_t(n), kbits, s);
-    if (cfg.extrude && nc > 0) {
-        uint64_t* ek = ws.get<uint64_t>("grid.cellsB", nc * 27);
-        extrude_kernel<<<ceil_div(nc * 27, 256), 256, 0, s>>>(ck, int(nc), F, ek);
+    const bool dense = use_dense(kbits, size_t(n));
+    const size_t NK = dense ? size_t(1) << kbits : 0;
+    uint32_t* dflags = dense ? ws.get<uint32_t>("grid.dflags", NK) : nullptr;
+    uint32_t* dpos = dense ? ws.get<uint32_t>("grid.dpos", NK + 1) : nullptr;
+    uint64_t* ck;
+    size_t nc;
+    if (dense) {
+        LVRGB_CUDA(cudaMemsetAsync(dflags, 0, NK * sizeof(uint32_t), s));
+        mark_point_cells_kernel<<<ceil_div(n, 256), 256, 0, s>>>(T.pts, n, F, dflags);
         LVRGB_LAUNCH_CHECK();
-        nc = sort_unique(ws, "grid.cellsB", ek, nc * 27, kbits, s);
-        ck = ek;
+        nc = dense_scan(ws, dflags, dpos, NK, s);
+        ck = ws.get<uint64_t>("grid.cellsA", std::max<size_t>(nc, 1));
+        dense_compact_kernel<<<ceil_div(NK, 256), 256, 0, s>>>(dflags, dpos, NK, ck);
+        LVRGB_LAUNCH_CHECK();
+        if (cfg.extrude && nc > 0) {
+            // the point cells stay marked; their neighbours join them
+            mark_extrude_kernel<<<ceil_div(nc * 27, 256), 256, 0, s>>>(ck, int(nc), F, dflags);
+            LVRGB_LAUNCH_CHECK();
+            nc = dense_scan(ws, dflags, dpos, NK, s);
+            ck = ws.get<uint64_t>("grid.cellsB", std::max<size_t>(nc, 1));
+            dense_compact_kernel<<<ceil_div(NK, 256), 256, 0, s>>>(dflags, dpos, NK, ck);
+            LVRGB_LAUNCH_CHECK();
+        }
+    } else {
+        ck = ws.get<uint64_t>("grid.cellsA", size_t(n));
+        point_cells_kernel<<<ceil_div(n, 256), 256, 0, s>>>(T.pts, n, F, ck);
+        LVRGB_LAUNCH_CHECK();
+        nc = sort_unique(ws, "grid.cellsA", ck, size_t(n), kbits, s);
+        if (cfg.extrude && nc > 0) {
+            uint64_t* ek = ws.get<uint64_t>("grid.cellsB", nc * 27);
+            extrude_kernel<<<ceil_div(nc * 27, 256), 256, 0, s>>>(ck, int(nc), F, ek);
+            LVRGB_LAUNCH_CHECK();
+            nc = sort_unique(ws, "grid.cellsB", ek, nc * 27, kbits, s);
+            ck = ek;
+        }
     }
     R.ncells_all = (long long)nc;
     R.cell_keys = ck;
 
     // ---- grid vertices: the 8 corners of every cell, deduplicated --------
     const size_t ncorner = nc * 8;
-    uint64_t* pk = ws.get<uint64_t>("grid.cornerk", ncorner);
-    uint32_t* pv = ws.get<uint32_t>("grid.cornerv", ncorner);
-    uint64_t* pk2 = ws.get<uint64_t>("grid.cornerk2", ncorner);
-    uint32_t* pv2 = ws.get<uint32_t>("grid.cornerv2", ncorner);
     uint32_t* cell_corner = ws.get<uint32_t>("grid.cell_corner", ncorner);
     uint64_t* qk = ws.get<uint64_t>("grid.qp_keys", ncorner);
     size_t nqp = 0;
-    if (nc > 0) {
+    if (nc > 0 && dense) {
+        LVRGB_CUDA(cudaMemsetAsync(dflags, 0, NK * sizeof(uint32_t), s));
+        mark_corners_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(ck, int(nc), dflags);
+        LVRGB_LAUNCH_CHECK();
+        nqp = dense_scan(ws, dflags, dpos, NK, s);
+        dense_compact_kernel<<<ceil_div(NK, 256), 256, 0, s>>>(dflags, dpos, NK, qk);
+        LVRGB_LAUNCH_CHECK();
+        corner_ids_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(ck, int(nc), dpos, cell_corner);
+        LVRGB_LAUNCH_CHECK();
+    } else if (nc > 0) {
+        uint64_t* pk = ws.get<uint64_t>("grid.cornerk", ncorner);
+        uint32_t* pv = ws.get<uint32_t>("grid.cornerv", ncorner);
+        uint64_t* pk2 = ws.get<uint64_t>("grid.cornerk2", ncorner);
+        uint32_t* pv2 = ws.get<uint32_t>("grid.cornerv2", ncorner);
         corner_pairs_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(ck, int(nc), pk, pv);
         LVRGB_LAUNCH_CHECK();
         void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(ncorner));
@@ -484,14 +604,32 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     const size_t nref = nf * 3;
     uint64_t* rk = ws.get<uint64_t>("mc.rk", nref);
     uint32_t* rv = ws.get<uint32_t>("mc.rv", nref);
-    uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
-    uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
     float4* rp = ws.get<float4>("mc.rp", nref);
     uint32_t* faces = ws.get<uint32_t>("mc.faces", nref);
     uint64_t* vkeys = ws.get<uint64_t>("mc.vkeys", nref);
-    uint32_t* first = ws.get<uint32_t>("mc.first", nref);
     size_t nv = 0;
-    if (nf) {
+    const bool dense_edges = use_dense(kbits + 2, nref);
+    float* verts = nullptr;
+    if (nf && dense_edges) {
+        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
+        LVRGB_LAUNCH_CHECK();
+        const size_t NE = size_t(1) << (kbits + 2);
+        uint32_t* eflags = ws.get<uint32_t>("mc.dflags", NE);
+        uint32_t* epos = ws.get<uint32_t>("mc.dpos", NE + 1);
+        LVRGB_CUDA(cudaMemsetAsync(eflags, 0, NE * sizeof(uint32_t), s));
+        mark_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, nref, eflags);
+        LVRGB_LAUNCH_CHECK();
+        nv = dense_scan(ws, eflags, epos, NE, s);
+        dense_compact_kernel<<<ceil_div(NE, 256), 256, 0, s>>>(eflags, epos, NE, vkeys);
+        LVRGB_LAUNCH_CHECK();
+        verts = ws.get<float>("mc.verts", nv * 3);
+        dense_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rp, nref, epos, faces, verts);
+        LVRGB_LAUNCH_CHECK();
+    } else if (nf) {
+        uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
+        uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
+        uint32_t* first = ws.get<uint32_t>("mc.first", nref);
         mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
                                                               cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
         LVRGB_LAUNCH_CHECK();
@@ -508,12 +646,13 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
         assign_ids_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rv, flags, pos, int(nref), faces, vkeys, first);
         LVRGB_LAUNCH_CHECK();
         nv = size_t(uint32_t(read_u64(ws, pos + nref, sizeof(uint32_t), s)));
+        verts = ws.get<float>("mc.verts", nv * 3);
+        if (nv) {
+            vertex_out_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(first, int(nv), rp, verts);
+            LVRGB_LAUNCH_CHECK();
+        }
     }
-    float* verts = ws.get<float>("mc.verts", nv * 3);
-    if (nv) {
-        vertex_out_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(first, int(nv), rp, verts);
-        LVRGB_LAUNCH_CHECK();
-    }
+    if (!verts) verts = ws.get<float>("mc.verts", 1);
     timer.mark(4, s);
     R.nfaces = (long long)nf;
     R.nverts = (long long)nv;

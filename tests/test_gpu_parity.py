@@ -222,6 +222,33 @@ def test_end_to_end_mesh_against_oracle(gb, oracle_mod, dec):
     assert info.faces > 1000
 
 
+@pytest.mark.parametrize("dec", ["MC", "PMC"])
+def test_sparse_lattice_mesh_against_oracle(gb, oracle_mod, dec):
+    """A lattice too large for a flag per key (a sphere and one point 1000
+    units away: 16 bits per axis) takes the sort-and-unique form of the grid
+    and mesh build; it must agree with the oracle as the dense form does."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    v = rng.normal(size=(20_000, 3))
+    P = np.concatenate([0.3 * v / np.linalg.norm(v, axis=1, keepdims=True) + 0.5, [[1000.0, 0.5, 0.5]]])
+    P = P.astype(np.float32)
+    o = oracle_mod.OracleSurface(P)
+    with gb.Surface(P, kn=10, ki=10, kd=5, nem=3, flip_point=(0.5, 0.5, 0.5)) as s:
+        s.calculate_normals()
+        gn = s.normals()
+        info = s.reconstruct(voxelsize=0.02, decomposition=dec)
+        lat, pos, dist, inv = s.grid()
+        v, f, e = s.mesh()
+    r = o.reconstruct(gn, voxelsize=0.02, kd=5, decomposition=dec)
+    order = np.lexsort((lat[:, 2], lat[:, 1], lat[:, 0]))
+    assert np.array_equal(lat[order], r["qp_lattice"])
+    assert np.array_equal(dist[order], r["qp_dist"])
+    a = canonical_mesh(e, v, f)
+    b = canonical_mesh(r["vkeys"], r["vpos"], r["faces"])
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert info.faces > 1000
+
+
 def test_grid_distances_invalid_rule(gb):
     P = GOLD["scan/points"]
     vs = float(GOLD["scan/voxelsize"])
