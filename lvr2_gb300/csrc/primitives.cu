@@ -133,29 +133,46 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const K* __res
                                                                   int shift, uint32_t mask,
                                                                   uint32_t* __restrict__ counts,
                                                                   int ntiles) {
-    __shared__ uint32_t h[kRadix];
-    h[threadIdx.x] = 0;
+    // one sub-histogram per warp: shared atomics without cross-warp contention
+    __shared__ uint32_t h[kSortWarps][kRadix];
+#pragma unroll
+    for (int j = 0; j < kSortWarps; j++) h[j][threadIdx.x] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    size_t base = size_t(blockIdx.x) * kSortTile + size_t(w) * (kSortTile / kSortWarps);
+    const size_t base = size_t(blockIdx.x) * kSortTile + size_t(w) * (kSortTile / kSortWarps);
 #pragma unroll 4
     for (int r = 0; r < kSortItems; r++) {
-        size_t i = base + size_t(r) * 32 + lane;
-        uint32_t d = i < n ? uint32_t(keys[i] >> shift) & mask : 0xffffffffu;
-        unsigned peers = __match_any_sync(kFull, d);
-        if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&h[d], __popc(peers));
+        const size_t i = base + size_t(r) * 32 + lane;
+        if (i < n) atomicAdd(&h[w][uint32_t(keys[i] >> shift) & mask], 1u);
     }
     __syncthreads();
-    counts[size_t(threadIdx.x) * ntiles + blockIdx.x] = h[threadIdx.x];
+    uint32_t c = 0;
+#pragma unroll
+    for (int j = 0; j < kSortWarps; j++) c += h[j][threadIdx.x];
+    counts[size_t(threadIdx.x) * ntiles + blockIdx.x] = c;
 }
 
+// Dynamic shared memory of radix_scatter_kernel<K>.
+template <typename K>
+constexpr size_t scatter_smem_bytes() {
+    return size_t(kSortWarps + 2) * kRadix * sizeof(uint32_t) + size_t(kSortTile) * (sizeof(K) + sizeof(uint32_t));
+}
+
+// Stable scatter of one tile: items are ranked within the tile by digit
+// (warp rounds of __match_any_sync keep their order), placed in shared memory
+// in digit order, and then written out so that each digit's run goes to
+// consecutive global addresses (coalesced stores).
 template <typename K, bool kVals>
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
     uint32_t* __restrict__ vout, size_t n, int shift, uint32_t mask, const uint32_t* __restrict__ offsets,
     int ntiles) {
-    __shared__ uint32_t s_cnt[kSortWarps][kRadix];
-    __shared__ uint32_t s_goff[kRadix];
+    extern __shared__ __align__(16) unsigned char sm[];
+    uint32_t(*s_cnt)[kRadix] = reinterpret_cast<uint32_t(*)[kRadix]>(sm);
+    uint32_t* s_goff = reinterpret_cast<uint32_t*>(sm) + kSortWarps * kRadix;
+    uint32_t* s_toff = s_goff + kRadix;
+    K* s_key = reinterpret_cast<K*>(sm + size_t(kSortWarps + 2) * kRadix * sizeof(uint32_t));
+    uint32_t* s_val = reinterpret_cast<uint32_t*>(s_key + kSortTile);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < kSortWarps; j++) s_cnt[j][threadIdx.x] = 0;
@@ -163,7 +180,8 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     __syncthreads();
 
     const unsigned lt = (1u << lane) - 1u;
-    size_t base = size_t(blockIdx.x) * kSortTile + size_t(w) * (kSortTile / kSortWarps);
+    const size_t tile0 = size_t(blockIdx.x) * kSortTile;
+    const size_t base = tile0 + size_t(w) * (kSortTile / kSortWarps);
     K key[kSortItems];
     uint32_t val[kSortItems];
     uint32_t rank[kSortItems];
@@ -182,25 +200,49 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
         rank[r] = b + __popc(peers & lt);
     }
     __syncthreads();
-    {
-        uint32_t run = 0;
+    // per digit: offsets of the warps' runs within the digit, then the
+    // digit's offset within the tile (block-wide exclusive scan of totals)
+    uint32_t total = 0;
 #pragma unroll
-        for (int j = 0; j < kSortWarps; j++) {
-            uint32_t c = s_cnt[j][threadIdx.x];
-            s_cnt[j][threadIdx.x] = run;
-            run += c;
+    for (int j = 0; j < kSortWarps; j++) {
+        const uint32_t c = s_cnt[j][threadIdx.x];
+        s_cnt[j][threadIdx.x] = total;
+        total += c;
+    }
+    {
+        uint32_t incl = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
         }
+        __shared__ uint32_t s_warp[kSortWarps];
+        if (lane == 31) s_warp[w] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+#pragma unroll
+        for (int j = 0; j < kSortWarps; j++) before += j < w ? s_warp[j] : 0u;
+        s_toff[threadIdx.x] = before + incl - total;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortItems; r++) {
         size_t i = base + size_t(r) * 32 + lane;
         if (i < n) {
-            uint32_t d = uint32_t(key[r] >> shift) & mask;
-            uint32_t dst = s_goff[d] + s_cnt[w][d] + rank[r];
-            kout[dst] = key[r];
-            if (kVals) vout[dst] = val[r];
+            const uint32_t d = uint32_t(key[r] >> shift) & mask;
+            const uint32_t local = s_toff[d] + s_cnt[w][d] + rank[r];
+            s_key[local] = key[r];
+            if (kVals) s_val[local] = val[r];
         }
+    }
+    __syncthreads();
+    const int m = int(n - tile0 < size_t(kSortTile) ? n - tile0 : size_t(kSortTile));
+    for (int i = threadIdx.x; i < m; i += kSortThreads) {
+        const K k = s_key[i];
+        const uint32_t d = uint32_t(k >> shift) & mask;
+        const size_t dst = size_t(s_goff[d]) + size_t(i) - s_toff[d];
+        kout[dst] = k;
+        if (kVals) vout[dst] = s_val[i];
     }
 }
 
@@ -226,18 +268,35 @@ bool radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, 
     uint32_t* vin = vals;
     uint32_t* vout = vals_alt;
     bool alt = false;
+    {
+        // more than 48 KB of dynamic shared memory needs an opt-in, once per
+        // kernel and device (outside any stream capture: the first sort on a
+        // device runs eagerly)
+        static bool configured[256] = {};
+        int dev = 0;
+        LVRGB_CUDA(cudaGetDevice(&dev));
+        if (dev >= 0 && dev < 256 && !configured[dev]) {
+            constexpr int smem = int(scatter_smem_bytes<K>());
+            LVRGB_CUDA(cudaFuncSetAttribute(radix_scatter_kernel<K, true>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            LVRGB_CUDA(cudaFuncSetAttribute(radix_scatter_kernel<K, false>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            configured[dev] = true;
+        }
+    }
     for (int shift = lo_bit; shift < hi_bit; shift += kRadixBits) {
         int bits = hi_bit - shift < kRadixBits ? hi_bit - shift : kRadixBits;
         uint32_t mask = (1u << bits) - 1u;
         radix_hist_kernel<K><<<ntiles, kSortThreads, 0, s>>>(kin, n, shift, mask, counts, ntiles);
         LVRGB_LAUNCH_CHECK();
         exclusive_scan_u32(counts, counts, cnt, scan_tmp, nullptr, s);
+        constexpr size_t smem = scatter_smem_bytes<K>();
         if (vals)
-            radix_scatter_kernel<K, true><<<ntiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift,
-                                                                          mask, counts, ntiles);
+            radix_scatter_kernel<K, true><<<ntiles, kSortThreads, smem, s>>>(kin, vin, kout, vout, n, shift,
+                                                                             mask, counts, ntiles);
         else
-            radix_scatter_kernel<K, false><<<ntiles, kSortThreads, 0, s>>>(kin, nullptr, kout, nullptr, n,
-                                                                           shift, mask, counts, ntiles);
+            radix_scatter_kernel<K, false><<<ntiles, kSortThreads, smem, s>>>(kin, nullptr, kout, nullptr, n,
+                                                                              shift, mask, counts, ntiles);
         LVRGB_LAUNCH_CHECK();
         K* tk = kin; kin = kout; kout = tk;
         uint32_t* tv = vin; vin = vout; vout = tv;
