@@ -40,6 +40,17 @@ def _f32x3(a):
     return arr, 0
 
 
+def _host_out(buf, shape, dtype):
+    """A host array of `shape`: the leading rows of `buf` when given (it must
+    be C-contiguous with enough rows), else a new array."""
+    if buf is None:
+        return np.empty(shape, dtype)
+    a = np.asarray(buf)
+    if a.dtype != dtype or not a.flags["C_CONTIGUOUS"] or a.shape[1:] != tuple(shape[1:]) or a.shape[0] < shape[0]:
+        raise ValueError("output buffer must be a C-contiguous %s array with at least %s rows" % (dtype, shape[0]))
+    return a[:shape[0]]
+
+
 def _stream_ptr(stream):
     if stream is None:
         return None
@@ -140,10 +151,12 @@ class Surface:
         check(_lib.load().lvrgb_interpolate_normals(self._h, self._stream))
 
     def normals(self, out=None):
+        """Final normals (n, 3) in input order.  out: a CUDA tensor, or a
+        C-contiguous float32 host array (e.g. over pinned memory) to fill."""
         if out is not None and _is_torch_cuda(out):
             check(_lib.load().lvrgb_get_normals(self._h, _ptr(out), 1, self._stream))
             return out
-        res = np.empty((self.n, 3), np.float32)
+        res = _host_out(out, (self.n, 3), np.float32)
         check(_lib.load().lvrgb_get_normals(self._h, _ptr(res), 0, self._stream))
         return res
 
@@ -273,10 +286,14 @@ class Surface:
         check(_lib.load().lvrgb_optimize_planar_faces(self._h, int(kc), ctypes.byref(moved), self._stream))
         return int(moved.value)
 
-    def mesh(self, with_edges=True):
+    def mesh(self, with_edges=True, out_vertices=None, out_faces=None):
+        """The last mesh: vertices (V, 3), faces (F, 3) and, optionally, edge
+        keys (V, 4).  out_vertices / out_faces: host arrays (e.g. over pinned
+        memory) with at least V / F rows; their leading rows are filled and
+        returned."""
         info = self.info
-        v = np.empty((info.vertices, 3), np.float32)
-        f = np.empty((info.faces, 3), np.uint32)
+        v = _host_out(out_vertices, (info.vertices, 3), np.float32)
+        f = _host_out(out_faces, (info.faces, 3), np.uint32)
         e = np.empty((info.vertices, 4), np.int32) if with_edges else None
         check(_lib.load().lvrgb_get_mesh(self._h, _ptr(v), _ptr(f), _ptr(e), 0, self._stream))
         return v, f, e
