@@ -41,7 +41,8 @@ CPU_SAMPLE_FRACTION = 0.02
 # capture of the 2M-point case (profiles/normals_kernel_spheres_tori_2M.md,
 # profiles/sdf_kernel_spheres_tori_2M.md); the normal kernel's traffic is
 # per-point I/O (the neighbour gathers hit L2), so it scales with the points.
-NCU_DRAM_BYTES_PER_NORMAL = (47.096576e6 + 152.642304e6) / 2_000_000
+NCU_DRAM_BYTES_PER_NORMAL = (48.444928e6 + 159.263744e6) / 2e6
+NCU_DRAM_BYTES_PER_SDF_VERTEX = (150.959616e6 + 28.552192e6) / 4415248
 
 
 def parse():
@@ -451,7 +452,8 @@ def run_gpu(args):
         dom = {"kernel": "normals_kernel<3> (fused kNN + PCA + flip, all adaptive rounds)",
                "bytes": nb, "ms": normals_ms, "traffic": NCU_DRAM_BYTES_PER_NORMAL * n}
     else:
-        dom = {"kernel": "sdf_kernel (kd-nearest signed distance)", "bytes": sb, "ms": sdf_ms, "traffic": None}
+        dom = {"kernel": "sdf_kernel (kd-nearest signed distance)", "bytes": sb, "ms": sdf_ms,
+               "traffic": NCU_DRAM_BYTES_PER_SDF_VERTEX * nq}
     achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "normals/s", "n_gpus": world, "steps": args.steps,
@@ -477,7 +479,7 @@ def run_gpu(args):
                      "algorithmic_bytes": int(dom["bytes"]),
                      "traffic": int(dom["traffic"]) if dom["traffic"] else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2M-point capture, "
-                                       "scaled per point"},
+                                       "scaled per point (normals) or per grid vertex (signed distance)"},
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "e2e": e2e,
