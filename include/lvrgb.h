@@ -240,6 +240,25 @@ lvrgb_status lvrgb_get_mesh(lvrgb_surface s, float* vertices, uint32_t* faces, i
  * moved (may be NULL) receives the number of moved vertices.  Synchronous. */
 lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* moved, void* stream);
 
+/* calcVertexNormals(mesh, calcFaceNormals(mesh), surface)
+ * (include/lvr2/algorithm/NormalAlgorithms.tcc:57-152), as lvr2_reconstruct
+ * computes them for the finished mesh (src/tools/lvr2_reconstruct/Main.cpp:855-871):
+ * each vertex normal is the normalised sum of the normals of its faces
+ * (summed in ascending face order), or the normal of its nearest point when
+ * that sum is zero.  Applies to the last mesh (after lvrgb_optimize_planar_faces
+ * if that ran).  vertex_normals: V x 3. */
+lvrgb_status lvrgb_mesh_vertex_normals(lvrgb_surface s, float* vertex_normals, int32_t on_device, void* stream);
+
+/* The same for any triangle mesh against this surface's points and normals
+ * (the reference's calcVertexNormals takes any BaseMesh and PointsetSurface):
+ * vertices V x 3, faces F x 3 with indices < V (checked; an index out of range
+ * is LVRGB_ERR_INVALID_ARGUMENT).  nearest_count (optional) receives the number
+ * of vertices that took their nearest point's normal (no faces, or a zero
+ * face normal sum). */
+lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_t nv, const uint32_t* faces,
+                                  int64_t nf, float* vertex_normals, int64_t* nearest_count, int32_t on_device,
+                                  void* stream);
+
 /* The last grid, sorted by lattice key: each grid vertex's lattice index
  * (Q x 3), position (Q x 3), projected distance and invalid flag; any
  * pointer may be NULL.  Same content as HashGrid::getQueryPoints

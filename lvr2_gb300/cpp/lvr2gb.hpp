@@ -43,6 +43,9 @@ struct QueryPoint {
 struct Mesh {
     std::vector<float> vertices;  // V x 3
     std::vector<uint32_t> faces;  // F x 3 vertex indices
+    // calcVertexNormals(mesh, calcFaceNormals(mesh), surface), as handed to the
+    // finalizer (src/tools/lvr2_reconstruct/Main.cpp:855-873); V x 3
+    std::vector<float> vertexNormals;
     lvrgb_mesh_info info{};
 };
 
@@ -182,6 +185,8 @@ class Surface {
         m.vertices.resize(size_t(3 * m.info.vertices));
         m.faces.resize(size_t(3 * m.info.faces));
         check(lvrgb_get_mesh(h_, m.vertices.data(), m.faces.data(), nullptr, 0, nullptr), "getMesh");
+        m.vertexNormals.resize(m.vertices.size());
+        check(lvrgb_mesh_vertex_normals(h_, m.vertexNormals.data(), 0, nullptr), "calcVertexNormals");
         return m;
     }
 

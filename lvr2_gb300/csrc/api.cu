@@ -13,6 +13,7 @@
 #include "chunks.h"
 #include "adjoint.h"
 #include "grid.h"
+#include "meshops.h"
 #include "planar.h"
 #include "lbvh_build.h"
 #include "primitives.cuh"
@@ -682,6 +683,51 @@ lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* m
         const long long m = optimize_planar_faces(s->T, s->d_box, s->grid, kc, s->ws, s->d_err, st);
         check_kernel_error(s, st);
         if (moved) *moved = m;
+    });
+}
+
+lvrgb_status lvrgb_mesh_vertex_normals(lvrgb_surface s, float* vertex_normals, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
+        const size_t nv = size_t(s->grid.nverts);
+        require(nv == 0 || vertex_normals != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nv == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        float* d = stage_out(s->ws, "api.vnormals", vertex_normals, nv * 3, on_device);
+        mesh_vertex_normals(s->T, s->normals, s->d_box, s->grid.verts, int(nv), s->grid.faces, int(s->grid.nfaces),
+                            d, s->ws, s->d_err, st);
+        finish_out(vertex_normals, d, nv * 3, on_device, st);
+        check_kernel_error(s, st);
+    });
+}
+
+lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_t nv, const uint32_t* faces,
+                                  int64_t nf, float* vertex_normals, int64_t* nearest_count, int32_t on_device,
+                                  void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(nv >= 0 && nv < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "vertex count out of range");
+        require(nf >= 0 && 3 * nf < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "face count out of range");
+        require(nv == 0 || (vertices && vertex_normals), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        require(nf == 0 || faces, LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        require(nf == 0 || nv > 0, LVRGB_ERR_INVALID_ARGUMENT, "faces without vertices");
+        long long mz = 0;
+        if (nv > 0) {
+            DeviceScope dev(s->device);
+            cudaStream_t st = as_stream(stream);
+            const float* dv = stage_in(s->ws, "vn.in.v", vertices, size_t(nv) * 3, on_device, st);
+            const uint32_t* df = stage_in(s->ws, "vn.in.f", faces, size_t(nf) * 3, on_device, st);
+            require(max_index(df, size_t(nf) * 3, s->ws, st) < uint64_t(nv), LVRGB_ERR_INVALID_ARGUMENT,
+                    "face index out of range");
+            float* d = stage_out(s->ws, "api.vnormals", vertex_normals, size_t(nv) * 3, on_device);
+            mz = mesh_vertex_normals(s->T, s->normals, s->d_box, dv, int(nv), df, int(nf), d, s->ws, s->d_err, st);
+            finish_out(vertex_normals, d, size_t(nv) * 3, on_device, st);
+            check_kernel_error(s, st);
+        }
+        if (nearest_count) *nearest_count = mz;
     });
 }
 

@@ -286,12 +286,35 @@ class Surface:
         check(_lib.load().lvrgb_optimize_planar_faces(self._h, int(kc), ctypes.byref(moved), self._stream))
         return int(moved.value)
 
+    def _mesh_info(self):
+        """Counts of the last reconstruction (zeros before the first: the
+        library then reports the missing mesh)."""
+        return getattr(self, "info", None) or MeshInfo()
+
+    def vertex_normals(self, vertices=None, faces=None):
+        """calcVertexNormals: per-vertex normals (V, 3) of the last mesh, or of
+        the mesh given as vertices (V, 3) and faces (F, 3) against this
+        surface's points and normals.  For a given mesh also returns the number
+        of vertices that took their nearest point's normal."""
+        L = _lib.load()
+        if vertices is None:
+            out = np.empty((self._mesh_info().vertices, 3), np.float32)
+            check(L.lvrgb_mesh_vertex_normals(self._h, _ptr(out), 0, self._stream))
+            return out
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+        out = np.empty((len(v), 3), np.float32)
+        cnt = ctypes.c_int64(0)
+        check(L.lvrgb_vertex_normals(self._h, _ptr(v), len(v), _ptr(f), len(f), _ptr(out), ctypes.byref(cnt), 0,
+                                     self._stream))
+        return out, int(cnt.value)
+
     def mesh(self, with_edges=True, out_vertices=None, out_faces=None):
         """The last mesh: vertices (V, 3), faces (F, 3) and, optionally, edge
         keys (V, 4).  out_vertices / out_faces: host arrays (e.g. over pinned
         memory) with at least V / F rows; their leading rows are filled and
         returned."""
-        info = self.info
+        info = self._mesh_info()
         v = _host_out(out_vertices, (info.vertices, 3), np.float32)
         f = _host_out(out_faces, (info.faces, 3), np.uint32)
         e = np.empty((info.vertices, 4), np.int32) if with_edges else None

@@ -185,6 +185,66 @@ class OracleSurface:
                     vkeys=vkeys, vpos=vpos, faces=faces, planar_moved=moved)
 
 
+def _normalize(v):
+    """BaseVector::normalize (include/lvr2/geometry/BaseVector.hpp:130-143):
+    divide by sqrt(x*x + y*y + z*z) unless the vector is zero; float32."""
+    v = np.array(v, np.float32, copy=True)
+    x, y, z = v[:, 0], v[:, 1], v[:, 2]
+    nz = ~((x == 0) & (y == 0) & (z == 0))
+    ln = np.sqrt((x * x + y * y) + z * z)
+    v[nz] = v[nz] / ln[nz, None]
+    return v
+
+
+def face_normals(vpos, faces):
+    """calcFaceNormals / getFaceNormal (include/lvr2/algorithm/NormalAlgorithms.tcc:45-72):
+    normalize((v1 - v2) x (v1 - v3)), (0, 0, 1) when its length2 is zero."""
+    V = np.asarray(vpos, np.float32)
+    F = np.asarray(faces, np.int64)
+    if len(F) == 0:
+        return np.zeros((0, 3), np.float32)
+    v1, v2, v3 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    a, b = v1 - v2, v1 - v3
+    c = np.stack([a[:, 1] * b[:, 2] - a[:, 2] * b[:, 1],
+                  a[:, 2] * b[:, 0] - a[:, 0] * b[:, 2],
+                  a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]], 1).astype(np.float32)
+    l2 = (c[:, 0] * c[:, 0] + c[:, 1] * c[:, 1]) + c[:, 2] * c[:, 2]
+    c[l2 == 0] = np.array([0, 0, 1], np.float32)
+    return _normalize(c)
+
+
+def vertex_normals(vpos, faces, point_normals, surface):
+    """calcVertexNormals(mesh, faceNormals, surface)
+    (include/lvr2/algorithm/NormalAlgorithms.tcc:74-152): the normalised sum of
+    each vertex's face normals, summed in ascending face order; the nearest
+    point's normal (kSearch k = 1, canonical (d2, index) ties) where there
+    are no faces or the sum is zero.  surface: an OracleSurface of the points
+    whose normals are point_normals.  Returns (normals, fallback count)."""
+    V = np.asarray(vpos, np.float32)
+    F = np.asarray(faces, np.int64).reshape(-1, 3)
+    fn = face_normals(V, F)
+    acc = np.zeros((len(V), 3), np.float32)
+    ref = F.reshape(-1)
+    order = np.argsort(ref, kind="stable")  # each vertex's references, ascending face
+    vk = ref[order]
+    start = np.ones(len(vk), bool)
+    start[1:] = vk[1:] != vk[:-1]
+    run = np.cumsum(start) - 1
+    first = np.flatnonzero(start)
+    rank = np.arange(len(vk)) - first[run]
+    for t in range(int(rank.max()) + 1 if len(rank) else 0):
+        m = rank == t  # one addition per vertex per pass, in face order
+        acc[vk[m]] = acc[vk[m]] + fn[order[m] // 3]
+    l2 = (acc[:, 0] * acc[:, 0] + acc[:, 1] * acc[:, 1]) + acc[:, 2] * acc[:, 2]
+    out = _normalize(acc)
+    fb = np.flatnonzero(l2 == 0)
+    if len(fb):
+        idx, _, cnt = surface.knn(V[fb], 1)
+        ok = cnt > 0
+        out[fb[ok]] = _normalize(np.asarray(point_normals, np.float32)[idx[ok, 0].astype(np.int64)])
+    return out, len(fb)
+
+
 def mc_table():
     out = np.empty((256, 13), np.int32)
     lib().orc_mc_table(out)

@@ -73,6 +73,18 @@ int main() {
     lvr2gb::Mesh m = s.reconstruct(go);
     EXPECT(m.info.faces > 1000 && m.info.vertices > 500);
     for (uint32_t f : m.faces) EXPECT(f < uint32_t(m.info.vertices));
+    // vertex normals: unit length, along the sphere's radius
+    EXPECT(m.vertexNormals.size() == m.vertices.size());
+    size_t radial = 0;
+    for (size_t v = 0; v < size_t(m.info.vertices); v++) {
+        const float* p = &m.vertices[3 * v];
+        const float* q = &m.vertexNormals[3 * v];
+        const float rx = p[0] - 0.5f, ry = p[1] - 0.5f, rz = p[2] - 0.5f;
+        const float rl = std::sqrt(rx * rx + ry * ry + rz * rz);
+        EXPECT(std::fabs(std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) - 1.0f) < 1e-5f);
+        radial += std::fabs(q[0] * rx + q[1] * ry + q[2] * rz) > 0.9f * rl;
+    }
+    EXPECT(radial > size_t(0.95 * double(m.info.vertices)));
 
     // the CudaSurface call sequence of lvr2_reconstruct --useGPU (Main.cpp:353-379)
     std::shared_ptr<float[]> pts(new float[3 * n]);
