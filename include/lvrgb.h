@@ -249,6 +249,14 @@ lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* m
  * if that ran).  vertex_normals: V x 3. */
 lvrgb_status lvrgb_mesh_vertex_normals(lvrgb_surface s, float* vertex_normals, int32_t on_device, void* stream);
 
+/* calcColorFromPointCloud (include/lvr2/algorithm/ColorAlgorithms.tcc:43-92):
+ * each vertex of the last mesh takes the colour of its nearest point
+ * (kSearch with k = 1; ties to the lower point index).  point_colors: n x width
+ * bytes in input order (width 3 for RGB8, 4 for RGBA8; 1..16); vertex_colors:
+ * V x width. */
+lvrgb_status lvrgb_mesh_vertex_colors(lvrgb_surface s, const uint8_t* point_colors, int32_t width,
+                                      uint8_t* vertex_colors, int32_t on_device, void* stream);
+
 /* The same for any triangle mesh against this surface's points and normals
  * (the reference's calcVertexNormals takes any BaseMesh and PointsetSurface):
  * vertices V x 3, faces F x 3 with indices < V (checked; an index out of range

@@ -703,6 +703,25 @@ lvrgb_status lvrgb_mesh_vertex_normals(lvrgb_surface s, float* vertex_normals, i
     });
 }
 
+lvrgb_status lvrgb_mesh_vertex_colors(lvrgb_surface s, const uint8_t* point_colors, int32_t width,
+                                      uint8_t* vertex_colors, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
+        require(width >= 1 && width <= 16, LVRGB_ERR_INVALID_ARGUMENT, "colour width must be 1..16 bytes");
+        const size_t nv = size_t(s->grid.nverts);
+        require(nv == 0 || (point_colors && vertex_colors), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nv == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const uint8_t* dc = stage_in(s->ws, "vc.in", point_colors, size_t(s->T.n) * width, on_device, st);
+        uint8_t* d = stage_out(s->ws, "api.vcolors", vertex_colors, nv * width, on_device);
+        mesh_vertex_colors(s->T, s->d_box, s->grid.verts, int(nv), dc, width, d, s->ws, s->d_err, st);
+        finish_out(vertex_colors, d, nv * width, on_device, st);
+        check_kernel_error(s, st);
+    });
+}
+
 lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_t nv, const uint32_t* faces,
                                   int64_t nf, float* vertex_normals, int64_t* nearest_count, int32_t on_device,
                                   void* stream) {

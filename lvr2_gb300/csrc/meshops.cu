@@ -112,6 +112,15 @@ __global__ void nearest_normal_kernel(const uint32_t* __restrict__ list, const u
     out[3 * v + 2] = z;
 }
 
+__global__ void nearest_color_kernel(const uint32_t* __restrict__ idx, const int32_t* __restrict__ cnt, int nv,
+                                     const uint8_t* __restrict__ colors, int width, uint8_t* __restrict__ out) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const bool ok = cnt[v] > 0;
+    const size_t src = ok ? size_t(idx[v]) * width : 0;
+    for (int c = 0; c < width; c++) out[size_t(v) * width + c] = ok ? colors[src + c] : uint8_t(0);
+}
+
 __global__ void max_index_kernel(const uint32_t* __restrict__ a, size_t n, uint32_t* __restrict__ out) {
     uint32_t m = 0;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
@@ -121,6 +130,19 @@ __global__ void max_index_kernel(const uint32_t* __restrict__ a, size_t n, uint3
 }
 
 }  // namespace
+
+void mesh_vertex_colors(const Lbvh& T, const float* d_box, const float* verts, int nv, const uint8_t* colors,
+                        int width, uint8_t* out, Workspace& ws, int* d_err, cudaStream_t s) {
+    if (nv == 0) return;
+    float4* qs = ws.get<float4>("vc.qs", size_t(nv));
+    sort_queries(verts, nv, d_box, qs, ws, s);
+    uint32_t* idx = ws.get<uint32_t>("vc.idx", size_t(nv));
+    float* dist = ws.get<float>("vc.dist", size_t(nv));
+    int32_t* cnt = ws.get<int32_t>("vc.cnt", size_t(nv));
+    knn_rows(T, qs, nv, 1, idx, dist, cnt, ws, d_err, s);
+    nearest_color_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(idx, cnt, nv, colors, width, out);
+    LVRGB_LAUNCH_CHECK();
+}
 
 uint32_t max_index(const uint32_t* a, size_t n, Workspace& ws, cudaStream_t s) {
     if (n == 0) return 0;

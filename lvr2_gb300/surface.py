@@ -309,6 +309,18 @@ class Surface:
                                      self._stream))
         return out, int(cnt.value)
 
+    def vertex_colors(self, point_colors):
+        """calcColorFromPointCloud: each vertex of the last mesh takes the
+        colour of its nearest point.  point_colors: (n, width) uint8 in input
+        order; returns (V, width) uint8."""
+        c = np.ascontiguousarray(point_colors, np.uint8)
+        c = c.reshape(len(c), -1)
+        if len(c) != self.n:
+            raise ValueError("point_colors has %d rows, the surface %d points" % (len(c), self.n))
+        out = np.empty((self._mesh_info().vertices, c.shape[1]), np.uint8)
+        check(_lib.load().lvrgb_mesh_vertex_colors(self._h, _ptr(c), c.shape[1], _ptr(out), 0, self._stream))
+        return out
+
     def mesh(self, with_edges=True, out_vertices=None, out_faces=None):
         """The last mesh: vertices (V, 3), faces (F, 3) and, optionally, edge
         keys (V, 4).  out_vertices / out_faces: host arrays (e.g. over pinned

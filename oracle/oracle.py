@@ -245,6 +245,19 @@ def vertex_normals(vpos, faces, point_normals, surface):
     return out, len(fb)
 
 
+def vertex_colors(vpos, point_colors, surface):
+    """calcColorFromPointCloud (include/lvr2/algorithm/ColorAlgorithms.tcc:43-92):
+    the colour of each vertex's nearest point (k = 1; r / 1 casts back to the
+    same byte)."""
+    V = np.asarray(vpos, np.float32)
+    c = np.asarray(point_colors, np.uint8)
+    c = c.reshape(len(c), -1)
+    idx, _, cnt = surface.knn(V, 1)
+    out = c[idx[:, 0].astype(np.int64)].copy()
+    out[cnt <= 0] = 0
+    return out
+
+
 def mc_table():
     out = np.empty((256, 13), np.int32)
     lib().orc_mc_table(out)

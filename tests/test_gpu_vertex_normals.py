@@ -68,6 +68,24 @@ def test_fallbacks(gb, oracle_mod, scene):
         assert vn.shape == (0, 3) and fb == 0
 
 
+@pytest.mark.parametrize("width", [3, 4, 1])
+def test_vertex_colors_match_oracle(gb, oracle_mod, scene, width):
+    """calcColorFromPointCloud: the nearest point's colour per vertex."""
+    P, flip = scene
+    rng = np.random.Generator(np.random.PCG64(width))
+    C = rng.integers(0, 256, size=(len(P), width), dtype=np.uint8)
+    with gb.Surface(P, kn=10, ki=10, kd=10, nem=3, flip_point=flip) as s:
+        s.calculate_normals()
+        s.reconstruct(voxelsize=0.02, decomposition="PMC")
+        s.optimize_planar_faces(5)
+        v, _, _ = s.mesh(with_edges=False)
+        vc = s.vertex_colors(C)
+        with pytest.raises(ValueError):
+            s.vertex_colors(C[:-1])
+    ref = oracle_mod.vertex_colors(v, C, oracle_mod.OracleSurface(P))
+    assert vc.shape == (len(v), width) and np.array_equal(vc, ref)
+
+
 def test_errors(gb, scene):
     P, _ = scene
     with gb.Surface(P[:5000], kn=10, ki=10, kd=10, nem=3) as s:
