@@ -181,14 +181,29 @@ void read_ply(const std::string& path, std::vector<float>& xyz, std::vector<floa
     }
 }
 
+// Vertex element x, y, z, nx, ny, nz (the vertex normals lvr2_reconstruct hands
+// the finalizer; PLYIO.cpp:226-240 writes them after the position), then the
+// faces as uchar-int lists.
 void write_mesh_ply(const std::string& path, const lvr2gb::Mesh& m) {
     std::ofstream out(path, std::ios::binary);
     if (!out) throw std::runtime_error("cannot write " + path);
     const size_t nv = m.vertices.size() / 3, nf = m.faces.size() / 3;
+    const bool normals = m.vertexNormals.size() == m.vertices.size() && nv > 0;
     out << "ply\nformat binary_little_endian 1.0\ncomment lvr2gb_reconstruct\n"
-        << "element vertex " << nv << "\nproperty float x\nproperty float y\nproperty float z\n"
-        << "element face " << nf << "\nproperty list uchar int vertex_indices\nend_header\n";
-    out.write(reinterpret_cast<const char*>(m.vertices.data()), std::streamsize(m.vertices.size() * sizeof(float)));
+        << "element vertex " << nv << "\nproperty float x\nproperty float y\nproperty float z\n";
+    if (normals) out << "property float nx\nproperty float ny\nproperty float nz\n";
+    out << "element face " << nf << "\nproperty list uchar int vertex_indices\nend_header\n";
+    if (normals) {
+        std::vector<float> row(6 * nv);
+        for (size_t v = 0; v < nv; v++)
+            for (int c = 0; c < 3; c++) {
+                row[6 * v + c] = m.vertices[3 * v + c];
+                row[6 * v + 3 + c] = m.vertexNormals[3 * v + c];
+            }
+        out.write(reinterpret_cast<const char*>(row.data()), std::streamsize(row.size() * sizeof(float)));
+    } else {
+        out.write(reinterpret_cast<const char*>(m.vertices.data()), std::streamsize(m.vertices.size() * sizeof(float)));
+    }
     for (size_t f = 0; f < nf; f++) {
         const unsigned char three = 3;
         const int32_t idx[3] = {int32_t(m.faces[3 * f]), int32_t(m.faces[3 * f + 1]), int32_t(m.faces[3 * f + 2])};

@@ -37,6 +37,21 @@ def read_ply_counts(path):
     return nv, nf
 
 
+def read_ply_mesh(path):
+    """Vertices (x y z [nx ny nz] floats) and faces (uchar 3 + int32 x 3) of
+    a binary little-endian PLY written by lvr2gb_reconstruct."""
+    data = Path(path).read_bytes()
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    head = data[:end].decode()
+    nv, nf = read_ply_counts(path)
+    width = 6 if "property float nx" in head else 3
+    v = np.frombuffer(data, np.float32, nv * width, end).reshape(nv, width)
+    rec = np.dtype([("n", "u1"), ("i", "<i4", 3)])
+    f = np.frombuffer(data, rec, nf, end + v.nbytes)
+    assert np.all(f["n"] == 3)
+    return v[:, :3], (v[:, 3:] if width == 6 else None), f["i"]
+
+
 @pytest.mark.gpu
 def test_cpp_adapters_on_gpu(built):
     _, test_bin = built
@@ -66,5 +81,10 @@ def test_cli_matches_python_path(built, tmp_path):
     with lvr2_gb300.Surface(pts_read, kn=10, ki=10, kd=5, nem=0, flip_point=(0, 0, 0)) as s:
         s.calculate_normals()
         info = s.reconstruct(voxelsize=10.0, decomposition="PMC")
+        s.optimize_planar_faces(5)
+        v, f, _ = s.mesh(with_edges=False)
+        vn = s.vertex_normals()
     assert (nv, nf) == (info.vertices, info.faces)
+    pv, pn, pf = read_ply_mesh(out)
+    assert np.array_equal(pv, v) and np.array_equal(pf, f.astype(np.int32)) and np.array_equal(pn, vn)
     assert (tmp_path / "pointnormals.ply").exists()
