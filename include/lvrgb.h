@@ -57,7 +57,11 @@ typedef struct lvrgb_surface_config {
     int32_t kn;            /* normal estimation neighbourhood (first search uses 2*kn) */
     int32_t ki;            /* interpolation neighbourhood, 0 = no interpolation */
     int32_t kd;            /* signed-distance neighbourhood */
-    int32_t nem;           /* plane fit: 0 least squares (lvr2 default), 2 iterative, 3 PCA */
+    int32_t nem;           /* plane fit: 0 least squares (lvr2 default), 2 iterative, 3 PCA,
+                              4 the LBVH comparator's FP64 fit (LBVHIndex::knn_normals,
+                              src/liblvr2/reconstruction/cuda/lbvh/knn_normals_kernel.cu:54-206;
+                              CudaKSearchSurface, --pcm LBVH_CUDA): one search with k = kn <= 96,
+                              no adaptive rounds, slot 0 (the query) left out */
     int32_t adaptive;      /* 1: k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed */
     int32_t flip_set;      /* 0: flip point = bounding-box centroid (AdaptiveKSearchSurface::init) */
     float flip[3];         /* flip point when flip_set != 0 */
@@ -95,7 +99,8 @@ lvrgb_status lvrgb_surface_set_k(lvrgb_surface s, int32_t kn, int32_t ki, int32_
 lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, float z);
 
 /* Plane-fit method: AdaptiveKSearchSurface calcMethod / CudaSurface::setMethod
- * (CudaSurface.hpp:144).  nem 1 (RANSAC) returns LVRGB_ERR_UNSUPPORTED. */
+ * (CudaSurface.hpp:144).  nem 1 (RANSAC) returns LVRGB_ERR_UNSUPPORTED; nem 4 is
+ * the fit of CudaKSearchSurface (see lvrgb_surface_config). */
 lvrgb_status lvrgb_surface_set_method(lvrgb_surface s, int32_t nem);
 
 /* PointsetSurface::getBoundingBox (PointsetSurface.hpp:106): out9 = min xyz,
@@ -273,6 +278,16 @@ lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_
  * (include/lvr2/reconstruction/HashGrid.hpp:179). */
 lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, float* distance,
                             uint8_t* invalid, int32_t on_device, void* stream);
+
+/* HashGrid::toPointBuffer (include/lvr2/reconstruction/HashGrid.tcc:196-233),
+ * the per-chunk grid the large-scale reconstruction stores and merges: for
+ * each cell kept after culling (lattice-key order, in place of the hash map's
+ * bucket order) its centre (centers, C x 3) and the projected distances at
+ * its 8 corners in FastBox corner order (tsdf_values, C x 8, the
+ * "tsdf_values" channel).  C = lvrgb_mesh_info.cells_valid.  Either array
+ * may be NULL. */
+lvrgb_status lvrgb_get_cell_tsdf(lvrgb_surface s, float* centers, float* tsdf_values, int32_t on_device,
+                                 void* stream);
 
 /* Cells of the last grid as lattice indices (x, y, z of the cell's lowest
  * corner): all cells before culling and the valid cells (either may be NULL).

@@ -197,6 +197,29 @@ class Surface {
     size_t n_ = 0;
 };
 
+// CudaKSearchSurface (include/lvr2/reconstruction/CudaKSearchSurface.hpp,
+// .tcc:12-65; --pcm LBVH_CUDA): normals by the LBVH comparator's fit (nem 4)
+// with k = kn (default 50), flipped toward its fixed point (1e6, 1e6, 1e6),
+// without interpolation; distance() is not provided, as in lvr2.
+class CudaKSearchSurface {
+  public:
+    CudaKSearchSurface(const float* xyz, size_t n, size_t k = 50, int device = 0)
+        : s_(xyz, n, int(k), 0, 5, 4, device) {
+        s_.setFlipPoint(Vec3{1e6f, 1e6f, 1e6f});
+    }
+    void setKn(int k) { s_.setKn(k); }
+    void calculateSurfaceNormals() { s_.calculateSurfaceNormals(); }
+    // The "normals" channel (n x 3, input order).
+    std::vector<float> normals() const { return s_.normals(); }
+    std::pair<float, float> distance(const Vec3&) const {
+        throw std::runtime_error("Do not use this function!");
+    }
+    lvrgb_surface handle() const { return s_.handle(); }
+
+  private:
+    Surface s_;
+};
+
 // The GpuSurface API of lvr2 (CudaSurface.hpp:70-158) over the same handle.
 class CudaSurface {
   public:

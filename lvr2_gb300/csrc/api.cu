@@ -216,7 +216,15 @@ NormalsConfig normals_config(const lvrgb_surface_s* s) {
 
 void check_nem(int nem) {
     require(nem != 1, LVRGB_ERR_UNSUPPORTED, "nem 1 (RANSAC plane fit) is not supported");
-    require(nem == 0 || nem == 2 || nem == 3, LVRGB_ERR_INVALID_ARGUMENT, "nem must be 0, 2 or 3");
+    require(nem == 0 || nem == 2 || nem == 3 || nem == 4, LVRGB_ERR_INVALID_ARGUMENT, "nem must be 0, 2, 3 or 4");
+}
+
+// k of the first normal search: 2 kn (adaptive k doubles before every
+// search), kn for nem 4 (LBVHIndex::knn_normals searches once with kn).
+int first_search_k(int kn, int nem) { return nem == 4 ? kn : 2 * kn; }
+
+void check_lbvh_k(int kn, int nem) {
+    require(nem != 4 || kn <= kSmemHeapMax, LVRGB_ERR_INVALID_ARGUMENT, "nem 4 needs kn <= 96");
 }
 
 // Sorts host/device query positions into Morton order on the device.
@@ -375,10 +383,11 @@ lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
         DeviceScope dev(s->device);
         cudaStream_t st = as_stream(stream);
         LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
+        check_lbvh_k(s->cfg.kn, s->cfg.nem);
         NormalsConfig c = normals_config(s);
         // The interpolation's kNN(ki) is the first ki of the estimation's
-        // kNN(k >= 2kn): keep those lists instead of searching again.
-        const bool lists = s->cfg.ki > 0 && s->cfg.ki <= 2 * s->cfg.kn;
+        // kNN (k >= 2kn, or kn for nem 4): keep those lists instead of searching again.
+        const bool lists = s->cfg.ki > 0 && s->cfg.ki <= first_search_k(s->cfg.kn, s->cfg.nem);
         uint32_t* nbr = lists ? s->ws.get<uint32_t>("api.nbr", size_t(s->T.n) * size_t(s->cfg.ki)) : nullptr;
         record(s, 2, st);
         compute_normals(s->T, c, s->raw_normals, s->kused, s->ws, s->d_err, s->d_stats, st, nbr, s->cfg.ki);
@@ -830,6 +839,24 @@ lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, 
     });
 }
 
+lvrgb_status lvrgb_get_cell_tsdf(lvrgb_surface s, float* centers, float* tsdf_values, int32_t on_device,
+                                 void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no grid: call lvrgb_reconstruct");
+        const size_t n = size_t(s->grid.ncells_valid);
+        if (n == 0 || (!centers && !tsdf_values)) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        float* dc = centers ? stage_out(s->ws, "api.cc", centers, n * 3, on_device) : nullptr;
+        float* dt = tsdf_values ? stage_out(s->ws, "api.tsdf", tsdf_values, n * 8, on_device) : nullptr;
+        cell_tsdf(s->grid, dc, dt, st);
+        if (centers) finish_out(centers, dc, n * 3, on_device, st);
+        if (tsdf_values) finish_out(tsdf_values, dt, n * 8, on_device, st);
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 lvrgb_status lvrgb_get_cells(lvrgb_surface s, int32_t* cells_all, int32_t* cells_valid, int32_t on_device,
                              void* stream) {
     return guarded([&] {
@@ -973,9 +1000,11 @@ lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xy
         require(cfg && scan_offsets && flip_points, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
         require(nscans >= 1 && nscans <= 65535, LVRGB_ERR_INVALID_ARGUMENT, "nscans must be in 1..65535");
         require(cfg->kn > 0 && cfg->ki >= 0, LVRGB_ERR_INVALID_ARGUMENT, "kn must be > 0, ki >= 0");
-        require(cfg->ki <= 2 * cfg->kn, LVRGB_ERR_UNSUPPORTED,
-                "scan projects interpolate from the estimation's neighbour lists: ki must be <= 2 * kn");
         check_nem(cfg->nem);
+        check_lbvh_k(cfg->kn, cfg->nem);
+        require(cfg->ki <= first_search_k(cfg->kn, cfg->nem), LVRGB_ERR_UNSUPPORTED,
+                "scan projects interpolate from the estimation's neighbour lists: ki must be <= 2 * kn "
+                "(<= kn for nem 4)");
         require(cfg->bucket >= 0 && cfg->bucket <= 32, LVRGB_ERR_INVALID_ARGUMENT, "bucket must be in 0..32");
         require(scan_offsets[0] == 0, LVRGB_ERR_INVALID_ARGUMENT, "scan_offsets[0] must be 0");
         for (int k = 0; k < nscans; k++)

@@ -663,4 +663,34 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     timer.finish(timings, s);
 }
 
+namespace {
+__global__ void cell_tsdf_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ valid, int n,
+                                 int bx, int by, int bz, float vs, const uint32_t* __restrict__ corner,
+                                 const float* __restrict__ dist, float* __restrict__ centers,
+                                 float* __restrict__ tsdf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t c = valid[i];
+    uint32_t x, y, z;
+    lattice_decode(keys[c], x, y, z);
+    if (centers) {
+        centers[3 * size_t(i)] = cell_center(int(x) + bx, vs);
+        centers[3 * size_t(i) + 1] = cell_center(int(y) + by, vs);
+        centers[3 * size_t(i) + 2] = cell_center(int(z) + bz, vs);
+    }
+    if (tsdf) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) tsdf[8 * size_t(i) + k] = dist[corner[8 * size_t(c) + k]];
+    }
+}
+}  // namespace
+
+void cell_tsdf(const GridResult& R, float* centers, float* tsdf, cudaStream_t s) {
+    const int n = int(R.ncells_valid);
+    if (n == 0) return;
+    cell_tsdf_kernel<<<ceil_div(n, 256), 256, 0, s>>>(R.cell_keys, R.valid_cells, n, R.base[0], R.base[1],
+                                                      R.base[2], R.vs, R.cell_corner, R.qp_dist, centers, tsdf);
+    LVRGB_LAUNCH_CHECK();
+}
+
 }  // namespace lvrgb

@@ -51,6 +51,11 @@ struct GridTimings {
 void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], const GridConfig& cfg,
                       Workspace& ws, GridResult& R, int* d_err, cudaStream_t s, GridTimings* timings = nullptr);
 
+// HashGrid::toPointBuffer (HashGrid.tcc:196-233) of the culled grid: per valid
+// cell (lattice-key order) its centre (centers, 3 floats) and the projected
+// distances at its 8 corners in FastBox corner order (tsdf, 8 floats).
+void cell_tsdf(const GridResult& R, float* centers, float* tsdf, cudaStream_t s);
+
 // Batched AdaptiveKSearchSurface::distance at nq positions (float4 xyz, w =
 // row index bits), rows written to dist/eucl; invalid (optional) uses the
 // 1.75 * voxelsize rule of PointsetGrid::calcDistanceValues.

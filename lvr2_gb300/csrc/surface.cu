@@ -182,7 +182,9 @@ __device__ __forceinline__ void neighbour_pass(const Lbvh& T, const LaneHeap& he
         const float4 p = neighbour_point(T, heap.at(s));
         P.lo[0] = fminf(p.x, P.lo[0]); P.lo[1] = fminf(p.y, P.lo[1]); P.lo[2] = fminf(p.z, P.lo[2]);
         P.hi[0] = fmaxf(p.x, P.hi[0]); P.hi[1] = fmaxf(p.y, P.hi[1]); P.hi[2] = fmaxf(p.z, P.hi[2]);
-        if (kNem == 2) {
+        if (kNem == 4) {
+            // the box only (nem 4 sums in FP64 in lbvh_knn_normal)
+        } else if (kNem == 2) {
             const float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
             P.r[0] = __fadd_rn(P.r[0], __fmul_rn(rx, rx));
             P.r[1] = __fadd_rn(P.r[1], __fmul_rn(rx, ry));
@@ -324,6 +326,74 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
     solve_plane<kNem>(A.gap_thr, q, mean, S, P.r, n, fp64);
 }
 
+// nem 4: the plane fit of lvr2's LBVH comparator (LBVHIndex::knn_normals,
+// src/liblvr2/reconstruction/cuda/lbvh/knn_normals_kernel.cu:54-206), used by
+// CudaKSearchSurface (--pcm LBVH_CUDA): in FP64, the centroid and covariance
+// of neighbours 1..n-1 (slot 0 is the query itself), each term divided by
+// n - 1 before it is added; the det^2-weighted sum of the three cofactor axes
+// (sign-aligned with the running sum), normalised; flipped toward the flip
+// point; a NaN or infinite flip product, or fewer than 3 neighbours, gives the
+// zero normal.  Every operation is rounded on its own (no contraction), in
+// the reference's order.  Neighbours in ascending (d2, index) order.
+__device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, float fx,
+                                                float fy, float fz, float n[3]) {
+    n[0] = n[1] = n[2] = 0.0f;
+    if (cnt < 3) return;
+    const double nf = __dsub_rn(double(cnt), 1.0);
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int s = 1; s < cnt; s++) {
+        const float4 p = neighbour_point(T, heap.at(s));
+        sx = __dadd_rn(sx, __ddiv_rn(double(p.x), nf));
+        sy = __dadd_rn(sy, __ddiv_rn(double(p.y), nf));
+        sz = __dadd_rn(sz, __ddiv_rn(double(p.z), nf));
+    }
+    double xx = 0.0, xy = 0.0, xz = 0.0, yy = 0.0, yz = 0.0, zz = 0.0;
+    for (int s = 1; s < cnt; s++) {
+        const float4 p = neighbour_point(T, heap.at(s));
+        const double rx = __dsub_rn(double(p.x), sx), ry = __dsub_rn(double(p.y), sy), rz = __dsub_rn(double(p.z), sz);
+        xx = __dadd_rn(xx, __ddiv_rn(__dmul_rn(rx, rx), nf));
+        xy = __dadd_rn(xy, __ddiv_rn(__dmul_rn(rx, ry), nf));
+        xz = __dadd_rn(xz, __ddiv_rn(__dmul_rn(rx, rz), nf));
+        yy = __dadd_rn(yy, __ddiv_rn(__dmul_rn(ry, ry), nf));
+        yz = __dadd_rn(yz, __ddiv_rn(__dmul_rn(ry, rz), nf));
+        zz = __dadd_rn(zz, __ddiv_rn(__dmul_rn(rz, rz), nf));
+    }
+    double wx = 0.0, wy = 0.0, wz = 0.0;
+    auto add_axis = [&](double ax, double ay, double az, double det) {
+        double w = __dmul_rn(det, det);
+        const double dot = __dadd_rn(__dadd_rn(__dmul_rn(wx, ax), __dmul_rn(wy, ay)), __dmul_rn(wz, az));
+        if (dot < 0.0) w = -w;
+        wx = __dadd_rn(wx, __dmul_rn(ax, w));
+        wy = __dadd_rn(wy, __dmul_rn(ay, w));
+        wz = __dadd_rn(wz, __dmul_rn(az, w));
+    };
+    const double det_x = __dsub_rn(__dmul_rn(yy, zz), __dmul_rn(yz, yz));
+    add_axis(det_x, __dsub_rn(__dmul_rn(xz, yz), __dmul_rn(xy, zz)), __dsub_rn(__dmul_rn(xy, yz), __dmul_rn(xz, yy)),
+             det_x);
+    const double det_y = __dsub_rn(__dmul_rn(xx, zz), __dmul_rn(xz, xz));
+    add_axis(__dsub_rn(__dmul_rn(xz, yz), __dmul_rn(xy, zz)), det_y, __dsub_rn(__dmul_rn(xy, xz), __dmul_rn(yz, xx)),
+             det_y);
+    const double det_z = __dsub_rn(__dmul_rn(xx, yy), __dmul_rn(xy, xy));
+    add_axis(__dsub_rn(__dmul_rn(xy, yz), __dmul_rn(xz, yy)), __dsub_rn(__dmul_rn(xy, xz), __dmul_rn(yz, xx)), det_z,
+             det_z);
+    const double mag = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(wx, wx), __dmul_rn(wy, wy)), __dmul_rn(wz, wz)));
+    wx = __ddiv_rn(wx, mag);
+    wy = __ddiv_rn(wy, mag);
+    wz = __ddiv_rn(wz, mag);
+    const double dx = __dsub_rn(double(fx), double(q.x)), dy = __dsub_rn(double(fy), double(q.y)),
+                 dz = __dsub_rn(double(fz), double(q.z));
+    const double scalar = __dadd_rn(__dadd_rn(__dmul_rn(dx, wx), __dmul_rn(dy, wy)), __dmul_rn(dz, wz));
+    if (!(scalar <= 0.0 || scalar >= 0.0) || isinf(scalar)) {
+        wx = 0.0; wy = 0.0; wz = 0.0;
+    }
+    if (scalar < 0.0) {
+        wx = -wx; wy = -wy; wz = -wz;
+    }
+    n[0] = float(wx);
+    n[1] = float(wy);
+    n[2] = float(wz);
+}
+
 template <int kNem>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -385,14 +455,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
             }
             if (fit) {
                 float n[3];
-                bool fp64;
-                fit_plane<kNem>(A, heap, cnt, q, P, n, fp64);
-                // Flip toward the flip point; Normal::operator-() re-normalises.
-                const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
-                const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
-                if (dot < 0.0f) {
-                    n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
-                    normalize_ieee(n[0], n[1], n[2]);
+                bool fp64 = false;
+                if (kNem == 4) {
+                    lbvh_knn_normal(A.T, heap, cnt, q, fx, fy, fz, n);
+                } else {
+                    fit_plane<kNem>(A, heap, cnt, q, P, n, fp64);
+                    // Flip toward the flip point; Normal::operator-() re-normalises.
+                    const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
+                    const float dot =
+                        __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
+                    if (dot < 0.0f) {
+                        n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
+                        normalize_ieee(n[0], n[1], n[2]);
+                    }
                 }
                 A.normals[pos] = make_float4(n[0], n[1], n[2], 0.0f);
                 if (A.kused) A.kused[pos] = A.K;
@@ -1042,6 +1117,16 @@ void compact_retry(const uint8_t* flags, const uint32_t* list, int nq, const uin
     LVRGB_LAUNCH_CHECK();
 }
 
+// nem 4 runs with the per-lane heaps only (k <= kSmemHeapMax, checked by the API).
+void launch_normals_lbvh(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
+    if (A.K > kSmemHeapMax) throw std::invalid_argument("nem 4 needs k <= 96");
+    const HeapPlan P = plan_heap(grid_nq, A.K, ws);
+    A.gheap = P.gheap;
+    set_smem(normals_kernel<4>, P.smem);
+    normals_kernel<4><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
 void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) {
     if (g_num_sms == 0) {
         int dev = 0;
@@ -1051,6 +1136,7 @@ void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) 
     switch (A.nem) {
         case 2: launch_normals_nem<2>(A, grid_nq, ws, s); break;
         case 3: launch_normals_nem<3>(A, grid_nq, ws, s); break;
+        case 4: launch_normals_lbvh(A, grid_nq, ws, s); break;
         default: launch_normals_nem<0>(A, grid_nq, ws, s); break;
     }
 }
@@ -1069,10 +1155,11 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
     int nq = n;
     const uint32_t* list = nullptr;
     size_t k = size_t(cfg.kn);
+    const bool lbvh = cfg.nem == 4;  // LBVHIndex::knn_normals: one search with k = kn
     for (int round = 1; round <= 5 && nq > 0; round++) {
-        k *= 2;  // the reference doubles k before every search
+        if (!lbvh) k *= 2;  // the reference doubles k before every search
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
-        const int last = (!cfg.adaptive || round == 5) ? 1 : 0;
+        const int last = (!cfg.adaptive || lbvh || round == 5) ? 1 : 0;
         uint32_t* retry = lists[round & 1];
         NormalsArgs A;
         A.T = T;
@@ -1122,10 +1209,11 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
     uint8_t* flags = ws.get<uint8_t>("segn.flags", size_t(n));
     float* kth_d2 = cfg.adaptive ? ws.get<float>("segn.kth", size_t(n)) : nullptr;
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s));
-    const int rounds = cfg.adaptive ? 5 : 1;
+    const bool lbvh = cfg.nem == 4;  // LBVHIndex::knn_normals: one search with k = kn
+    const int rounds = (cfg.adaptive && !lbvh) ? 5 : 1;
     size_t k = size_t(cfg.kn);
     for (int round = 1; round <= rounds; round++) {
-        k *= 2;  // the reference doubles k before every search
+        if (!lbvh) k *= 2;  // the reference doubles k before every search
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
         NormalsArgs A;
         A.T = T;

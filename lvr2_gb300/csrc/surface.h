@@ -7,7 +7,7 @@ namespace lvrgb {
 
 struct NormalsConfig {
     int kn = 10;          // AdaptiveKSearchSurface kn
-    int nem = 0;          // 0 LSQ plane, 2 iterative, 3 PCA (IPCA exact)
+    int nem = 0;          // 0 LSQ plane, 2 iterative, 3 PCA (IPCA exact), 4 LBVH comparator (FP64, k = kn)
     int adaptive = 1;     // k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed
     float flip[3] = {0, 0, 0};
     float gap_threshold = 1e-3f;  // relative eigengap below which the eigensolve runs in FP64

@@ -309,6 +309,15 @@ class Surface:
                                      self._stream))
         return out, int(cnt.value)
 
+    def cell_tsdf(self):
+        """HashGrid::toPointBuffer of the culled grid: cell centres (C, 3) and
+        the distances at their 8 corners (C, 8), cells in lattice-key order."""
+        n = self._mesh_info().cells_valid
+        c = np.empty((n, 3), np.float32)
+        t = np.empty((n, 8), np.float32)
+        check(_lib.load().lvrgb_get_cell_tsdf(self._h, _ptr(c), _ptr(t), 0, self._stream))
+        return c, t
+
     def vertex_colors(self, point_colors):
         """calcColorFromPointCloud: each vertex of the last mesh takes the
         colour of its nearest point.  point_colors: (n, width) uint8 in input

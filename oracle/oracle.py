@@ -185,6 +185,70 @@ class OracleSurface:
                     vkeys=vkeys, vpos=vpos, faces=faces, planar_moved=moved)
 
 
+def lbvh_knn_normals(surface, kn, flip=(1e6, 1e6, 1e6)):
+    """The plane fit of lvr2's LBVH comparator, LBVHIndex::knn_normals
+    (src/liblvr2/reconstruction/cuda/lbvh/knn_normals_kernel.cu:54-206), over
+    the canonical kNN(kn) of every point (ascending (d2, index); slot 0, the
+    query itself, is left out): FP64 centroid and covariance with each term
+    divided by n - 1 before it is added, the det^2-weighted, sign-aligned sum
+    of the three cofactor axes, normalised, flipped toward `flip`; fewer than 3
+    neighbours or a NaN / infinite flip product give the zero normal.  numpy
+    float64 rounds every operation on its own, in the kernel's order."""
+    P = surface.points.astype(np.float64)
+    idx, _, cnt = surface.knn(surface.points, kn)
+    idx = idx.astype(np.int64)
+    m = len(P)
+    n = cnt.astype(np.int64)
+    nf = n.astype(np.float64) - 1.0
+    ok = n >= 3
+    sx = np.zeros(m); sy = np.zeros(m); sz = np.zeros(m)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for j in range(1, kn):
+            r = ok & (j < n)
+            p = P[idx[r, j]]
+            sx[r] = sx[r] + p[:, 0] / nf[r]
+            sy[r] = sy[r] + p[:, 1] / nf[r]
+            sz[r] = sz[r] + p[:, 2] / nf[r]
+        xx = np.zeros(m); xy = np.zeros(m); xz = np.zeros(m); yy = np.zeros(m); yz = np.zeros(m); zz = np.zeros(m)
+        for j in range(1, kn):
+            r = ok & (j < n)
+            p = P[idx[r, j]]
+            rx, ry, rz = p[:, 0] - sx[r], p[:, 1] - sy[r], p[:, 2] - sz[r]
+            f = nf[r]
+            xx[r] = xx[r] + rx * rx / f
+            xy[r] = xy[r] + rx * ry / f
+            xz[r] = xz[r] + rx * rz / f
+            yy[r] = yy[r] + ry * ry / f
+            yz[r] = yz[r] + ry * rz / f
+            zz[r] = zz[r] + rz * rz / f
+        w = np.zeros((m, 3))
+
+        def add_axis(ax, ay, az, det):
+            wt = det * det
+            dot = (w[:, 0] * ax + w[:, 1] * ay) + w[:, 2] * az
+            wt = np.where(dot < 0.0, -wt, wt)
+            w[:, 0] = w[:, 0] + ax * wt
+            w[:, 1] = w[:, 1] + ay * wt
+            w[:, 2] = w[:, 2] + az * wt
+
+        det_x = yy * zz - yz * yz
+        add_axis(det_x, xz * yz - xy * zz, xy * yz - xz * yy, det_x)
+        det_y = xx * zz - xz * xz
+        add_axis(xz * yz - xy * zz, det_y, xy * xz - yz * xx, det_y)
+        det_z = xx * yy - xy * xy
+        add_axis(xy * yz - xz * yy, xy * xz - yz * xx, det_z, det_z)
+        mag = np.sqrt((w[:, 0] * w[:, 0] + w[:, 1] * w[:, 1]) + w[:, 2] * w[:, 2])
+        w = w / mag[:, None]
+        f = np.asarray(flip, np.float32).astype(np.float64)
+        d = f[None, :] - P
+        scalar = (d[:, 0] * w[:, 0] + d[:, 1] * w[:, 1]) + d[:, 2] * w[:, 2]
+    bad = ~np.isfinite(scalar)
+    w[bad] = 0.0
+    w[scalar < 0] = -w[scalar < 0]
+    w[~ok] = 0.0
+    return w.astype(np.float32)
+
+
 def _normalize(v):
     """BaseVector::normalize (include/lvr2/geometry/BaseVector.hpp:130-143):
     divide by sqrt(x*x + y*y + z*z) unless the vector is zero; float32."""

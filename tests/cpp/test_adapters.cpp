@@ -86,6 +86,29 @@ int main() {
     }
     EXPECT(radial > size_t(0.95 * double(m.info.vertices)));
 
+    // CudaKSearchSurface (--pcm LBVH_CUDA): unit normals pointing toward (1e6, 1e6, 1e6)
+    {
+        lvr2gb::CudaKSearchSurface ks(xyz.data(), n, 20);
+        ks.calculateSurfaceNormals();
+        auto kn = ks.normals();
+        EXPECT(kn.size() == 3 * n);
+        size_t unit = 0, toward = 0;
+        for (size_t i = 0; i < n; i++) {
+            const float* q = &kn[3 * i];
+            const float* p = &xyz[3 * i];
+            unit += std::fabs(std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) - 1.0f) < 1e-5f;
+            toward += q[0] * (1e6f - p[0]) + q[1] * (1e6f - p[1]) + q[2] * (1e6f - p[2]) >= -1.0f;
+        }
+        EXPECT(unit == n && toward == n);
+        bool threw = false;
+        try {
+            ks.distance(lvr2gb::Vec3{0, 0, 0});
+        } catch (const std::runtime_error&) {
+            threw = true;
+        }
+        EXPECT(threw);
+    }
+
     // the CudaSurface call sequence of lvr2_reconstruct --useGPU (Main.cpp:353-379)
     std::shared_ptr<float[]> pts(new float[3 * n]);
     std::copy(xyz.begin(), xyz.end(), pts.get());

@@ -135,3 +135,26 @@ def test_unsupported_method(oracle_mod):
     s = oracle_mod.OracleSurface(GOLD["sphere/points"])
     with pytest.raises(ValueError):
         s.normals(5, nem=1)
+
+
+def test_lbvh_comparator_fit_restatement(oracle_mod):
+    """The restated LBVHIndex::knn_normals fit (nem 4): close to FP64 PCA of
+    the same neighbours (slot 0 left out) on a dense noisy sphere, flipped
+    toward the flip point, zero for collinear neighbourhoods and for fewer
+    than 3 neighbours."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    v = rng.standard_normal((40_000, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    P = (0.5 * v + 0.0005 * rng.standard_normal((40_000, 3))).astype(np.float32)
+    S = oracle_mod.OracleSurface(P)
+    n = oracle_mod.lbvh_knn_normals(S, 20, flip=(0.0, 0.0, 0.0))
+    idx, _, _ = S.knn(P, 20)
+    Q = P.astype(np.float64)[idx[:, 1:].astype(np.int64)]
+    C = Q - Q.mean(1, keepdims=True)
+    _, vec = np.linalg.eigh(np.einsum("nki,nkj->nij", C, C))
+    assert np.percentile(angle_deg(vec[:, :, 0], n, unsigned=True), 99) < 2.0
+    assert np.all((n * P).sum(1) < 0)  # toward the centre
+    line = np.c_[np.linspace(0, 1, 50), np.zeros(50), np.zeros(50)].astype(np.float32)
+    assert not oracle_mod.lbvh_knn_normals(oracle_mod.OracleSurface(line), 10).any()
+    two = np.array([[0, 0, 0], [1, 0, 0]], np.float32)
+    assert not oracle_mod.lbvh_knn_normals(oracle_mod.OracleSurface(two), 10).any()
