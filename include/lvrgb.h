@@ -279,6 +279,25 @@ lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_
 lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, float* distance,
                             uint8_t* invalid, int32_t on_device, void* stream);
 
+/* The large-scale reconstruction's merge and mesh step
+ * (LargeScaleReconstruction.tcc:433-449, 781-789): HashGrid(chunks, innerBoxes,
+ * bb, voxelsize) (include/lvr2/reconstruction/HashGrid.tcc:136-193) built from
+ * stored chunk grids, then FastReconstruction::getMesh.  The cells are the
+ * concatenation of the chunks' lvrgb_get_cell_tsdf outputs: centers (n x 3)
+ * and tsdf_values (n x 8), chunk c holding cells [chunk_offsets[c],
+ * chunk_offsets[c + 1]) (host array of nchunks + 1, or NULL for one chunk).
+ * inner_boxes (host, nchunks x 6: min xyz, max xyz, or NULL): a cell is kept
+ * when its chunk's box contains its centre (BoundingBox::contains).  A cell
+ * index (floor(centre / voxel_size)) already present keeps its first copy, and
+ * a grid vertex takes the distance of the earliest cell holding it, as
+ * HashGrid::addBox does.  decomposition 0 = FastBox (the large-scale default),
+ * 1 = BilinearFastBox.  The result replaces the surface's last mesh (read it
+ * with lvrgb_get_mesh); the surface's points are not used. */
+lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t decomposition, const float* centers,
+                                     const float* tsdf_values, int64_t ncells, const int64_t* chunk_offsets,
+                                     int32_t nchunks, const float* inner_boxes, lvrgb_mesh_info* info,
+                                     int32_t on_device, void* stream);
+
 /* HashGrid::toPointBuffer (include/lvr2/reconstruction/HashGrid.tcc:196-233),
  * the per-chunk grid the large-scale reconstruction stores and merges: for
  * each cell kept after culling (lattice-key order, in place of the hash map's

@@ -682,6 +682,61 @@ lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrg
     });
 }
 
+lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t decomposition, const float* centers,
+                                     const float* tsdf_values, int64_t ncells, const int64_t* chunk_offsets,
+                                     int32_t nchunks, const float* inner_boxes, lvrgb_mesh_info* info,
+                                     int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(voxel_size > 0 && std::isfinite(voxel_size), LVRGB_ERR_INVALID_ARGUMENT, "voxel size must be > 0");
+        require(decomposition == 0 || decomposition == 1, LVRGB_ERR_UNSUPPORTED,
+                "decomposition must be 0 (MC) or 1 (PMC)");
+        require(ncells >= 0 && ncells < (int64_t(1) << 28), LVRGB_ERR_INVALID_ARGUMENT, "cell count out of range");
+        require(ncells == 0 || (centers && tsdf_values), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        std::vector<int64_t> off;
+        if (chunk_offsets) {
+            require(nchunks >= 1, LVRGB_ERR_INVALID_ARGUMENT, "nchunks must be >= 1");
+            require(chunk_offsets[0] == 0 && chunk_offsets[nchunks] == ncells, LVRGB_ERR_INVALID_ARGUMENT,
+                    "chunk_offsets must run from 0 to ncells");
+            for (int c = 0; c < nchunks; c++)
+                require(chunk_offsets[c + 1] >= chunk_offsets[c], LVRGB_ERR_INVALID_ARGUMENT,
+                        "chunk_offsets must not decrease");
+            off.assign(chunk_offsets, chunk_offsets + nchunks + 1);
+        } else {
+            require(inner_boxes == nullptr, LVRGB_ERR_INVALID_ARGUMENT, "inner_boxes need chunk_offsets");
+            nchunks = 1;
+            off = {0, ncells};
+        }
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const int n = int(ncells);
+        const float* dc = stage_in(s->ws, "cells.c", centers, size_t(n) * 3, on_device, st);
+        const float* dt = stage_in(s->ws, "cells.t", tsdf_values, size_t(n) * 8, on_device, st);
+        int64_t* doff = s->ws.get<int64_t>("cells.off", off.size());
+        LVRGB_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        float* dbox = nullptr;
+        if (inner_boxes) {
+            dbox = s->ws.get<float>("cells.box", size_t(nchunks) * 6);
+            LVRGB_CUDA(cudaMemcpyAsync(dbox, inner_boxes, size_t(nchunks) * 6 * sizeof(float), cudaMemcpyHostToDevice,
+                                       st));
+        }
+        s->has_grid = false;
+        grid_from_cells(dc, dt, n, doff, nchunks, dbox, voxel_size, decomposition, s->ws, s->grid, s->d_err, st);
+        LVRGB_CUDA(cudaStreamSynchronize(st));  // the host offsets and boxes are read by then
+        check_kernel_error(s, st);
+        s->has_grid = true;
+        if (info) {
+            *info = lvrgb_mesh_info{};
+            info->cells_all = s->grid.ncells_all;
+            info->grid_vertices = s->grid.nqp;
+            info->cells_valid = s->grid.ncells_valid;
+            info->vertices = s->grid.nverts;
+            info->faces = s->grid.nfaces;
+            info->voxelsize = s->grid.vs;
+        }
+    });
+}
+
 lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* moved, void* stream) {
     return guarded([&] {
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");

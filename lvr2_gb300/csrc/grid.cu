@@ -7,6 +7,7 @@
 // so that sorted cells and vertices are spatially coherent: consecutive grid
 // vertices form the 32-query groups of the signed-distance kNN.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <stdexcept>
 
@@ -445,6 +446,90 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
     LVRGB_LAUNCH_CHECK();
 }
 
+namespace {
+// Marching cubes over the valid cells of R (FastReconstruction::getMesh with
+// FastBox / BilinearFastBox): count, scan, emit, deduplicate the vertices.
+void mc_stage(GridResult& R, const Frame& F, int kbits, int decomposition, Workspace& ws, cudaStream_t s) {
+    const uint64_t* ck = R.cell_keys;
+    const uint32_t* cell_corner = R.cell_corner;
+    const uint32_t* valid = R.valid_cells;
+    const size_t nvalid = size_t(R.ncells_valid);
+    GridConfig cfg;
+    cfg.decomposition = decomposition;
+    size_t nf = 0;
+    uint32_t* fcount = ws.get<uint32_t>("mc.count", nvalid);
+    uint32_t* foff = ws.get<uint32_t>("mc.off", nvalid + 1);
+    if (nvalid) {
+        mc_kernel<false><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                               cfg.decomposition == 1, fcount, nullptr, nullptr,
+                                                               nullptr, nullptr);
+        LVRGB_LAUNCH_CHECK();
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nvalid));
+        exclusive_scan_u32(fcount, foff, nvalid, stmp, foff + nvalid, s);
+        nf = size_t(uint32_t(read_u64(ws, foff + nvalid, sizeof(uint32_t), s)));
+    }
+    const size_t nref = nf * 3;
+    uint64_t* rk = ws.get<uint64_t>("mc.rk", nref);
+    uint32_t* rv = ws.get<uint32_t>("mc.rv", nref);
+    float4* rp = ws.get<float4>("mc.rp", nref);
+    uint32_t* faces = ws.get<uint32_t>("mc.faces", nref);
+    uint64_t* vkeys = ws.get<uint64_t>("mc.vkeys", nref);
+    size_t nv = 0;
+    const bool dense_edges = use_dense(kbits + 2, nref);
+    float* verts = nullptr;
+    if (nf && dense_edges) {
+        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
+        LVRGB_LAUNCH_CHECK();
+        const size_t NE = size_t(1) << (kbits + 2);
+        uint32_t* eflags = ws.get<uint32_t>("mc.dflags", NE);
+        uint32_t* epos = ws.get<uint32_t>("mc.dpos", NE + 1);
+        LVRGB_CUDA(cudaMemsetAsync(eflags, 0, NE * sizeof(uint32_t), s));
+        mark_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, nref, eflags);
+        LVRGB_LAUNCH_CHECK();
+        nv = dense_scan(ws, eflags, epos, NE, s);
+        dense_compact_kernel<<<ceil_div(NE, 256), 256, 0, s>>>(eflags, epos, NE, vkeys);
+        LVRGB_LAUNCH_CHECK();
+        verts = ws.get<float>("mc.verts", nv * 3);
+        dense_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rp, nref, epos, faces, verts);
+        LVRGB_LAUNCH_CHECK();
+    } else if (nf) {
+        uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
+        uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
+        uint32_t* first = ws.get<uint32_t>("mc.first", nref);
+        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
+        LVRGB_LAUNCH_CHECK();
+        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(nref));
+        if (radix_sort_pairs<uint64_t>(rk, rv, rk2, rv2, nref, 0, kbits + 2, tmp, s)) {
+            std::swap(rk, rk2);
+            std::swap(rv, rv2);
+        }
+        uint32_t* flags = ws.get<uint32_t>("grid.flags", nref);
+        uint32_t* pos = ws.get<uint32_t>("grid.pos", nref + 1);
+        head_flags_u64(rk, nref, flags, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nref));
+        exclusive_scan_u32(flags, pos, nref, stmp, pos + nref, s);
+        assign_ids_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rv, flags, pos, int(nref), faces, vkeys, first);
+        LVRGB_LAUNCH_CHECK();
+        nv = size_t(uint32_t(read_u64(ws, pos + nref, sizeof(uint32_t), s)));
+        verts = ws.get<float>("mc.verts", nv * 3);
+        if (nv) {
+            vertex_out_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(first, int(nv), rp, verts);
+            LVRGB_LAUNCH_CHECK();
+        }
+    }
+    if (!verts) verts = ws.get<float>("mc.verts", 1);
+    R.nfaces = (long long)nf;
+    R.nverts = (long long)nv;
+    R.faces = faces;
+    R.face_cell_off = foff;
+    R.vert_keys = vkeys;
+    R.verts = verts;
+}
+
+}  // namespace
+
 void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], const GridConfig& cfg, Workspace& ws,
                       GridResult& R, int* d_err, cudaStream_t s, GridTimings* timings) {
     StageTimer timer(timings != nullptr);
@@ -588,79 +673,220 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     R.valid_cells = valid;
     timer.mark(3, s);
 
-    // ---- marching cubes: count, scan, emit, deduplicate vertices ---------
-    size_t nf = 0;
-    uint32_t* fcount = ws.get<uint32_t>("mc.count", nvalid);
-    uint32_t* foff = ws.get<uint32_t>("mc.off", nvalid + 1);
-    if (nvalid) {
-        mc_kernel<false><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                               cfg.decomposition == 1, fcount, nullptr, nullptr,
-                                                               nullptr, nullptr);
-        LVRGB_LAUNCH_CHECK();
-        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nvalid));
-        exclusive_scan_u32(fcount, foff, nvalid, stmp, foff + nvalid, s);
-        nf = size_t(uint32_t(read_u64(ws, foff + nvalid, sizeof(uint32_t), s)));
-    }
-    const size_t nref = nf * 3;
-    uint64_t* rk = ws.get<uint64_t>("mc.rk", nref);
-    uint32_t* rv = ws.get<uint32_t>("mc.rv", nref);
-    float4* rp = ws.get<float4>("mc.rp", nref);
-    uint32_t* faces = ws.get<uint32_t>("mc.faces", nref);
-    uint64_t* vkeys = ws.get<uint64_t>("mc.vkeys", nref);
-    size_t nv = 0;
-    const bool dense_edges = use_dense(kbits + 2, nref);
-    float* verts = nullptr;
-    if (nf && dense_edges) {
-        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
-        LVRGB_LAUNCH_CHECK();
-        const size_t NE = size_t(1) << (kbits + 2);
-        uint32_t* eflags = ws.get<uint32_t>("mc.dflags", NE);
-        uint32_t* epos = ws.get<uint32_t>("mc.dpos", NE + 1);
-        LVRGB_CUDA(cudaMemsetAsync(eflags, 0, NE * sizeof(uint32_t), s));
-        mark_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, nref, eflags);
-        LVRGB_LAUNCH_CHECK();
-        nv = dense_scan(ws, eflags, epos, NE, s);
-        dense_compact_kernel<<<ceil_div(NE, 256), 256, 0, s>>>(eflags, epos, NE, vkeys);
-        LVRGB_LAUNCH_CHECK();
-        verts = ws.get<float>("mc.verts", nv * 3);
-        dense_refs_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rp, nref, epos, faces, verts);
-        LVRGB_LAUNCH_CHECK();
-    } else if (nf) {
-        uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
-        uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
-        uint32_t* first = ws.get<uint32_t>("mc.first", nref);
-        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
-        LVRGB_LAUNCH_CHECK();
-        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(nref));
-        if (radix_sort_pairs<uint64_t>(rk, rv, rk2, rv2, nref, 0, kbits + 2, tmp, s)) {
-            std::swap(rk, rk2);
-            std::swap(rv, rv2);
-        }
-        uint32_t* flags = ws.get<uint32_t>("grid.flags", nref);
-        uint32_t* pos = ws.get<uint32_t>("grid.pos", nref + 1);
-        head_flags_u64(rk, nref, flags, s);
-        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nref));
-        exclusive_scan_u32(flags, pos, nref, stmp, pos + nref, s);
-        assign_ids_kernel<<<ceil_div(nref, 256), 256, 0, s>>>(rk, rv, flags, pos, int(nref), faces, vkeys, first);
-        LVRGB_LAUNCH_CHECK();
-        nv = size_t(uint32_t(read_u64(ws, pos + nref, sizeof(uint32_t), s)));
-        verts = ws.get<float>("mc.verts", nv * 3);
-        if (nv) {
-            vertex_out_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(first, int(nv), rp, verts);
-            LVRGB_LAUNCH_CHECK();
-        }
-    }
-    if (!verts) verts = ws.get<float>("mc.verts", 1);
+    mc_stage(R, F, kbits, cfg.decomposition, ws, s);
     timer.mark(4, s);
-    R.nfaces = (long long)nf;
-    R.nverts = (long long)nv;
-    R.faces = faces;
-    R.face_cell_off = foff;
-    R.vert_keys = vkeys;
-    R.verts = verts;
     timer.finish(timings, s);
+}
+
+namespace {
+
+// Merged grid of stored chunk cells (HashGrid(chunks, innerBoxes, bb, voxelsize),
+// HashGrid.tcc:136-193).
+__global__ void merge_index_kernel(const float* __restrict__ centers, int n, const int64_t* __restrict__ off,
+                                   int nchunks, const float* __restrict__ boxes, float vs, int4* __restrict__ idx,
+                                   uint32_t* __restrict__ keep, int* __restrict__ range) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = centers[3 * size_t(i)], y = centers[3 * size_t(i) + 1], z = centers[3 * size_t(i) + 2];
+    bool ok = true;
+    if (boxes) {
+        int lo = 0, hi = nchunks - 1;  // chunk c holds cells [off[c], off[c + 1])
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        const float* b = boxes + 6 * size_t(lo);
+        // BoundingBox::contains (BoundingBox.tcc:166-171)
+        ok = (b[0] <= x && b[3] >= x) && (b[1] <= y && b[4] >= y) && (b[2] <= z && b[5] >= z);
+    }
+    // HashGrid::calcIndex (HashGrid.hpp:263-268)
+    const float fx = floorf(__fdiv_rn(x, vs)), fy = floorf(__fdiv_rn(y, vs)), fz = floorf(__fdiv_rn(z, vs));
+    ok = ok && fabsf(fx) < 1e9f && fabsf(fy) < 1e9f && fabsf(fz) < 1e9f;  // NaN fails too
+    keep[i] = ok ? 1u : 0u;
+    if (!ok) return;
+    const int ix = int(fx), iy = int(fy), iz = int(fz);
+    idx[i] = make_int4(ix, iy, iz, 0);
+    atomicMin(range + 0, ix); atomicMin(range + 1, iy); atomicMin(range + 2, iz);
+    atomicMax(range + 3, ix); atomicMax(range + 4, iy); atomicMax(range + 5, iz);
+}
+
+__global__ void merge_keys_kernel(const int4* __restrict__ idx, const uint32_t* __restrict__ keep,
+                                  const uint32_t* __restrict__ pos, int n, int bx, int by, int bz,
+                                  uint64_t* __restrict__ keys, uint32_t* __restrict__ rank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !keep[i]) return;
+    const int4 c = idx[i];
+    keys[pos[i]] = lattice_key(uint32_t(c.x - bx), uint32_t(c.y - by), uint32_t(c.z - bz));
+    rank[pos[i]] = uint32_t(i);
+}
+
+// Unique cells (the first of each run of equal keys: the earliest input cell).
+__global__ void merge_unique_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ rank,
+                                    const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, int n,
+                                    uint64_t* __restrict__ ukeys, uint32_t* __restrict__ urank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flags[i]) return;
+    ukeys[pos[i]] = keys[i];
+    urank[pos[i]] = rank[i];
+}
+
+// Corner slots j * 8 + k, generated cell by cell in input order so that a
+// stable sort by corner key puts the earliest cell's slot first.
+__global__ void merge_corner_kernel(const uint64_t* __restrict__ ukeys, const uint32_t* __restrict__ order, int nc,
+                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc * 8) return;
+    const uint32_t j = order[t >> 3];
+    const int k = t & 7;
+    uint32_t x, y, z;
+    lattice_decode(ukeys[j], x, y, z);
+    keys[t] = lattice_key(x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2]);
+    vals[t] = j * 8u + uint32_t(k);
+}
+
+// A grid vertex takes the distance the earliest cell holding it gave
+// (HashGrid::addBox keeps a shared corner found by findQueryPoint).
+__global__ void merge_dist_kernel(const uint32_t* __restrict__ first, int nqp, const uint32_t* __restrict__ urank,
+                                  const float* __restrict__ tsdf, float* __restrict__ dist) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nqp) return;
+    const uint32_t slot = first[q];
+    dist[q] = tsdf[size_t(urank[slot >> 3]) * 8 + (slot & 7u)];
+}
+
+}  // namespace
+
+void grid_from_cells(const float* centers, const float* tsdf, int n, const int64_t* chunk_off, int nchunks,
+                     const float* boxes, float vs, int decomposition, Workspace& ws, GridResult& R, int* d_err,
+                     cudaStream_t s) {
+    (void)d_err;
+    R = GridResult();
+    if (!(vs > 0.0f) || !std::isfinite(vs)) throw std::invalid_argument("voxel size must be positive");
+    R.vs = vs;
+    Frame F;
+    F.vs = vs;
+    for (int a = 0; a < 3; a++) {
+        F.lo[a] = -INFINITY;
+        F.hi[a] = INFINITY;
+    }
+    int4* idx = ws.get<int4>("merge.idx", size_t(std::max(n, 1)));
+    uint32_t* keep = ws.get<uint32_t>("merge.keep", size_t(std::max(n, 1)));
+    uint32_t* kpos = ws.get<uint32_t>("merge.kpos", size_t(n) + 1);
+    int* range = ws.get<int>("merge.range", 6);
+    const int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+    LVRGB_CUDA(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    size_t nk = 0;
+    if (n > 0) {
+        merge_index_kernel<<<ceil_div(n, 256), 256, 0, s>>>(centers, n, chunk_off, nchunks, boxes, vs, idx, keep, range);
+        LVRGB_LAUNCH_CHECK();
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(size_t(n)));
+        exclusive_scan_u32(keep, kpos, size_t(n), stmp, kpos + n, s);
+        nk = size_t(uint32_t(read_u64(ws, kpos + n, sizeof(uint32_t), s)));
+    }
+    int rng[6] = {0, 0, 0, 0, 0, 0};
+    if (nk) {
+        LVRGB_CUDA(cudaMemcpyAsync(rng, range, sizeof(rng), cudaMemcpyDeviceToHost, s));
+        LVRGB_CUDA(cudaStreamSynchronize(s));
+    }
+    int top = 1;
+    for (int a = 0; a < 3; a++) {
+        R.base[a] = rng[a] - 1;
+        top = std::max(top, rng[3 + a] - R.base[a] + 2);
+    }
+    F.bx = R.base[0]; F.by = R.base[1]; F.bz = R.base[2];
+    int nbits = 1;
+    while ((1 << nbits) <= top + 1) nbits++;
+    if (nbits > 20) throw std::invalid_argument("grid extent exceeds 2^20 cells per axis");
+    R.nbits = nbits;
+    const int kbits = 3 * nbits;
+
+    // kept cells (key, input index), sorted by key; the first of equal keys wins
+    uint64_t* ck = ws.get<uint64_t>("merge.keys", std::max<size_t>(nk, 1));
+    uint32_t* cr = ws.get<uint32_t>("merge.rank", std::max<size_t>(nk, 1));
+    size_t nc = 0;
+    uint64_t* uck = ws.get<uint64_t>("grid.cellsA", std::max<size_t>(nk, 1));
+    uint32_t* urank = ws.get<uint32_t>("merge.urank", std::max<size_t>(nk, 1));
+    if (nk) {
+        merge_keys_kernel<<<ceil_div(n, 256), 256, 0, s>>>(idx, keep, kpos, n, R.base[0], R.base[1], R.base[2], ck, cr);
+        LVRGB_LAUNCH_CHECK();
+        uint64_t* ck2 = ws.get<uint64_t>("merge.keys2", nk);
+        uint32_t* cr2 = ws.get<uint32_t>("merge.rank2", nk);
+        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(nk));
+        if (radix_sort_pairs<uint64_t>(ck, cr, ck2, cr2, nk, 0, kbits, tmp, s)) {
+            std::swap(ck, ck2);
+            std::swap(cr, cr2);
+        }
+        uint32_t* flags = ws.get<uint32_t>("grid.flags", nk);
+        uint32_t* pos = ws.get<uint32_t>("grid.pos", nk + 1);
+        head_flags_u64(ck, nk, flags, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nk));
+        exclusive_scan_u32(flags, pos, nk, stmp, pos + nk, s);
+        merge_unique_kernel<<<ceil_div(nk, 256), 256, 0, s>>>(ck, cr, flags, pos, int(nk), uck, urank);
+        LVRGB_LAUNCH_CHECK();
+        nc = size_t(uint32_t(read_u64(ws, pos + nk, sizeof(uint32_t), s)));
+    }
+    R.ncells_all = (long long)nc;
+    R.cell_keys = uck;
+
+    // grid vertices: corners of the cells, taken in input order of the cells
+    const size_t ncorner = nc * 8;
+    uint32_t* cell_corner = ws.get<uint32_t>("grid.cell_corner", std::max<size_t>(ncorner, 1));
+    uint64_t* qk = ws.get<uint64_t>("grid.qp_keys", std::max<size_t>(ncorner, 1));
+    size_t nqp = 0;
+    uint32_t* first = ws.get<uint32_t>("merge.first", std::max<size_t>(ncorner, 1));
+    if (nc) {
+        // cells in input order
+        uint32_t* rk = ws.get<uint32_t>("merge.rk", nc);
+        uint32_t* rk2 = ws.get<uint32_t>("merge.rk2", nc);
+        uint32_t* ord = ws.get<uint32_t>("merge.ord", nc);
+        uint32_t* ord2 = ws.get<uint32_t>("merge.ord2", nc);
+        LVRGB_CUDA(cudaMemcpyAsync(rk, urank, nc * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        iota_u32(ord, nc, s);
+        void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint32_t>(nc));
+        if (radix_sort_pairs<uint32_t>(rk, ord, rk2, ord2, nc, 0, 32, tmp, s)) std::swap(ord, ord2);
+        uint64_t* pk = ws.get<uint64_t>("grid.cornerk", ncorner);
+        uint32_t* pv = ws.get<uint32_t>("grid.cornerv", ncorner);
+        uint64_t* pk2 = ws.get<uint64_t>("grid.cornerk2", ncorner);
+        uint32_t* pv2 = ws.get<uint32_t>("grid.cornerv2", ncorner);
+        merge_corner_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(uck, ord, int(nc), pk, pv);
+        LVRGB_LAUNCH_CHECK();
+        void* tmp2 = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(ncorner));
+        if (radix_sort_pairs<uint64_t>(pk, pv, pk2, pv2, ncorner, 0, kbits, tmp2, s)) {
+            std::swap(pk, pk2);
+            std::swap(pv, pv2);
+        }
+        uint32_t* flags = ws.get<uint32_t>("grid.flags", ncorner);
+        uint32_t* pos = ws.get<uint32_t>("grid.pos", ncorner + 1);
+        head_flags_u64(pk, ncorner, flags, s);
+        void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(ncorner));
+        exclusive_scan_u32(flags, pos, ncorner, stmp, pos + ncorner, s);
+        assign_ids_kernel<<<ceil_div(ncorner, 256), 256, 0, s>>>(pk, pv, flags, pos, int(ncorner), cell_corner, qk,
+                                                                   first);
+        LVRGB_LAUNCH_CHECK();
+        nqp = size_t(uint32_t(read_u64(ws, pos + ncorner, sizeof(uint32_t), s)));
+    }
+    R.nqp = (long long)nqp;
+    R.qp_keys = qk;
+    R.cell_corner = cell_corner;
+    float4* qpos = ws.get<float4>("grid.qp_pos", std::max<size_t>(nqp, 1));
+    R.qp_pos = qpos;
+    R.qp_dist = ws.get<float>("grid.qp_dist", std::max<size_t>(nqp, 1));
+    R.qp_eucl = ws.get<float>("grid.qp_eucl", std::max<size_t>(nqp, 1));
+    R.qp_invalid = ws.get<uint8_t>("grid.qp_invalid", std::max<size_t>(nqp, 1));
+    if (nqp) {
+        qp_pos_kernel<<<ceil_div(nqp, 256), 256, 0, s>>>(qk, int(nqp), F, qpos);
+        LVRGB_LAUNCH_CHECK();
+        merge_dist_kernel<<<ceil_div(nqp, 256), 256, 0, s>>>(first, int(nqp), urank, tsdf, R.qp_dist);
+        LVRGB_LAUNCH_CHECK();
+        LVRGB_CUDA(cudaMemsetAsync(R.qp_eucl, 0, nqp * sizeof(float), s));
+        LVRGB_CUDA(cudaMemsetAsync(R.qp_invalid, 0, nqp, s));
+    }
+    // every merged cell is valid (the chunks were culled when they were made)
+    uint32_t* valid = ws.get<uint32_t>("grid.valid", std::max<size_t>(nc, 1));
+    if (nc) iota_u32(valid, nc, s);
+    R.ncells_valid = (long long)nc;
+    R.valid_cells = valid;
+    mc_stage(R, F, kbits, decomposition, ws, s);
 }
 
 namespace {

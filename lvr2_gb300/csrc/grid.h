@@ -51,6 +51,16 @@ struct GridTimings {
 void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], const GridConfig& cfg,
                       Workspace& ws, GridResult& R, int* d_err, cudaStream_t s, GridTimings* timings = nullptr);
 
+// HashGrid(chunks, innerBoxes, bb, voxelsize) (HashGrid.tcc:136-193) followed
+// by marching cubes: n stored cells (centres n x 3, corner distances n x 8,
+// device), chunk c holding cells [chunk_off[c], chunk_off[c + 1]) (device);
+// boxes (device, nchunks x 6, or null): a cell is kept when its chunk's box
+// contains its centre.  A cell already present keeps its first copy; a grid
+// vertex takes the distance of the earliest cell holding it.
+void grid_from_cells(const float* centers, const float* tsdf, int n, const int64_t* chunk_off, int nchunks,
+                     const float* boxes, float vs, int decomposition, Workspace& ws, GridResult& R, int* d_err,
+                     cudaStream_t s);
+
 // HashGrid::toPointBuffer (HashGrid.tcc:196-233) of the culled grid: per valid
 // cell (lattice-key order) its centre (centers, 3 floats) and the projected
 // distances at its 8 corners in FastBox corner order (tsdf, 8 floats).

@@ -309,6 +309,25 @@ class Surface:
                                      self._stream))
         return out, int(cnt.value)
 
+    def reconstruct_cells(self, centers, tsdf, voxelsize, chunk_offsets=None, inner_boxes=None, decomposition="MC"):
+        """HashGrid(chunks, innerBoxes, bb, voxelsize) + marching cubes over
+        stored chunk cells (centres (n, 3), corner distances (n, 8));
+        chunk_offsets (nchunks + 1) and inner_boxes (nchunks, 6) optional.
+        The mesh replaces this surface's last mesh."""
+        c = np.ascontiguousarray(centers, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(tsdf, np.float32).reshape(-1, 8)
+        if len(c) != len(t):
+            raise ValueError("centers and tsdf differ in length")
+        off = None if chunk_offsets is None else np.ascontiguousarray(chunk_offsets, np.int64)
+        box = None if inner_boxes is None else np.ascontiguousarray(inner_boxes, np.float32).reshape(-1, 6)
+        nch = 0 if off is None else len(off) - 1
+        info = MeshInfo()
+        dec = {"MC": 0, "PMC": 1}[decomposition]
+        check(_lib.load().lvrgb_reconstruct_cells(self._h, float(voxelsize), dec, _ptr(c), _ptr(t), len(c), _ptr(off),
+                                                  nch, _ptr(box), ctypes.byref(info), 0, self._stream))
+        self.info = info
+        return info
+
     def cell_tsdf(self):
         """HashGrid::toPointBuffer of the culled grid: cell centres (C, 3) and
         the distances at their 8 corners (C, 8), cells in lattice-key order."""

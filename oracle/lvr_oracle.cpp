@@ -739,6 +739,75 @@ struct orc_recon {
     std::vector<int64_t> cell_face_off;  // faces of valid cell c: [off[c], off[c + 1])
 };
 
+// Marching cubes over the given cells of r (cells_all, qp_pos, qp_dist set).
+static void mc_cells(orc_recon* r, const std::vector<std::array<int32_t, 8>>& cell_qp,
+                     const std::vector<size_t>& valid_cells, int decomposition) {
+    // Marching cubes (FastReconstruction.tcc:47-66, FastBox.tcc:205-269,
+    // BilinearFastBox.tcc:55-138).  Each mesh vertex is identified by the
+    // grid edge it lies on; the reference shares a vertex among the four cells
+    // of an edge through neighbor_table / neighbor_vertex_table, which gives
+    // the same identification.
+    std::unordered_map<EdgeKey, int32_t, EdgeKeyHash> vmap;
+    r->cell_face_off.push_back(0);
+    for (size_t vc : valid_cells) {
+        const L3& ci = r->cells_all[vc];
+        float dist[8];
+        V3 corner[8];
+        for (int k = 0; k < 8; k++) {
+            int32_t q = cell_qp[vc][size_t(k)];
+            dist[k] = r->qp_dist[size_t(q)];
+            corner[k] = r->qp_pos[size_t(q)];
+        }
+        int index = 0;
+        for (int k = 0; k < 8; k++)
+            if (dist[k] > 0) index |= (1 << k);
+        V3 epos[12];
+        EdgeKey ekey[12];
+        for (int e = 0; e < 12; e++) {
+            int a = kEdgeCorners[e][0], b = kEdgeCorners[e][1];
+            int axis = 0;
+            for (int t = 0; t < 3; t++)
+                if (kCornerOff[a][t] != kCornerOff[b][t]) axis = t;
+            int lo = kCornerOff[a][axis] < kCornerOff[b][axis] ? a : b;
+            int hi = lo == a ? b : a;
+            float x = calc_intersection(corner[lo][axis], corner[hi][axis], dist[lo], dist[hi]);
+            V3 p = corner[lo];
+            if (axis == 0) p.x = x;
+            else if (axis == 1) p.y = x;
+            else p.z = x;
+            epos[e] = p;
+            ekey[e] = EdgeKey{L3{ci.x + kCornerOff[lo][0], ci.y + kCornerOff[lo][1],
+                                 ci.z + kCornerOff[lo][2]},
+                              axis};
+        }
+        uint64_t word = kMCTable[index];
+        int ntri = int(word >> 60);
+        for (int t = 0; t < ntri; t++) {
+            int e3[3];
+            for (int b = 0; b < 3; b++) e3[b] = int((word >> (4 * (3 * t + b))) & 0xf);
+            if (decomposition == 1) {
+                if (epos[e3[0]] == epos[e3[1]] || epos[e3[0]] == epos[e3[2]] ||
+                    epos[e3[2]] == epos[e3[1]])
+                    continue;
+            }
+            for (int b = 0; b < 3; b++) {
+                auto it = vmap.find(ekey[e3[b]]);
+                int32_t vid;
+                if (it == vmap.end()) {
+                    vid = int32_t(r->mv_key.size());
+                    vmap.emplace(ekey[e3[b]], vid);
+                    r->mv_key.push_back(ekey[e3[b]]);
+                    r->mv_pos.push_back(epos[e3[b]]);
+                } else {
+                    vid = it->second;
+                }
+                r->faces.push_back(vid);
+            }
+        }
+        r->cell_face_off.push_back(int64_t(r->faces.size() / 3));
+    }
+}
+
 extern "C" {
 
 orc_recon* orc_reconstruct(const orc_surface* s, const float* normals, float resolution,
@@ -843,70 +912,66 @@ orc_recon* orc_reconstruct(const orc_surface* s, const float* normals, float res
         }
     }
 
-    // Marching cubes (FastReconstruction.tcc:47-66, FastBox.tcc:205-269,
-    // BilinearFastBox.tcc:55-138).  Each mesh vertex is identified by the
-    // grid edge it lies on; the reference shares a vertex among the four cells
-    // of an edge through neighbor_table / neighbor_vertex_table, which gives
-    // the same identification.
-    std::unordered_map<EdgeKey, int32_t, EdgeKeyHash> vmap;
-    r->cell_face_off.push_back(0);
-    for (size_t vc : valid_cells) {
-        const L3& ci = r->cells_all[vc];
-        float dist[8];
-        V3 corner[8];
-        for (int k = 0; k < 8; k++) {
-            int32_t q = cell_qp[vc][size_t(k)];
-            dist[k] = r->qp_dist[size_t(q)];
-            corner[k] = r->qp_pos[size_t(q)];
-        }
-        int index = 0;
-        for (int k = 0; k < 8; k++)
-            if (dist[k] > 0) index |= (1 << k);
-        V3 epos[12];
-        EdgeKey ekey[12];
-        for (int e = 0; e < 12; e++) {
-            int a = kEdgeCorners[e][0], b = kEdgeCorners[e][1];
-            int axis = 0;
-            for (int t = 0; t < 3; t++)
-                if (kCornerOff[a][t] != kCornerOff[b][t]) axis = t;
-            int lo = kCornerOff[a][axis] < kCornerOff[b][axis] ? a : b;
-            int hi = lo == a ? b : a;
-            float x = calc_intersection(corner[lo][axis], corner[hi][axis], dist[lo], dist[hi]);
-            V3 p = corner[lo];
-            if (axis == 0) p.x = x;
-            else if (axis == 1) p.y = x;
-            else p.z = x;
-            epos[e] = p;
-            ekey[e] = EdgeKey{L3{ci.x + kCornerOff[lo][0], ci.y + kCornerOff[lo][1],
-                                 ci.z + kCornerOff[lo][2]},
-                              axis};
-        }
-        uint64_t word = kMCTable[index];
-        int ntri = int(word >> 60);
-        for (int t = 0; t < ntri; t++) {
-            int e3[3];
-            for (int b = 0; b < 3; b++) e3[b] = int((word >> (4 * (3 * t + b))) & 0xf);
-            if (decomposition == 1) {
-                if (epos[e3[0]] == epos[e3[1]] || epos[e3[0]] == epos[e3[2]] ||
-                    epos[e3[2]] == epos[e3[1]])
-                    continue;
+    mc_cells(r, cell_qp, valid_cells, decomposition);
+    return r;
+}
+
+// HashGrid(chunks, innerBoxes, bb, voxelsize) (HashGrid.tcc:136-193) over
+// stored chunk cells, then marching cubes: chunk by chunk, cell by cell, a
+// cell whose centre its chunk's inner box contains (BoundingBox::contains)
+// and whose index floor(centre / vs) is new is added; each of its corners
+// reuses an existing grid vertex (findQueryPoint) or is created with this
+// cell's distance (addBox).  Grid vertex positions use the lattice formula.
+orc_recon* orc_reconstruct_cells(const float* centers, const float* tsdf, int64_t n, const int64_t* off,
+                                 int nchunks, const float* boxes, float vs, int decomposition) {
+    auto* r = new orc_recon();
+    r->vs = vs;
+    std::unordered_map<L3, int32_t, L3Hash> cell_index, qp_index;
+    std::vector<std::array<int32_t, 8>> qp_of;
+    std::vector<L3> order;
+    for (int c = 0; c < nchunks; c++) {
+        for (int64_t i = off[c]; i < off[c + 1]; i++) {
+            const float x = centers[3 * i], y = centers[3 * i + 1], z = centers[3 * i + 2];
+            if (boxes) {
+                const float* b = boxes + 6 * c;
+                if (!((b[0] <= x && b[3] >= x) && (b[1] <= y && b[4] >= y) && (b[2] <= z && b[5] >= z))) continue;
             }
-            for (int b = 0; b < 3; b++) {
-                auto it = vmap.find(ekey[e3[b]]);
-                int32_t vid;
-                if (it == vmap.end()) {
-                    vid = int32_t(r->mv_key.size());
-                    vmap.emplace(ekey[e3[b]], vid);
-                    r->mv_key.push_back(ekey[e3[b]]);
-                    r->mv_pos.push_back(epos[e3[b]]);
+            const float fx = std::floor(x / vs), fy = std::floor(y / vs), fz = std::floor(z / vs);
+            if (!(std::fabs(fx) < 1e9f && std::fabs(fy) < 1e9f && std::fabs(fz) < 1e9f)) continue;
+            const L3 idx{int32_t(fx), int32_t(fy), int32_t(fz)};
+            if (cell_index.count(idx)) continue;
+            std::array<int32_t, 8> q{};
+            for (int k = 0; k < 8; k++) {
+                const L3 L{idx.x + kCornerOff[k][0], idx.y + kCornerOff[k][1], idx.z + kCornerOff[k][2]};
+                auto it = qp_index.find(L);
+                if (it == qp_index.end()) {
+                    const int32_t id = int32_t(r->qp_lat.size());
+                    qp_index.emplace(L, id);
+                    r->qp_lat.push_back(L);
+                    r->qp_pos.push_back(V3(lattice_coord(L.x, vs), lattice_coord(L.y, vs), lattice_coord(L.z, vs)));
+                    r->qp_dist.push_back(tsdf[8 * i + k]);
+                    r->qp_invalid.push_back(0);
+                    q[size_t(k)] = id;
                 } else {
-                    vid = it->second;
+                    q[size_t(k)] = it->second;
                 }
-                r->faces.push_back(vid);
             }
+            cell_index.emplace(idx, int32_t(qp_of.size()));
+            qp_of.push_back(q);
+            order.push_back(idx);
         }
-        r->cell_face_off.push_back(int64_t(r->faces.size() / 3));
     }
+    // cells in lattice order (any order gives the same canonical mesh)
+    r->cells_all = order;
+    std::sort(r->cells_all.begin(), r->cells_all.end());
+    std::vector<std::array<int32_t, 8>> cell_qp(r->cells_all.size());
+    std::vector<size_t> valid_cells(r->cells_all.size());
+    for (size_t c = 0; c < r->cells_all.size(); c++) {
+        cell_qp[c] = qp_of[size_t(cell_index[r->cells_all[c]])];
+        valid_cells[c] = c;
+    }
+    r->cells_valid = r->cells_all;
+    mc_cells(r, cell_qp, valid_cells, decomposition);
     return r;
 }
 

@@ -62,6 +62,8 @@ def lib():
     L.orc_recon_optimize_planar.restype = _i64
     L.orc_recon_optimize_planar.argtypes = [_vp, _vp, _int, _int, _int]
     L.orc_mc_table.argtypes = [_i32p]
+    L.orc_reconstruct_cells.restype = _vp
+    L.orc_reconstruct_cells.argtypes = [_f32p, _f32p, _i64, _i64p, _int, ctypes.c_void_p, ctypes.c_float, _int]
     _lib = L
     return L
 
@@ -162,27 +164,39 @@ class OracleSurface:
             moved = 0
             if planar_kc > 0:
                 moved = int(L.orc_recon_optimize_planar(h, self._h, int(planar_kc), int(canonical), self.threads))
-            c = np.zeros(8, np.int64)
-            f = np.zeros(4, np.float32)
-            L.orc_recon_counts(h, c, f)
-            ncell, nqp, nvalid, nv, nf = (int(x) for x in c[:5])
-            lat = np.empty((nqp, 3), np.int32)
-            pos = np.empty((nqp, 3), np.float32)
-            dist = np.empty(nqp, np.float32)
-            inv = np.empty(nqp, np.uint8)
-            L.orc_recon_grid(h, lat, pos, dist, inv)
-            cells_all = np.empty((ncell, 3), np.int32)
-            cells_valid = np.empty((nvalid, 3), np.int32)
-            L.orc_recon_cells(h, cells_all, cells_valid)
-            vkeys = np.empty((nv, 4), np.int32)
-            vpos = np.empty((nv, 3), np.float32)
-            faces = np.empty((nf, 3), np.int32)
-            L.orc_recon_mesh(h, vkeys, vpos, faces)
-        finally:
+        except BaseException:
             L.orc_recon_destroy(h)
-        return dict(voxelsize=float(f[0]), cells_all=cells_all, cells_valid=cells_valid,
-                    qp_lattice=lat, qp_pos=pos, qp_dist=dist, qp_invalid=inv,
-                    vkeys=vkeys, vpos=vpos, faces=faces, planar_moved=moved)
+            raise
+        out = _recon_result(h)
+        out["planar_moved"] = moved
+        return out
+
+
+def _recon_result(h):
+    """Arrays of an orc_recon handle (destroyed here)."""
+    L = lib()
+    try:
+        c = np.zeros(8, np.int64)
+        f = np.zeros(4, np.float32)
+        L.orc_recon_counts(h, c, f)
+        ncell, nqp, nvalid, nv, nf = (int(x) for x in c[:5])
+        lat = np.empty((nqp, 3), np.int32)
+        pos = np.empty((nqp, 3), np.float32)
+        dist = np.empty(nqp, np.float32)
+        inv = np.empty(nqp, np.uint8)
+        L.orc_recon_grid(h, lat, pos, dist, inv)
+        cells_all = np.empty((ncell, 3), np.int32)
+        cells_valid = np.empty((nvalid, 3), np.int32)
+        L.orc_recon_cells(h, cells_all, cells_valid)
+        vkeys = np.empty((nv, 4), np.int32)
+        vpos = np.empty((nv, 3), np.float32)
+        faces = np.empty((nf, 3), np.int32)
+        L.orc_recon_mesh(h, vkeys, vpos, faces)
+    finally:
+        L.orc_recon_destroy(h)
+    return dict(voxelsize=float(f[0]), cells_all=cells_all, cells_valid=cells_valid,
+                qp_lattice=lat, qp_pos=pos, qp_dist=dist, qp_invalid=inv,
+                vkeys=vkeys, vpos=vpos, faces=faces, planar_moved=0)
 
 
 def lbvh_knn_normals(surface, kn, flip=(1e6, 1e6, 1e6)):
@@ -320,6 +334,21 @@ def vertex_colors(vpos, point_colors, surface):
     out = c[idx[:, 0].astype(np.int64)].copy()
     out[cnt <= 0] = 0
     return out
+
+
+def reconstruct_cells(centers, tsdf, voxelsize, chunk_offsets=None, inner_boxes=None, decomposition="MC"):
+    """HashGrid(chunks, innerBoxes, bb, voxelsize) over stored chunk cells,
+    then marching cubes (oracle/lvr_oracle.cpp orc_reconstruct_cells).
+    Returns a dict like OracleSurface.reconstruct."""
+    c = np.ascontiguousarray(centers, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tsdf, np.float32).reshape(-1, 8)
+    off = np.array([0, len(c)], np.int64) if chunk_offsets is None else np.ascontiguousarray(chunk_offsets, np.int64)
+    box = None if inner_boxes is None else np.ascontiguousarray(inner_boxes, np.float32).reshape(-1, 6)
+    L = lib()
+    h = L.orc_reconstruct_cells(c.reshape(-1), t.reshape(-1), len(c), off, len(off) - 1,
+                                None if box is None else box.ctypes.data_as(ctypes.c_void_p), float(voxelsize),
+                                {"MC": 0, "PMC": 1}[decomposition])
+    return _recon_result(h)
 
 
 def mc_table():

@@ -158,3 +158,42 @@ def test_lbvh_comparator_fit_restatement(oracle_mod):
     assert not oracle_mod.lbvh_knn_normals(oracle_mod.OracleSurface(line), 10).any()
     two = np.array([[0, 0, 0], [1, 0, 0]], np.float32)
     assert not oracle_mod.lbvh_knn_normals(oracle_mod.OracleSurface(two), 10).any()
+
+
+def _cells_and_tsdf(r):
+    """Valid cells of an oracle reconstruction as stored chunk cells:
+    centres (index + 0.5) * vs and the 8 corner distances."""
+    vs = np.float32(r["voxelsize"])
+    corners = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+    key = {tuple(v): i for i, v in enumerate(r["qp_lattice"].tolist())}
+    cells = r["cells_valid"].astype(np.int64)
+    ids = np.array([[key[tuple(c)] for c in (v + corners).tolist()] for v in cells])
+    return (cells.astype(np.float32) + np.float32(0.5)) * vs, r["qp_dist"][ids]
+
+
+def test_merged_grid_reproduces_the_chunk_mesh(oracle_mod):
+    """HashGrid(chunks, innerBoxes, ...) restated: the stored cells of one
+    reconstruction, merged back (as one chunk, and as two overlapping chunks
+    cut by inner boxes), give the same marching-cubes mesh."""
+    from lvr2_gb300 import synthetic
+    P = synthetic.spheres_tori(20_000, seed=6)
+    o = oracle_mod.OracleSurface(P)
+    normals = o.normals(10, nem=3)
+    r = o.reconstruct(normals, voxelsize=0.03, kd=10, decomposition="MC")
+    centers, tsdf = _cells_and_tsdf(r)
+    ref = canonical_mesh(r["vkeys"], r["vpos"], r["faces"])
+    m = oracle_mod.reconstruct_cells(centers, tsdf, r["voxelsize"])
+    got = canonical_mesh(m["vkeys"], m["vpos"], m["faces"])
+    assert all(np.array_equal(a, b) for a, b in zip(ref, got))
+    cut = np.float32(0.5)
+    a = centers[:, 0] <= cut + 0.1
+    b = centers[:, 0] >= cut - 0.1  # overlapping chunks; the inner boxes split them at `cut`
+    C = np.concatenate([centers[a], centers[b]])
+    T = np.concatenate([tsdf[a], tsdf[b]])
+    off = np.array([0, a.sum(), a.sum() + b.sum()], np.int64)
+    big = 1e9
+    boxes = np.array([[-big, -big, -big, cut, big, big], [cut, -big, -big, big, big, big]], np.float32)
+    m2 = oracle_mod.reconstruct_cells(C, T, r["voxelsize"], chunk_offsets=off, inner_boxes=boxes)
+    got2 = canonical_mesh(m2["vkeys"], m2["vpos"], m2["faces"])
+    assert len(m2["cells_all"]) == len(centers)
+    assert all(np.array_equal(x, y) for x, y in zip(ref, got2))
