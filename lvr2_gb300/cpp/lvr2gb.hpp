@@ -46,6 +46,8 @@ struct Mesh {
     // calcVertexNormals(mesh, calcFaceNormals(mesh), surface), as handed to the
     // finalizer (src/tools/lvr2_reconstruct/Main.cpp:855-873); V x 3
     std::vector<float> vertexNormals;
+    // calcColorFromPointCloud (ColorAlgorithms.tcc:43-92), V x 3; empty for a cloud without colours
+    std::vector<uint8_t> vertexColors;
     lvrgb_mesh_info info{};
 };
 
@@ -180,6 +182,7 @@ class Surface {
         }
         Mesh m;
         check(lvrgb_reconstruct(h_, &g, &m.info, nullptr), "reconstruct");
+        mesh_vertices_ = m.info.vertices;
         if (g.decomposition == 1 && o.optimizePlanarFaces)
             check(lvrgb_optimize_planar_faces(h_, 5, nullptr, nullptr), "optimizePlanarFaces");
         m.vertices.resize(size_t(3 * m.info.vertices));
@@ -190,11 +193,21 @@ class Surface {
         return m;
     }
 
+    // calcColorFromPointCloud of the last mesh: each vertex takes its nearest
+    // point's colour (pointColors: n x 3 bytes, input order).
+    std::vector<uint8_t> vertexColors(const std::vector<uint8_t>& pointColors) const {
+        if (pointColors.size() != 3 * n_) throw std::runtime_error("vertexColors: need 3 bytes per point");
+        std::vector<uint8_t> out(size_t(3 * mesh_vertices_));
+        check(lvrgb_mesh_vertex_colors(h_, pointColors.data(), 3, out.data(), 0, nullptr), "vertexColors");
+        return out;
+    }
+
     lvrgb_surface handle() const { return h_; }
 
   private:
     lvrgb_surface h_ = nullptr;
     size_t n_ = 0;
+    int64_t mesh_vertices_ = 0;  // vertices of the last reconstruct()
 };
 
 // CudaKSearchSurface (include/lvr2/reconstruction/CudaKSearchSurface.hpp,

@@ -44,7 +44,7 @@ struct Options {
 void usage() {
     std::puts(
         "usage: lvr2gb_reconstruct <inputFile> [--voxelsize|-v F] [--intersections|-i N] [--pcm|-p NAME]\n"
-        "       [--nem 0|2|3] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
+        "       [--nem 0|2|3|4] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
         "       [--flipPoint X Y Z] [--recalcNormals|-r] [--exportPointNormals|-e] [--outputFile PATH]\n"
         "       [--useGPU] [--threads N] [--device N]");
 }
@@ -114,16 +114,36 @@ bool ends_with(const std::string& s, const std::string& t) {
     return s.size() >= t.size() && s.compare(s.size() - t.size(), t.size(), t) == 0;
 }
 
-// ASCII point file: lines of >= 3 numbers; a first line with a single number
-// (point count header) is skipped.
-void read_ascii(const std::string& path, std::vector<float>& xyz) {
+// ASCII point file as AsciiIO::read reads it (src/liblvr2/io/modelio/AsciiIO.cpp:
+// 227-270, 60-200): the first line is skipped; the second line's column count
+// tells the attributes after x y z (3: r g b; 4: intensity r g b; 1:
+// intensity); colours are read as unsigned integers and kept as bytes.
+void read_ascii(const std::string& path, std::vector<float>& xyz, std::vector<uint8_t>& rgb) {
     std::ifstream in(path);
     if (!in) throw std::runtime_error("cannot open " + path);
     std::string line;
+    std::getline(in, line);  // metadata or count
+    std::vector<std::string> lines;
+    int rpos = -1, columns = 0;
     while (std::getline(in, line)) {
         std::istringstream ss(line);
-        float v[3];
-        if (ss >> v[0] >> v[1] >> v[2]) xyz.insert(xyz.end(), v, v + 3);
+        std::vector<double> v;
+        double t;
+        while (ss >> t) v.push_back(t);
+        if (columns == 0) {
+            columns = int(v.size());
+            const int attributes = columns - 3;
+            if (attributes == 3) rpos = 3;
+            if (attributes == 4) rpos = 4;
+        }
+        if (v.size() < 3) continue;
+        for (int a = 0; a < 3; a++) xyz.push_back(float(v[size_t(a)]));
+        if (rpos >= 0) {
+            for (int c = 0; c < 3; c++) {
+                const size_t k = size_t(rpos + c);
+                rgb.push_back(k < v.size() ? uint8_t(unsigned(v[k])) : uint8_t(0));
+            }
+        }
     }
 }
 
@@ -181,29 +201,29 @@ void read_ply(const std::string& path, std::vector<float>& xyz, std::vector<floa
     }
 }
 
-// Vertex element x, y, z, nx, ny, nz (the vertex normals lvr2_reconstruct hands
-// the finalizer; PLYIO.cpp:226-240 writes them after the position), then the
-// faces as uchar-int lists.
+// Vertex element x, y, z, [red, green, blue], nx, ny, nz (the vertex colours
+// and normals lvr2_reconstruct hands the finalizer, in PLYIO.cpp's property
+// order, :166-240), then the faces as uchar-int lists.
 void write_mesh_ply(const std::string& path, const lvr2gb::Mesh& m) {
     std::ofstream out(path, std::ios::binary);
     if (!out) throw std::runtime_error("cannot write " + path);
     const size_t nv = m.vertices.size() / 3, nf = m.faces.size() / 3;
     const bool normals = m.vertexNormals.size() == m.vertices.size() && nv > 0;
+    const bool colors = m.vertexColors.size() == m.vertices.size() && nv > 0;
     out << "ply\nformat binary_little_endian 1.0\ncomment lvr2gb_reconstruct\n"
         << "element vertex " << nv << "\nproperty float x\nproperty float y\nproperty float z\n";
+    if (colors) out << "property uchar red\nproperty uchar green\nproperty uchar blue\n";
     if (normals) out << "property float nx\nproperty float ny\nproperty float nz\n";
     out << "element face " << nf << "\nproperty list uchar int vertex_indices\nend_header\n";
-    if (normals) {
-        std::vector<float> row(6 * nv);
-        for (size_t v = 0; v < nv; v++)
-            for (int c = 0; c < 3; c++) {
-                row[6 * v + c] = m.vertices[3 * v + c];
-                row[6 * v + 3 + c] = m.vertexNormals[3 * v + c];
-            }
-        out.write(reinterpret_cast<const char*>(row.data()), std::streamsize(row.size() * sizeof(float)));
-    } else {
-        out.write(reinterpret_cast<const char*>(m.vertices.data()), std::streamsize(m.vertices.size() * sizeof(float)));
+    const size_t stride = 12 + (colors ? 3 : 0) + (normals ? 12 : 0);
+    std::vector<char> rows(stride * nv);
+    for (size_t v = 0; v < nv; v++) {
+        char* r = rows.data() + stride * v;
+        std::memcpy(r, &m.vertices[3 * v], 12);
+        if (colors) std::memcpy(r + 12, &m.vertexColors[3 * v], 3);
+        if (normals) std::memcpy(r + 12 + (colors ? 3 : 0), &m.vertexNormals[3 * v], 12);
     }
+    out.write(rows.data(), std::streamsize(rows.size()));
     for (size_t f = 0; f < nf; f++) {
         const unsigned char three = 3;
         const int32_t idx[3] = {int32_t(m.faces[3 * f]), int32_t(m.faces[3 * f + 1]), int32_t(m.faces[3 * f + 2])};
@@ -234,19 +254,28 @@ int main(int argc, char** argv) {
     Options o = parse(argc, argv);
     try {
         std::vector<float> xyz, given_normals;
+        std::vector<uint8_t> rgb;
         if (ends_with(o.input, ".ply")) read_ply(o.input, xyz, given_normals);
-        else read_ascii(o.input, xyz);
+        else read_ascii(o.input, xyz, rgb);
         const size_t n = xyz.size() / 3;
         std::printf("[lvr2gb_reconstruct] %zu points from %s\n", n, o.input.c_str());
         if (o.pcm != "LVR2" && o.pcm != "FLANN" && o.pcm != "NANOFLANN" && o.pcm != "LBVH_CUDA" && o.pcm != "GB300")
             std::printf("[lvr2gb_reconstruct] --pcm %s: using the GB300 LBVH\n", o.pcm.c_str());
         double t0 = now_ms();
-        lvr2gb::Surface surface(xyz.data(), n, o.kn, o.ki, o.kd, o.nem, o.device);
+        // --pcm LBVH_CUDA makes lvr2_reconstruct use CudaKSearchSurface (Main.cpp:310-319):
+        // the comparator's fit (nem 4) with k = kn, no interpolation, flipped toward
+        // its fixed point.  (lvr2's CudaKSearchSurface has no distance(); the grid
+        // here uses the AdaptiveKSearchSurface distance with kd.)
+        const bool lbvh = o.pcm == "LBVH_CUDA";
+        lvr2gb::Surface surface(xyz.data(), n, o.kn, lbvh ? 0 : o.ki, o.kd, lbvh ? 4 : o.nem, o.device);
         auto bb = surface.getBoundingBox();
         std::printf("[lvr2gb_reconstruct] BB of points: [%g, %g, %g] - [%g, %g, %g]\n", bb[0].x, bb[0].y, bb[0].z,
                     bb[1].x, bb[1].y, bb[1].z);
         // lvr2_reconstruct sets the flip point to (0,0,0) unless --flipPoint (Main.cpp:335-349)
-        surface.setFlipPoint(lvr2gb::Vec3{o.flip[0], o.flip[1], o.flip[2]});
+        if (lbvh)
+            surface.setFlipPoint(lvr2gb::Vec3{1e6f, 1e6f, 1e6f});
+        else
+            surface.setFlipPoint(lvr2gb::Vec3{o.flip[0], o.flip[1], o.flip[2]});
         const bool have_normals = given_normals.size() == xyz.size() && !given_normals.empty();
         if (!have_normals || o.recalc) {
             surface.calculateSurfaceNormals();
@@ -261,6 +290,8 @@ int main(int argc, char** argv) {
         g.extrude = o.extrude;
         g.decomposition = o.decomposition;
         lvr2gb::Mesh mesh = surface.reconstruct(g);
+        // calcColorFromPointCloud (Main.cpp:868): only for clouds with colours
+        if (rgb.size() == xyz.size()) mesh.vertexColors = surface.vertexColors(rgb);
         double t2 = now_ms();
         std::printf("[lvr2gb_reconstruct] Grid Cells: %lld\n", (long long)mesh.info.cells_valid);
         std::printf("[lvr2gb_reconstruct] Reconstructed mesh (vertices, faces): %lld, %lld\n",

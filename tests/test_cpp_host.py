@@ -38,18 +38,20 @@ def read_ply_counts(path):
 
 
 def read_ply_mesh(path):
-    """Vertices (x y z [nx ny nz] floats) and faces (uchar 3 + int32 x 3) of
-    a binary little-endian PLY written by lvr2gb_reconstruct."""
+    """Vertex records (a numpy structured array with the header's float and
+    uchar properties) and faces (uchar 3 + int32 x 3) of a binary
+    little-endian PLY written by lvr2gb_reconstruct."""
     data = Path(path).read_bytes()
     end = data.index(b"end_header\n") + len(b"end_header\n")
-    head = data[:end].decode()
+    head = data[:end].decode().split("element face")[0]
+    types = {"float": "<f4", "uchar": "u1"}
+    fields = [(ln.split()[2], types[ln.split()[1]]) for ln in head.splitlines() if ln.startswith("property ")]
     nv, nf = read_ply_counts(path)
-    width = 6 if "property float nx" in head else 3
-    v = np.frombuffer(data, np.float32, nv * width, end).reshape(nv, width)
+    v = np.frombuffer(data, np.dtype(fields), nv, end)
     rec = np.dtype([("n", "u1"), ("i", "<i4", 3)])
     f = np.frombuffer(data, rec, nf, end + v.nbytes)
     assert np.all(f["n"] == 3)
-    return v[:, :3], (v[:, 3:] if width == 6 else None), f["i"]
+    return v, f["i"]
 
 
 @pytest.mark.gpu
@@ -85,6 +87,41 @@ def test_cli_matches_python_path(built, tmp_path):
         v, f, _ = s.mesh(with_edges=False)
         vn = s.vertex_normals()
     assert (nv, nf) == (info.vertices, info.faces)
-    pv, pn, pf = read_ply_mesh(out)
-    assert np.array_equal(pv, v) and np.array_equal(pf, f.astype(np.int32)) and np.array_equal(pn, vn)
+    pv, pf = read_ply_mesh(out)
+    assert pv.dtype.names == ("x", "y", "z", "nx", "ny", "nz")
+    assert np.array_equal(np.c_[pv["x"], pv["y"], pv["z"]], v) and np.array_equal(pf, f.astype(np.int32))
+    assert np.array_equal(np.c_[pv["nx"], pv["ny"], pv["nz"]], vn)
     assert (tmp_path / "pointnormals.ply").exists()
+
+
+@pytest.mark.gpu
+def test_cli_colours(built, tmp_path):
+    """A .pts with r g b columns (AsciiIO autodetection; the first line is
+    skipped): the PLY carries red green blue per vertex, the colour of the
+    vertex's nearest point."""
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    cli, _ = built
+    P = synthetic.spheres_tori(30_000, seed=14)
+    rng = np.random.Generator(np.random.PCG64(3))
+    C = rng.integers(0, 256, size=(len(P), 3))
+    src = tmp_path / "scan.pts"
+    with open(src, "w") as fh:
+        fh.write("x y z r g b\n")
+        for p, c in zip(P.tolist(), C.tolist()):
+            fh.write("%.9g %.9g %.9g %d %d %d\n" % (*p, *c))
+    out = tmp_path / "mesh.ply"
+    r = subprocess.run([str(cli), str(src), "-v", "0.02", "--nem", "3", "--outputFile", str(out)], capture_output=True,
+                       text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    pv, _ = read_ply_mesh(out)
+    assert pv.dtype.names == ("x", "y", "z", "red", "green", "blue", "nx", "ny", "nz")
+    pts = np.loadtxt(src, skiprows=1, dtype=np.float64)
+    with lvr2_gb300.Surface(pts[:, :3].astype(np.float32), kn=10, ki=10, kd=5, nem=3, flip_point=(0, 0, 0)) as s:
+        s.calculate_normals()
+        s.reconstruct(voxelsize=0.02, decomposition="PMC")
+        s.optimize_planar_faces(5)
+        v, _, _ = s.mesh(with_edges=False)
+        vc = s.vertex_colors(pts[:, 3:].astype(np.uint8))
+    assert np.array_equal(np.c_[pv["x"], pv["y"], pv["z"]], v)
+    assert np.array_equal(np.c_[pv["red"], pv["green"], pv["blue"]], vc)
