@@ -399,7 +399,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArg
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
-    const unsigned lt = (1u << lane) - 1u;
     const int nq = A.nq_dev ? int(*A.nq_dev) : A.nq;
     TravStats st;
     for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < nq;
