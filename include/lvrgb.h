@@ -151,6 +151,15 @@ lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]);
 lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, uint32_t* idx, float* dist,
                        int32_t* count, int32_t on_device, void* stream);
 
+/* SearchTree::radiusSearch (include/lvr2/reconstruction/SearchTree.hpp:86,
+ * SearchKDTree::radiusSearch in include/lvr2/algorithm/KDTree.tcc:368-380): up
+ * to k nearest points with distance below radius, for nq queries; rows as in
+ * lvrgb_knn (ascending (d2, index), idx 0xffffffff and dist +inf padding;
+ * count = points found).  Canonical test: float d2 < radius * radius (the
+ * reference compares double d2 with a double radius^2). */
+lvrgb_status lvrgb_radius_search(lvrgb_surface s, const float* q, int64_t nq, int32_t k, float radius,
+                                 uint32_t* idx, float* dist, int32_t* count, int32_t on_device, void* stream);
+
 /* AdaptiveKSearchSurface::distance for nq positions
  * (AdaptiveKSearchSurface.tcc:414-457, PointsetSurface.hpp:74-75): projected
  * and Euclidean distance to the mean of the kd nearest points along their

@@ -518,6 +518,32 @@ lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, u
     });
 }
 
+lvrgb_status lvrgb_radius_search(lvrgb_surface s, const float* q, int64_t nq, int32_t k, float radius,
+                                 uint32_t* idx, float* dist, int32_t* count, int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(k > 0 && k <= (1 << 16), LVRGB_ERR_INVALID_ARGUMENT, "k must be in 1..65536");
+        const float r2 = radius * radius;
+        require(radius > 0.0f && r2 > 0.0f && r2 < FLT_MAX, LVRGB_ERR_INVALID_ARGUMENT,
+                "radius must be > 0 with a finite, nonzero square");
+        require(nq == 0 || (q && idx && dist), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float4* qs = prepare_queries(s, q, nq, on_device, st);
+        const size_t rows = size_t(nq) * size_t(k);
+        uint32_t* di = stage_out(s->ws, "api.idx", idx, rows, on_device);
+        float* dd = stage_out(s->ws, "api.dist", dist, rows, on_device);
+        int32_t* dc = count ? stage_out(s->ws, "api.cnt", count, size_t(nq), on_device) : nullptr;
+        knn_rows(s->T, qs, int(nq), k, di, dd, dc, s->ws, s->d_err, st, r2);
+        finish_out(idx, di, rows, on_device, st);
+        finish_out(dist, dd, rows, on_device, st);
+        if (count) finish_out(count, dc, size_t(nq), on_device, st);
+        if (!on_device) check_kernel_error(s, st);
+    });
+}
+
 lvrgb_status lvrgb_distance(lvrgb_surface s, const float* q, int64_t nq, float* projected, float* euclidean,
                             int32_t on_device, void* stream) {
     return guarded([&] {

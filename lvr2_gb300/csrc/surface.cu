@@ -830,6 +830,7 @@ struct RowsArgs {
     float* nout;
     unsigned long long* gheap;
     int* err;
+    float radius2 = INFINITY;  // radius search: only d2 < radius2 (strict)
 };
 
 __device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, float4 q) {
@@ -882,6 +883,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
         LaneHeap heap;
         heap.init(ctx.heap, A.K);
+        // radius search: keys below (radius2, index 0) are those with d2 < radius2
+        if (A.radius2 < FLT_MAX) heap.top = make_key(A.radius2, 0u);
         const float4 q0 = A.qs[tile * 32];
         const int seed = seed_bucket_for(A.T, q0.x, q0.y, q0.z);
         knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, seed);
@@ -902,6 +905,9 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) rows_wide_kernel(RowsArgs 
     W.keys = A.gheap ? A.gheap + (size_t(blockIdx.x) * kWideWarps + wib) * size_t(W.cap)
                      : reinterpret_cast<unsigned long long*>(smem + kWideWarps * 1024) + size_t(wib) * W.cap;
     const float inf = __int_as_float(0x7f800000);
+    // radius search (radius2 > 0): the largest float below radius2, so that
+    // d2 <= limit exactly when d2 < radius2
+    const float limit = A.radius2 < FLT_MAX ? __int_as_float(__float_as_int(A.radius2) - 1) : inf;
     TravStats st;
     for (int tile = blockIdx.x * kWideWarps + wib; tile * TQ < A.nq; tile += gridDim.x * kWideWarps) {
         const int nt = min(TQ, A.nq - tile * TQ);
@@ -917,10 +923,11 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) rows_wide_kernel(RowsArgs 
                 bound = __fmul_rn(__fmul_rn(r, r), 1.0000038f);
             }
             const int seed = seed_bucket_for(A.T, q.x, q.y, q.z);
+            bound = fminf(bound, limit);
             for (int attempt = 0; attempt < 2; attempt++) {
                 wide_knn(A.T, q.x, q.y, q.z, W, A.err, st, seed, 0, 0, 0x7fffffff, bound);
-                if (W.cnt >= W.K || !(bound < FLT_MAX)) break;
-                bound = inf;
+                if (W.cnt >= W.K || !(bound < limit)) break;
+                bound = limit;
             }
             const int cnt = W.cnt;
             const size_t row = __float_as_uint(q.w);
@@ -1286,9 +1293,10 @@ void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Worksp
 }
 
 void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
-              Workspace& ws, int* d_err, cudaStream_t s) {
+              Workspace& ws, int* d_err, cudaStream_t s, float radius2) {
     if (nq == 0 || k <= 0) return;
     RowsArgs A;
+    A.radius2 = radius2;
     A.T = T;
     A.K = k;
     A.qs = qs;

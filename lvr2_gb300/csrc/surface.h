@@ -56,8 +56,9 @@ void sort_queries(const float* q, int nq, const float* d_box, float4* qs, Worksp
 
 // k nearest neighbours for sorted queries; rows (by qs[i].w) of idx (original
 // indices, 0xffffffff padding) and dist (sqrt of d2, +inf padding), ascending.
+// radius2 (> 0): only points with d2 < radius2 (a radius search).
 void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, float* dist, int32_t* count,
-              Workspace& ws, int* d_err, cudaStream_t s);
+              Workspace& ws, int* d_err, cudaStream_t s, float radius2 = INFINITY);
 
 // knn_rows with the heaps in shared memory only (k <= kSmemHeapMax) and no
 // workspace: allocates nothing.

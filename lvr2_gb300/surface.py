@@ -191,6 +191,19 @@ class Surface:
                                     self._stream))
         return idx, dist, cnt
 
+    def radius_search(self, queries, k, radius):
+        """SearchTree::radiusSearch: up to k nearest points with distance
+        below radius (host arrays): idx, dist (padded), count."""
+        q, on_dev = _f32x3(queries)
+        if on_dev:
+            raise ValueError("use host arrays with radius_search()")
+        idx = np.empty((len(q), k), np.uint32)
+        dist = np.empty((len(q), k), np.float32)
+        cnt = np.empty(len(q), np.int32)
+        check(_lib.load().lvrgb_radius_search(self._h, _ptr(q), len(q), int(k), float(radius), _ptr(idx), _ptr(dist),
+                                              _ptr(cnt), 0, self._stream))
+        return idx, dist, cnt
+
     def distance(self, queries):
         q, on_dev = _f32x3(queries)
         proj = np.empty(len(q), np.float32)
