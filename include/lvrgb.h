@@ -151,6 +151,17 @@ lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]);
 lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, uint32_t* idx, float* dist,
                        int32_t* count, int32_t on_device, void* stream);
 
+/* LBVHIndex::calculate_normals (src/liblvr2/reconstruction/cuda/LBVHIndex.cu:586-642,
+ * lbvh/normals_kernel.cu:11-180): the nem 4 plane fit from given neighbour
+ * lists.  queries: nq x 3; n_neighbors[nq] (<= k); indices: nq x k input
+ * indices of this surface's points, the first n_neighbors of each row used,
+ * slot 0 taken as the query itself and left out.  Flipped toward the
+ * surface's flip point (the comparator's default is (1e6, 1e6, 1e6)).  A count
+ * above k or a used index >= n is LVRGB_ERR_INVALID_ARGUMENT. */
+lvrgb_status lvrgb_normals_from_neighbors(lvrgb_surface s, const float* queries, int64_t nq, int32_t k,
+                                          const uint32_t* n_neighbors, const uint32_t* indices, float* normals,
+                                          int32_t on_device, void* stream);
+
 /* SearchTree::radiusSearch (include/lvr2/reconstruction/SearchTree.hpp:86,
  * SearchKDTree::radiusSearch in include/lvr2/algorithm/KDTree.tcc:368-380): up
  * to k nearest points with distance below radius, for nq queries; rows as in

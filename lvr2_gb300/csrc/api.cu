@@ -518,6 +518,32 @@ lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, u
     });
 }
 
+lvrgb_status lvrgb_normals_from_neighbors(lvrgb_surface s, const float* queries, int64_t nq, int32_t k,
+                                          const uint32_t* n_neighbors, const uint32_t* indices, float* normals,
+                                          int32_t on_device, void* stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
+        require(k > 0 && k <= (1 << 16), LVRGB_ERR_INVALID_ARGUMENT, "k must be in 1..65536");
+        require(nq == 0 || (queries && n_neighbors && indices && normals), LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        if (nq == 0) return;
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        const float* dq = stage_in(s->ws, "lists.q", queries, size_t(nq) * 3, on_device, st);
+        const uint32_t* dc = stage_in(s->ws, "lists.c", n_neighbors, size_t(nq), on_device, st);
+        const uint32_t* di = stage_in(s->ws, "lists.i", indices, size_t(nq) * size_t(k), on_device, st);
+        uint32_t ext[2];
+        list_extent(dc, di, int(nq), k, s->ws, ext, st);
+        require(ext[0] <= uint32_t(k), LVRGB_ERR_INVALID_ARGUMENT, "a neighbour count exceeds k");
+        require(ext[1] < uint32_t(s->T.n), LVRGB_ERR_INVALID_ARGUMENT, "a neighbour index is out of range");
+        const NormalsConfig c = normals_config(s);
+        float* dn = stage_out(s->ws, "lists.n", normals, size_t(nq) * 3, on_device);
+        normals_from_lists(s->T, dq, int(nq), k, dc, di, c.flip, dn, st);
+        finish_out(normals, dn, size_t(nq) * 3, on_device, st);
+        check_kernel_error(s, st);
+    });
+}
+
 lvrgb_status lvrgb_radius_search(lvrgb_surface s, const float* q, int64_t nq, int32_t k, float radius,
                                  uint32_t* idx, float* dist, int32_t* count, int32_t on_device, void* stream) {
     return guarded([&] {

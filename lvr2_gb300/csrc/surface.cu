@@ -2,6 +2,7 @@
 // calculateSurfaceNormals), normal interpolation, kNN rows and
 // getInterpolatedNormal, all on the warp-cooperative LBVH traversal.
 #include <algorithm>
+#include <cstring>
 #include <stdexcept>
 
 #include "primitives.cuh"
@@ -335,21 +336,23 @@ __device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& 
 // point; a NaN or infinite flip product, or fewer than 3 neighbours, gives the
 // zero normal.  Every operation is rounded on its own (no contraction), in
 // the reference's order.  Neighbours in ascending (d2, index) order.
-__device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, float fx,
-                                                float fy, float fz, float n[3]) {
+// point(s): the s-th neighbour (float4; s in 1..cnt-1).
+template <class Point>
+__device__ __forceinline__ void lbvh_plane_fit(Point point, int cnt, float qx, float qy, float qz, float fx, float fy,
+                                               float fz, float n[3]) {
     n[0] = n[1] = n[2] = 0.0f;
     if (cnt < 3) return;
     const double nf = __dsub_rn(double(cnt), 1.0);
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int s = 1; s < cnt; s++) {
-        const float4 p = neighbour_point(T, heap.at(s));
+        const float4 p = point(s);
         sx = __dadd_rn(sx, __ddiv_rn(double(p.x), nf));
         sy = __dadd_rn(sy, __ddiv_rn(double(p.y), nf));
         sz = __dadd_rn(sz, __ddiv_rn(double(p.z), nf));
     }
     double xx = 0.0, xy = 0.0, xz = 0.0, yy = 0.0, yz = 0.0, zz = 0.0;
     for (int s = 1; s < cnt; s++) {
-        const float4 p = neighbour_point(T, heap.at(s));
+        const float4 p = point(s);
         const double rx = __dsub_rn(double(p.x), sx), ry = __dsub_rn(double(p.y), sy), rz = __dsub_rn(double(p.z), sz);
         xx = __dadd_rn(xx, __ddiv_rn(__dmul_rn(rx, rx), nf));
         xy = __dadd_rn(xy, __ddiv_rn(__dmul_rn(rx, ry), nf));
@@ -380,8 +383,8 @@ __device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& h
     wx = __ddiv_rn(wx, mag);
     wy = __ddiv_rn(wy, mag);
     wz = __ddiv_rn(wz, mag);
-    const double dx = __dsub_rn(double(fx), double(q.x)), dy = __dsub_rn(double(fy), double(q.y)),
-                 dz = __dsub_rn(double(fz), double(q.z));
+    const double dx = __dsub_rn(double(fx), double(qx)), dy = __dsub_rn(double(fy), double(qy)),
+                 dz = __dsub_rn(double(fz), double(qz));
     const double scalar = __dadd_rn(__dadd_rn(__dmul_rn(dx, wx), __dmul_rn(dy, wy)), __dmul_rn(dz, wz));
     if (!(scalar <= 0.0 || scalar >= 0.0) || isinf(scalar)) {
         wx = 0.0; wy = 0.0; wz = 0.0;
@@ -392,6 +395,29 @@ __device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& h
     n[0] = float(wx);
     n[1] = float(wy);
     n[2] = float(wz);
+}
+
+__device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, float fx,
+                                                float fy, float fz, float n[3]) {
+    lbvh_plane_fit([&](int s) { return neighbour_point(T, heap.at(s)); }, cnt, q.x, q.y, q.z, fx, fy, fz, n);
+}
+
+// LBVHIndex::calculate_normals (src/liblvr2/reconstruction/cuda/LBVHIndex.cu:586-642,
+// lbvh/normals_kernel.cu:11-180): the same fit from given neighbour lists,
+// one thread per query.  idx rows of k input indices (checked < n by the
+// caller), cnt[i] <= k of them used; the query position comes from queries.
+__global__ void list_normals_kernel(Lbvh T, const float* __restrict__ queries, int nq, int k,
+                                    const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ idx, float fx,
+                                    float fy, float fz, float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const uint32_t* row = idx + size_t(i) * size_t(k);
+    float n[3];
+    lbvh_plane_fit([&](int s) { return __ldg(T.pts + __ldg(T.inv + row[s])); }, int(cnt[i]),
+                   queries[3 * size_t(i)], queries[3 * size_t(i) + 1], queries[3 * size_t(i) + 2], fx, fy, fz, n);
+    out[3 * size_t(i)] = n[0];
+    out[3 * size_t(i) + 1] = n[1];
+    out[3 * size_t(i) + 2] = n[2];
 }
 
 template <int kNem>
@@ -1370,6 +1396,42 @@ void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, cons
     A.gheap = P.gheap;
     set_smem(rows_kernel, P.smem);
     rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    LVRGB_LAUNCH_CHECK();
+}
+
+namespace {
+// Largest count and largest used index of neighbour lists (out[0], out[1]).
+__global__ void list_extent_kernel(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ idx, int nq, int k,
+                                   uint32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const uint32_t c = cnt[i];
+    uint32_t m = 0;
+    const uint32_t used = c < uint32_t(k) ? c : uint32_t(k);
+    for (uint32_t s = 0; s < used; s++) m = max(m, idx[size_t(i) * size_t(k) + s]);
+    atomicMax(out, c);
+    atomicMax(out + 1, m);
+}
+}  // namespace
+
+void list_extent(const uint32_t* cnt, const uint32_t* idx, int nq, int k, Workspace& ws, uint32_t out[2],
+                 cudaStream_t s) {
+    out[0] = out[1] = 0;
+    if (nq == 0) return;
+    uint32_t* d = ws.get<uint32_t>("lists.extent", 2);
+    LVRGB_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(uint32_t), s));
+    list_extent_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(cnt, idx, nq, k, d);
+    LVRGB_LAUNCH_CHECK();
+    uint64_t* h = ws.pinned();
+    LVRGB_CUDA(cudaMemcpyAsync(h, d, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    LVRGB_CUDA(cudaStreamSynchronize(s));
+    std::memcpy(out, h, 2 * sizeof(uint32_t));
+}
+
+void normals_from_lists(const Lbvh& T, const float* queries, int nq, int k, const uint32_t* cnt, const uint32_t* idx,
+                        const float flip[3], float* out, cudaStream_t s) {
+    if (nq == 0) return;
+    list_normals_kernel<<<ceil_div(nq, 128), 128, 0, s>>>(T, queries, nq, k, cnt, idx, flip[0], flip[1], flip[2], out);
     LVRGB_LAUNCH_CHECK();
 }
 

@@ -69,6 +69,16 @@ void knn_rows_smem(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx
 void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, const float4* qs, int nq,
                               float* out, Workspace& ws, int* d_err, cudaStream_t s);
 
+// LBVHIndex::calculate_normals: the nem 4 fit from given neighbour lists
+// (device arrays: queries nq x 3, cnt[nq] <= k, idx nq x k input indices < T.n,
+// slot 0 left out as the query itself), flipped toward flip; out nq x 3.
+void normals_from_lists(const Lbvh& T, const float* queries, int nq, int k, const uint32_t* cnt, const uint32_t* idx,
+                        const float flip[3], float* out, cudaStream_t s);
+// out[0] = the largest count, out[1] = the largest index among the used
+// entries (first min(cnt, k) of each row) of device neighbour lists.
+void list_extent(const uint32_t* cnt, const uint32_t* idx, int nq, int k, Workspace& ws, uint32_t out[2],
+                 cudaStream_t s);
+
 // Common launch plan for the per-lane heaps: heaps of up to kSmemHeapMax
 // entries live in shared memory, larger ones in a global scratch buffer.
 constexpr int kWarpsPerBlock = 4;

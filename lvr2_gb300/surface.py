@@ -191,6 +191,17 @@ class Surface:
                                     self._stream))
         return idx, dist, cnt
 
+    def normals_from_neighbors(self, queries, n_neighbors, indices):
+        """LBVHIndex::calculate_normals: the nem 4 fit of given neighbour lists
+        (indices (nq, k) of this surface's points, n_neighbors (nq,))."""
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(len(q), -1)
+        cnt = np.ascontiguousarray(n_neighbors, np.uint32).reshape(len(q))
+        out = np.empty((len(q), 3), np.float32)
+        check(_lib.load().lvrgb_normals_from_neighbors(self._h, _ptr(q), len(q), idx.shape[1], _ptr(cnt), _ptr(idx),
+                                                       _ptr(out), 0, self._stream))
+        return out
+
     def radius_search(self, queries, k, radius):
         """SearchTree::radiusSearch: up to k nearest points with distance
         below radius (host arrays): idx, dist (padded), count."""

@@ -202,17 +202,25 @@ def _recon_result(h):
 def lbvh_knn_normals(surface, kn, flip=(1e6, 1e6, 1e6)):
     """The plane fit of lvr2's LBVH comparator, LBVHIndex::knn_normals
     (src/liblvr2/reconstruction/cuda/lbvh/knn_normals_kernel.cu:54-206), over
-    the canonical kNN(kn) of every point (ascending (d2, index); slot 0, the
-    query itself, is left out): FP64 centroid and covariance with each term
-    divided by n - 1 before it is added, the det^2-weighted, sign-aligned sum
-    of the three cofactor axes, normalised, flipped toward `flip`; fewer than 3
-    neighbours or a NaN / infinite flip product give the zero normal.  numpy
-    float64 rounds every operation on its own, in the kernel's order."""
-    P = surface.points.astype(np.float64)
+    the canonical kNN(kn) of every point (ascending (d2, index))."""
     idx, _, cnt = surface.knn(surface.points, kn)
-    idx = idx.astype(np.int64)
-    m = len(P)
-    n = cnt.astype(np.int64)
+    return lbvh_fit_lists(surface.points, surface.points, idx, cnt, flip)
+
+
+def lbvh_fit_lists(points, queries, idx, cnt, flip=(1e6, 1e6, 1e6)):
+    """LBVHIndex::calculate_normals (lbvh/normals_kernel.cu:11-180) and the
+    fit of knn_normals: for each query, neighbours idx[i, 1:cnt[i]] (slot 0,
+    the query itself, is left out); FP64 centroid and covariance with each
+    term divided by n - 1 before it is added, the det^2-weighted, sign-aligned
+    sum of the three cofactor axes, normalised, flipped toward `flip`; fewer
+    than 3 neighbours or a NaN / infinite flip product give the zero normal.
+    numpy float64 rounds every operation on its own, in the kernel's order."""
+    P = np.asarray(points, np.float32).astype(np.float64)
+    Qp = np.asarray(queries, np.float32).astype(np.float64).reshape(-1, 3)
+    idx = np.asarray(idx).astype(np.int64).reshape(len(Qp), -1)
+    kn = idx.shape[1]
+    m = len(Qp)
+    n = np.asarray(cnt).astype(np.int64).reshape(m)
     nf = n.astype(np.float64) - 1.0
     ok = n >= 3
     sx = np.zeros(m); sy = np.zeros(m); sz = np.zeros(m)
@@ -253,8 +261,8 @@ def lbvh_knn_normals(surface, kn, flip=(1e6, 1e6, 1e6)):
         add_axis(xy * yz - xz * yy, xy * xz - yz * xx, det_z, det_z)
         mag = np.sqrt((w[:, 0] * w[:, 0] + w[:, 1] * w[:, 1]) + w[:, 2] * w[:, 2])
         w = w / mag[:, None]
-        f = np.asarray(flip, np.float32).astype(np.float64)
-        d = f[None, :] - P
+        fl = np.asarray(flip, np.float32).astype(np.float64)
+        d = fl[None, :] - Qp
         scalar = (d[:, 0] * w[:, 0] + d[:, 1] * w[:, 1]) + d[:, 2] * w[:, 2]
     bad = ~np.isfinite(scalar)
     w[bad] = 0.0

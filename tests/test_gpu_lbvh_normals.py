@@ -81,3 +81,34 @@ def test_k_limit(gb):
         with pytest.raises(gb.LvrgbError) as e:
             s.calculate_normals()
         assert e.value.status == 1
+
+
+def test_normals_from_neighbor_lists(gb, oracle_mod):
+    """LBVHIndex::calculate_normals: the fit of given lists, with the rows in
+    the given order (the sums follow it), padded rows and counts below k."""
+    from lvr2_gb300 import synthetic
+    P = synthetic.spheres_tori(50_000, seed=21)
+    rng = np.random.Generator(np.random.PCG64(5))
+    Q = P[rng.integers(0, len(P), 4000)] + rng.normal(scale=1e-3, size=(4000, 3)).astype(np.float32)
+    o = oracle_mod.OracleSurface(P)
+    idx, _, cnt = o.knn(Q, 24)
+    idx = idx.copy()
+    perm = rng.permuted(np.tile(np.arange(1, 24), (len(Q), 1)), axis=1)  # shuffle slots 1..23 per row
+    idx[:, 1:] = np.take_along_axis(idx[:, 1:], perm - 1, axis=1)
+    cnt = cnt.astype(np.uint32)
+    cnt[::7] = rng.integers(0, 24, len(cnt[::7]))  # shorter lists, some below 3
+    idx[1::5, 20:] = 0xFFFFFFFF  # padding past the count is never read
+    cnt[1::5] = np.minimum(cnt[1::5], 20)
+    flip = (0.3, -2.0, 5.0)
+    with gb.Surface(P, kn=10, ki=0, kd=5, nem=4, flip_point=flip) as s:
+        got = s.normals_from_neighbors(Q, cnt, idx)
+        bad = idx.copy()
+        bad[3, 2] = len(P)
+        with pytest.raises(gb.LvrgbError) as e:
+            s.normals_from_neighbors(Q, cnt, bad)
+        assert e.value.status == 1
+        with pytest.raises(gb.LvrgbError):
+            s.normals_from_neighbors(Q, np.full(len(Q), 25, np.uint32), idx)
+    ref = oracle_mod.lbvh_fit_lists(P, Q, np.where(idx == 0xFFFFFFFF, 0, idx), cnt, flip=flip)
+    assert np.array_equal(got, ref)
+    assert not got[cnt < 3].any()
