@@ -352,6 +352,13 @@ lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]);
  * no lvr2 counterpart). */
 lvrgb_status lvrgb_kernel_launches(uint64_t* out);
 
+/* Fault injection for tests of the out-of-memory path that lvr2's large-scale
+ * tool handles (LargeScaleReconstruction.tcc:647-671): the n-th device
+ * allocation from now on (through any handle's workspace) fails with
+ * LVRGB_ERR_OUT_OF_MEMORY, on the host, without touching the GPU.  n <= 0
+ * turns it off.  The handle stays usable after such a failure. */
+lvrgb_status lvrgb_debug_fail_allocation(int64_t n);
+
 /* k nearest neighbours of nq queries among n points WITHOUT ANY DEVICE
  * ALLOCATION.  No counterpart in lvr2: it exists for callers that cannot
  * call cudaMalloc during a call (real-time loops or driver callbacks where an

@@ -14,6 +14,7 @@
 #include "adjoint.h"
 #include "grid.h"
 #include "meshops.h"
+#include "nvtx.h"
 #include "planar.h"
 #include "lbvh_build.h"
 #include "primitives.cuh"
@@ -379,6 +380,7 @@ lvrgb_status lvrgb_surface_num_points(lvrgb_surface s, int64_t* n) {
 
 lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.calculate_normals");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         DeviceScope dev(s->device);
         cudaStream_t st = as_stream(stream);
@@ -411,6 +413,7 @@ lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
 
 lvrgb_status lvrgb_interpolate_normals(lvrgb_surface s, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.interpolate_normals");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(s->cfg.ki > 0, LVRGB_ERR_INVALID_ARGUMENT, "ki must be > 0");
@@ -498,6 +501,7 @@ lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]) {
 lvrgb_status lvrgb_knn(lvrgb_surface s, const float* q, int64_t nq, int32_t k, uint32_t* idx, float* dist,
                        int32_t* count, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.knn");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
         require(k > 0 && k <= (1 << 16), LVRGB_ERR_INVALID_ARGUMENT, "k must be in 1..65536");
@@ -547,6 +551,7 @@ lvrgb_status lvrgb_normals_from_neighbors(lvrgb_surface s, const float* queries,
 lvrgb_status lvrgb_radius_search(lvrgb_surface s, const float* q, int64_t nq, int32_t k, float radius,
                                  uint32_t* idx, float* dist, int32_t* count, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.radius_search");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
         require(k > 0 && k <= (1 << 16), LVRGB_ERR_INVALID_ARGUMENT, "k must be in 1..65536");
@@ -573,6 +578,7 @@ lvrgb_status lvrgb_radius_search(lvrgb_surface s, const float* q, int64_t nq, in
 lvrgb_status lvrgb_distance(lvrgb_surface s, const float* q, int64_t nq, float* projected, float* euclidean,
                             int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.distance");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
@@ -594,6 +600,7 @@ lvrgb_status lvrgb_distance_adjoint(lvrgb_surface s, const float* q, int64_t nq,
                                     const float* grad_euclidean, float* projected, float* euclidean, float* grad_q,
                                     float* grad_points, float* grad_normals, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.distance_adjoint");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
@@ -638,6 +645,7 @@ lvrgb_status lvrgb_distance_adjoint(lvrgb_surface s, const float* q, int64_t nq,
 lvrgb_status lvrgb_project_to_surface(lvrgb_surface s, const float* v, int64_t nv, int32_t steps,
                                       float* out_positions, float* out_normals, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.project_to_surface");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(nv >= 0 && nv < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "position count out of range");
@@ -662,6 +670,7 @@ lvrgb_status lvrgb_project_to_surface(lvrgb_surface s, const float* v, int64_t n
 lvrgb_status lvrgb_grid_distances(lvrgb_surface s, const float* q, int64_t nq, float voxel_size, float* distance,
                                   uint8_t* invalid, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.grid_distances");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(nq >= 0 && nq < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "query count out of range");
@@ -702,6 +711,7 @@ lvrgb_status lvrgb_interpolated_normal(lvrgb_surface s, const float* q, int64_t 
 
 lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrgb_mesh_info* info, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.reconstruct");
         require(s != nullptr && g != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(g->resolution > 0, LVRGB_ERR_INVALID_ARGUMENT, "resolution must be > 0");
@@ -739,6 +749,7 @@ lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t 
                                      int32_t nchunks, const float* inner_boxes, lvrgb_mesh_info* info,
                                      int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.reconstruct_cells");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(voxel_size > 0 && std::isfinite(voxel_size), LVRGB_ERR_INVALID_ARGUMENT, "voxel size must be > 0");
         require(decomposition == 0 || decomposition == 1, LVRGB_ERR_UNSUPPORTED,
@@ -791,6 +802,7 @@ lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t 
 
 lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* moved, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.optimize_planar_faces");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
         require(kc >= 1 && kc <= kSmemHeapMax, LVRGB_ERR_INVALID_ARGUMENT, "kc must be in 1..96");
@@ -804,6 +816,7 @@ lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* m
 
 lvrgb_status lvrgb_mesh_vertex_normals(lvrgb_surface s, float* vertex_normals, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.mesh_vertex_normals");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
         const size_t nv = size_t(s->grid.nverts);
@@ -842,6 +855,7 @@ lvrgb_status lvrgb_vertex_normals(lvrgb_surface s, const float* vertices, int64_
                                   int64_t nf, float* vertex_normals, int64_t* nearest_count, int32_t on_device,
                                   void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.vertex_normals");
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
         require(nv >= 0 && nv < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "vertex count out of range");
@@ -1025,6 +1039,11 @@ lvrgb_status lvrgb_kernel_launches(uint64_t* out) {
     return LVRGB_OK;
 }
 
+lvrgb_status lvrgb_debug_fail_allocation(int64_t n) {
+    alloc_fault_countdown().store(n > 0 ? n : 0);
+    return LVRGB_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1157,6 +1176,7 @@ lvrgb_status lvrgb_batch_destroy(lvrgb_batch b) {
 
 lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.batch_calculate_normals");
         require(b != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "batch is NULL");
         DeviceScope dev(b->device);
         cudaStream_t caller = as_stream(stream);
@@ -1214,6 +1234,7 @@ lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_d
 lvrgb_status lvrgb_batch_grid_distances(lvrgb_batch b, const float* q, const int64_t* q_offsets, float voxel_size,
                                         float* distance, uint8_t* invalid, int32_t on_device, void* stream) {
     return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.batch_grid_distances");
         require(b != nullptr && q_offsets != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
         require(b->ran, LVRGB_ERR_STATE, "no normals: call lvrgb_batch_calculate_normals");
         require(voxel_size > 0, LVRGB_ERR_INVALID_ARGUMENT, "voxel_size must be > 0");

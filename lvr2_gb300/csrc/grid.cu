@@ -8,10 +8,12 @@
 // vertices form the 32-query groups of the signed-distance kNN.
 #include <algorithm>
 #include <climits>
+#include <optional>
 #include <cmath>
 #include <stdexcept>
 
 #include "grid.h"
+#include "nvtx.h"
 #include "primitives.cuh"
 #include "surface.h"
 
@@ -534,6 +536,8 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
                       GridResult& R, int* d_err, cudaStream_t s, GridTimings* timings) {
     StageTimer timer(timings != nullptr);
     timer.mark(0, s);
+    std::optional<NvtxRange> stage;
+    stage.emplace("lvrgb.grid_build");
     R = GridResult();
     // HashGrid ctor (HashGrid.tcc:48-52)
     const float longest = std::max({bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2]});
@@ -646,6 +650,7 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
         LVRGB_LAUNCH_CHECK();
     }
     timer.mark(1, s);
+    stage.emplace("lvrgb.signed_distance");
 
     // ---- signed distance at every grid vertex (calcDistanceValues) -------
     R.qp_dist = ws.get<float>("grid.qp_dist", nqp);
@@ -653,6 +658,7 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     R.qp_invalid = ws.get<uint8_t>("grid.qp_invalid", nqp);
     signed_distance_rows(T, normals, cfg.kd, qpos, int(nqp), vs, R.qp_dist, R.qp_eucl, R.qp_invalid, ws, d_err, s);
     timer.mark(2, s);
+    stage.emplace("lvrgb.culling");
 
     // ---- remove cells with an invalid corner (PointsetGrid.tcc:153-184) --
     uint32_t* vflags = ws.get<uint32_t>("grid.vflags", nc);
@@ -672,9 +678,11 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     R.ncells_valid = (long long)nvalid;
     R.valid_cells = valid;
     timer.mark(3, s);
+    stage.emplace("lvrgb.marching_cubes");
 
     mc_stage(R, F, kbits, cfg.decomposition, ws, s);
     timer.mark(4, s);
+    stage.reset();
     timer.finish(timings, s);
 }
 

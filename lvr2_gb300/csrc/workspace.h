@@ -2,12 +2,28 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <unordered_map>
 
 #include "common.cuh"
 
 namespace lvrgb {
+
+// Host-side allocation fault injection (lvrgb_debug_fail_allocation): when
+// the countdown reaches zero, that device allocation of a workspace fails as
+// cudaErrorMemoryAllocation without calling the driver.  0 = off.
+inline std::atomic<long long>& alloc_fault_countdown() {
+    static std::atomic<long long> c{0};
+    return c;
+}
+inline bool alloc_fault_due() {
+    long long c = alloc_fault_countdown().load();
+    while (c > 0) {
+        if (alloc_fault_countdown().compare_exchange_weak(c, c - 1)) return c == 1;
+    }
+    return false;
+}
 
 class Workspace {
   public:
@@ -38,6 +54,7 @@ class Workspace {
             e.bytes = 0;
             size_t want = bytes + bytes / 8;  // headroom for slightly larger calls
             want = (want + 255) & ~size_t(255);
+            if (alloc_fault_due()) throw CudaError{cudaErrorMemoryAllocation, __FILE__, __LINE__};
             LVRGB_CUDA(cudaMalloc(&e.ptr, want));
             e.bytes = want;
         }

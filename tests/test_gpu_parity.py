@@ -303,3 +303,34 @@ def test_calculate_normals_interpolation_bit_exact(gb, oracle_mod, kn, ki):
         final = s.normals()
     ref = o.interpolate(raw, ki)
     assert np.array_equal(final, ref, equal_nan=True)
+
+
+@pytest.mark.parametrize("extrude", [True, False])
+@pytest.mark.parametrize("intersections", [40, 97])
+def test_intersections_and_extrusion_against_oracle(gb, oracle_mod, extrude, intersections):
+    """--intersections (voxel size = longest side / intersections) and
+    --noExtrusion: cells, grid values and mesh equal the oracle's."""
+    from lvr2_gb300 import synthetic
+    P = synthetic.spheres_tori(30_000, seed=22)
+    o = oracle_mod.OracleSurface(P)
+    normals = o.normals(10, nem=3)
+    with gb.Surface(P, kd=6) as s:
+        s.set_normals(normals)
+        info = s.reconstruct(intersections=intersections, extrude=extrude, decomposition="PMC")
+        cells_all, _ = s.cells()
+        lat, pos, dist, inv = s.grid()
+        v, f, e = s.mesh()
+    r = o.reconstruct(normals, intersections=intersections, extrude=extrude, kd=6, decomposition="PMC")
+    assert np.float32(info.voxelsize) == np.float32(r["voxelsize"])
+    ca = cells_all[np.lexsort((cells_all[:, 2], cells_all[:, 1], cells_all[:, 0]))]
+    rc = r["cells_all"][np.lexsort((r["cells_all"][:, 2], r["cells_all"][:, 1], r["cells_all"][:, 0]))]
+    assert np.array_equal(ca, rc)
+    order = np.lexsort((lat[:, 2], lat[:, 1], lat[:, 0]))
+    ro = np.lexsort((r["qp_lattice"][:, 2], r["qp_lattice"][:, 1], r["qp_lattice"][:, 0]))
+    assert np.array_equal(lat[order], r["qp_lattice"][ro])
+    assert np.array_equal(pos[order], r["qp_pos"][ro])
+    assert np.array_equal(dist[order], r["qp_dist"][ro])
+    assert np.array_equal(inv[order], r["qp_invalid"][ro])
+    a = canonical_mesh(e, v, f)
+    b = canonical_mesh(r["vkeys"], r["vpos"], r["faces"])
+    assert len(f) > 1000 and all(np.array_equal(x, y) for x, y in zip(a, b))
