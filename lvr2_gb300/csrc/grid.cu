@@ -207,7 +207,9 @@ __device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
 // AdaptiveKSearchSurface::distance (AdaptiveKSearchSurface.tcc:414-457) for
 // one query per lane, neighbours summed in ascending (d2, index) order, plus
 // the invalid rule of PointsetGrid::calcDistanceValues (PointsetGrid.tcc:133-140).
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_kernel(SdfArgs A) {
+// Nine resident blocks is what the shared memory allows at kd = 20; at that
+// bound the kernel may use 56 registers.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);

@@ -420,8 +420,10 @@ __global__ void list_normals_kernel(Lbvh T, const float* __restrict__ queries, i
     out[3 * size_t(i) + 2] = n[2];
 }
 
+// Five resident blocks is what the shared memory allows at k = 40 (2 kn for
+// kn = 20); at that bound the registers (up to 102) hold the kernel without spills.
 template <int kNem>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) normals_kernel(NormalsArgs A) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) normals_kernel(NormalsArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
