@@ -480,6 +480,16 @@ def run_gpu(args):
                      "traffic": int(dom["traffic"]) if dom["traffic"] else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2M-point capture, "
                                        "scaled per point (normals) or per grid vertex (signed distance)"},
+        # both kNN stages against the same HBM roofline; ncu shows them issue-bound
+        # (57% and 71% issue active), not bandwidth-bound
+        "stage_rooflines": [
+            {"stage": "normals", "kernel": "normals_kernel", "algorithmic_bytes": int(nb),
+             "achieved_gbs": nb / (normals_ms / 1000.0) / 1e9, "frac": nb / (normals_ms / 1000.0) / 1e9 / peak,
+             "traffic": int(NCU_DRAM_BYTES_PER_NORMAL * n)},
+            {"stage": "signed_distance", "kernel": "sdf_kernel", "algorithmic_bytes": int(sb),
+             "achieved_gbs": sb / (sdf_ms / 1000.0) / 1e9, "frac": sb / (sdf_ms / 1000.0) / 1e9 / peak,
+             "traffic": int(NCU_DRAM_BYTES_PER_SDF_VERTEX * nq)},
+        ],
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "e2e": e2e,
