@@ -81,7 +81,10 @@ void lvrgb_surface_config_default(lvrgb_surface_config* cfg);
  * include/lvr2/util/Factories.tcc:44-83; SearchKDTree ctor,
  * include/lvr2/algorithm/KDTree.tcc:317-329), PointsetSurface's bounding box
  * (include/lvr2/reconstruction/PointsetSurface.tcc:39-58) and
- * LBVHIndex::build (include/lvr2/reconstruction/cuda/LBVHIndex.hpp:114). */
+ * LBVHIndex::build (include/lvr2/reconstruction/cuda/LBVHIndex.hpp:114).
+ * A point with a NaN or infinite coordinate is LVRGB_ERR_INVALID_ARGUMENT (the
+ * same holds for lvrgb_surface_set_points and lvrgb_batch_create); a query
+ * with one has no neighbours. */
 lvrgb_status lvrgb_surface_create(const lvrgb_surface_config* cfg, const float* xyz, int64_t n,
                                   int32_t on_device, void* stream, lvrgb_surface* out);
 

@@ -3,6 +3,7 @@
 // extern "C" functions.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cstring>
 #include <mutex>
 #include <stdexcept>
@@ -241,12 +242,36 @@ void record(lvrgb_surface s, int i, cudaStream_t st) {
     LVRGB_CUDA(cudaEventRecord(s->ev[i], st));
 }
 
+__global__ void first_nonfinite_kernel(const float* __restrict__ xyz, int n, int* __restrict__ first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = xyz[3 * size_t(i)], y = xyz[3 * size_t(i) + 1], z = xyz[3 * size_t(i) + 2];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicMin(first, i);
+}
+
+// lvr2's trees order points by comparisons that NaN breaks: a point with a
+// non-finite coordinate is rejected (device array xyz, n x 3).
+void require_finite_points(Workspace& ws, const float* xyz, int64_t n, cudaStream_t st) {
+    if (n <= 0) return;
+    int* d_first = ws.get<int>("api.first_bad", 1);
+    const int init = INT_MAX;
+    LVRGB_CUDA(cudaMemcpyAsync(d_first, &init, sizeof(int), cudaMemcpyHostToDevice, st));
+    first_nonfinite_kernel<<<ceil_div(n, 256), 256, 0, st>>>(xyz, int(n), d_first);
+    LVRGB_LAUNCH_CHECK();
+    int first = INT_MAX;
+    LVRGB_CUDA(cudaMemcpyAsync(&first, d_first, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LVRGB_CUDA(cudaStreamSynchronize(st));
+    if (first != INT_MAX)
+        throw ApiError{LVRGB_ERR_INVALID_ARGUMENT, "point " + std::to_string(first) + " has a non-finite coordinate"};
+}
+
 // (Re)builds the search structure and bounding box of a handle.
 void build_points(lvrgb_surface s, const float* xyz, int64_t n, int on_device, cudaStream_t st) {
     require(n >= 0 && n < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "point count must be in [0, 2^31)");
     require(n == 0 || xyz != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "xyz is NULL");
     s->has_normals = s->has_raw = s->has_grid = false;
     const float* dx = stage_in(s->ws, "api.xyz", xyz, size_t(n) * 3, on_device, st);
+    require_finite_points(s->ws, dx, n, st);
     record(s, 0, st);
     lbvh_build(dx, int(n), s->cfg.bucket, s->ws, "tree", s->T, s->d_box, s->d_err, st);
     s->T.seed_radius = s->cfg.seed_radius;
@@ -1156,7 +1181,7 @@ lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xy
         b->d_xyz = b->ws.get<float>("batch.xyz", size_t(n) * 3);
         LVRGB_CUDA(cudaMemcpyAsync(b->d_xyz, xyz, size_t(n) * 3 * sizeof(float),
                                    on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-        LVRGB_CUDA(cudaStreamSynchronize(st));
+        require_finite_points(b->ws, b->d_xyz, n, st);
     });
     if (st != LVRGB_OK) {
         delete b;

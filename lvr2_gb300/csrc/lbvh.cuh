@@ -261,12 +261,16 @@ __device__ __forceinline__ int seed_bucket_for(const Lbvh& T, float x, float y, 
 // warp-uniform seed bucket (and seed_radius buckets on each side, which are
 // Morton neighbours) are scanned first so that the k-th distance bound is
 // small before the tree walk; the walk skips them.
-__device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
+__device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active_in,
                                              LaneHeap& heap, float4* stage, int* err, TravStats& st,
                                              int seed = -1, int root = 0, int blo = 0, int bhi = 0x7fffffff) {
     const int lane = threadIdx.x & 31;
+    // A query with a non-finite coordinate has no neighbours (every distance
+    // is NaN); it takes no part in the walk, where its NaN box distances
+    // would open every node.
+    const bool active = active_in && isfinite(qx) && isfinite(qy) && isfinite(qz);
     if (T.nbuckets <= 0) {
-        if (active) heap.finish();
+        if (active_in) heap.finish();
         return;
     }
     // warp query box and an empty, NaN-padded candidate buffer
@@ -304,7 +308,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         const int b = -1 - root;
         if (b < skip_lo || b > skip_hi) add_bucket(T, b, W, qx, qy, qz, active, heap, st);
         if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
-        if (active) heap.finish();
+        if (active_in) heap.finish();
         return;
     }
     int stk0 = 0, stk1 = 0, stk2 = 0;  // lane l holds stack entries l, l + 32, l + 64
@@ -394,7 +398,7 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
         }
     }
     if (W.count) flush_chunk(W, qx, qy, qz, active, heap, st);
-    if (active) heap.finish();
+    if (active_in) heap.finish();
 }
 
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,

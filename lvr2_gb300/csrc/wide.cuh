@@ -200,7 +200,8 @@ __device__ __forceinline__ void wide_knn(const Lbvh& T, float qx, float qy, floa
     W.cnt = 0;
     W.tau = bound;
     W.thr = bound < __int_as_float(0x7f800000) ? make_key(bound, 0xffffffffu) : kKeyEmpty;
-    if (T.nbuckets <= 0) return;
+    // a query with a non-finite coordinate has no neighbours (warp-uniform)
+    if (T.nbuckets <= 0 || !(isfinite(qx) && isfinite(qy) && isfinite(qz))) return;
     if (T.nbuckets == 1) root = -1;
     bhi = min(bhi, T.nbuckets - 1);
     // Morton window around the query's bucket holding at least K points
