@@ -42,7 +42,8 @@ typedef enum lvrgb_status {
     LVRGB_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed (lvr2 retries smaller chunks) */
     LVRGB_ERR_UNSUPPORTED = 4,      /* e.g. nem 1 (RANSAC) */
     LVRGB_ERR_STATE = 5,            /* call order: no normals yet, no mesh yet */
-    LVRGB_ERR_KERNEL = 6            /* a kernel reported an internal limit (traversal depth) */
+    LVRGB_ERR_KERNEL = 6,           /* a kernel reported an internal limit (traversal depth) */
+    LVRGB_ERR_TOPOLOGY = 7          /* complex edges: pmp's add_face would throw TopologyException */
 } lvrgb_status;
 
 typedef struct lvrgb_surface_s* lvrgb_surface;
@@ -320,6 +321,33 @@ lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t 
                                      const float* tsdf_values, int64_t ncells, const int64_t* chunk_offsets,
                                      int32_t nchunks, const float* inner_boxes, lvrgb_mesh_info* info,
                                      int32_t on_device, void* stream);
+
+/* Half-edge connectivity of the last mesh in pmp::SurfaceMesh's layout
+ * (include/lvr2/geometry/pmp/SurfaceMesh.h), for building the PMPMesh that
+ * lvr2_reconstruct fills face by face (PMPMesh::addFace,
+ * include/lvr2/geometry/PMPMesh.tcc; pmp SurfaceMesh::add_face,
+ * src/liblvr2/geometry/pmp/SurfaceMesh.cpp:283-460) in one pass:
+ *   edge e owns halfedges 2e and 2e + 1 (opposite = h ^ 1), numbered in the
+ *   order in which add_face over faces 0..F-1 creates them, 2e pointing the
+ *   way the edge first appeared; he_vertex[h] = the vertex h points to;
+ *   he_face[h] = its face or 0xffffffff on the boundary; he_next, he_prev;
+ *   vertex_he[v] = an outgoing halfedge, a boundary one on the boundary
+ *   (0xffffffff for a vertex without faces); face_he[f] = the halfedge from
+ *   its corner 2 to corner 0.
+ * At a vertex with several boundary gaps (info->complex_vertices) the
+ * boundary links pair incoming and outgoing boundary halfedges in ascending
+ * order.  Complex edges (more than two faces, or two of one orientation)
+ * return LVRGB_ERR_TOPOLOGY with info->complex_edges set.  Any array may be
+ * NULL (info only); he_* arrays have 2 * info->edges entries. */
+typedef struct lvrgb_halfedge_info {
+    int64_t vertices, faces, edges;
+    int64_t boundary_halfedges;
+    int64_t complex_edges;
+    int64_t complex_vertices;
+} lvrgb_halfedge_info;
+lvrgb_status lvrgb_mesh_halfedges(lvrgb_surface s, lvrgb_halfedge_info* info, uint32_t* he_vertex, uint32_t* he_next,
+                                  uint32_t* he_prev, uint32_t* he_face, uint32_t* vertex_he, uint32_t* face_he,
+                                  int32_t on_device, void* stream);
 
 /* HashGrid::toPointBuffer (include/lvr2/reconstruction/HashGrid.tcc:196-233),
  * the per-chunk grid the large-scale reconstruction stores and merges: for

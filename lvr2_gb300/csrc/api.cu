@@ -985,6 +985,43 @@ lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, 
     });
 }
 
+lvrgb_status lvrgb_mesh_halfedges(lvrgb_surface s, lvrgb_halfedge_info* info, uint32_t* he_vertex, uint32_t* he_next,
+                                  uint32_t* he_prev, uint32_t* he_face, uint32_t* vertex_he, uint32_t* face_he,
+                                  int32_t on_device, void* stream) {
+    return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.mesh_halfedges");
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
+        DeviceScope dev(s->device);
+        cudaStream_t st = as_stream(stream);
+        HalfedgeMesh H;
+        build_halfedges(s->grid.faces, int(s->grid.nfaces), int(s->grid.nverts), s->ws, H, st);
+        if (info) {
+            info->vertices = H.nverts;
+            info->faces = H.nfaces;
+            info->edges = H.nedges;
+            info->boundary_halfedges = H.boundary;
+            info->complex_edges = H.complex_edges;
+            info->complex_vertices = H.complex_vertices;
+        }
+        require(H.complex_edges == 0, LVRGB_ERR_TOPOLOGY, "the mesh has complex edges");
+        const size_t nh = size_t(2 * H.nedges);
+        auto out = [&](uint32_t* dst, const uint32_t* src, size_t n, const char* name) {
+            if (!dst || n == 0) return;
+            uint32_t* d = stage_out(s->ws, name, dst, n, on_device);
+            LVRGB_CUDA(cudaMemcpyAsync(d, src, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+            finish_out(dst, d, n, on_device, st);
+        };
+        out(he_vertex, H.he_vertex, nh, "he.out.v");
+        out(he_next, H.he_next, nh, "he.out.n");
+        out(he_prev, H.he_prev, nh, "he.out.p");
+        out(he_face, H.he_face, nh, "he.out.f");
+        out(vertex_he, H.vertex_he, size_t(H.nverts), "he.out.vh");
+        out(face_he, H.face_he, size_t(H.nfaces), "he.out.fh");
+        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 lvrgb_status lvrgb_get_cell_tsdf(lvrgb_surface s, float* centers, float* tsdf_values, int32_t on_device,
                                  void* stream) {
     return guarded([&] {

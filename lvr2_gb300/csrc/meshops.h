@@ -26,3 +26,30 @@ void mesh_vertex_colors(const Lbvh& T, const float* d_box, const float* verts, i
 uint32_t max_index(const uint32_t* a, size_t n, Workspace& ws, cudaStream_t s);
 
 }  // namespace lvrgb
+
+namespace lvrgb {
+
+// Half-edge connectivity of a triangle mesh in pmp::SurfaceMesh's layout
+// (include/lvr2/geometry/pmp/SurfaceMesh.h): edge e owns halfedges 2e and
+// 2e + 1 (opposite = h ^ 1); he_vertex = the vertex a halfedge points to,
+// he_face (0xffffffff on the boundary), he_next / he_prev, vertex_he (an
+// outgoing halfedge, a boundary one on the boundary), face_he.  Device arrays
+// in the workspace.
+struct HalfedgeMesh {
+    long long nverts = 0, nfaces = 0, nedges = 0;
+    long long boundary = 0;          // boundary halfedges
+    long long complex_edges = 0;     // edges of > 2 faces or of two faces of one orientation
+    long long complex_vertices = 0;  // vertices with more than one boundary gap
+    uint32_t* he_vertex = nullptr;
+    uint32_t* he_next = nullptr;
+    uint32_t* he_prev = nullptr;
+    uint32_t* he_face = nullptr;
+    uint32_t* vertex_he = nullptr;
+    uint32_t* face_he = nullptr;
+};
+
+// Builds H for faces (device, nf x 3, indices < nv).  With complex edges the
+// arrays are not built (H.complex_edges > 0).
+void build_halfedges(const uint32_t* faces, int nf, int nv, Workspace& ws, HalfedgeMesh& H, cudaStream_t s);
+
+}  // namespace lvrgb

@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import GridConfig, LvrgbError, MeshInfo, SurfaceConfig, check
+from ._lib import GridConfig, HalfedgeInfo, LvrgbError, MeshInfo, SurfaceConfig, check
 
 
 def _is_torch_cuda(a):
@@ -351,6 +351,25 @@ class Surface:
                                                   nch, _ptr(box), ctypes.byref(info), 0, self._stream))
         self.info = info
         return info
+
+    def halfedges(self):
+        """Half-edge connectivity of the last mesh (pmp::SurfaceMesh layout):
+        dict of he_vertex, he_next, he_prev, he_face (2E), vertex_he (V),
+        face_he (F) and the counts."""
+        L = _lib.load()
+        info = HalfedgeInfo()
+        check(L.lvrgb_mesh_halfedges(self._h, ctypes.byref(info), None, None, None, None, None, None, 0,
+                                     self._stream))
+        nh = 2 * info.edges
+        arrs = {k: np.empty(n, np.uint32) for k, n in (("he_vertex", nh), ("he_next", nh), ("he_prev", nh),
+                                                       ("he_face", nh), ("vertex_he", info.vertices),
+                                                       ("face_he", info.faces))}
+        check(L.lvrgb_mesh_halfedges(self._h, ctypes.byref(info), _ptr(arrs["he_vertex"]), _ptr(arrs["he_next"]),
+                                     _ptr(arrs["he_prev"]), _ptr(arrs["he_face"]), _ptr(arrs["vertex_he"]),
+                                     _ptr(arrs["face_he"]), 0, self._stream))
+        arrs.update(edges=info.edges, boundary_halfedges=info.boundary_halfedges,
+                    complex_edges=info.complex_edges, complex_vertices=info.complex_vertices)
+        return arrs
 
     def cell_tsdf(self):
         """HashGrid::toPointBuffer of the culled grid: cell centres (C, 3) and

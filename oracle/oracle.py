@@ -344,6 +344,82 @@ def vertex_colors(vpos, point_colors, surface):
     return out
 
 
+def halfedges(faces, nv):
+    """Half-edge connectivity in pmp::SurfaceMesh's layout with the canonical
+    choices of the GPU builder (lvr2_gb300/csrc/meshops.cu): edges in the order
+    pmp's add_face (src/liblvr2/geometry/pmp/SurfaceMesh.cpp:283-460) creates
+    them over faces 0..F-1, halfedge 2e along the first appearance, face
+    halfedge = corner 2 -> corner 0, boundary halfedges linked to the boundary
+    halfedge leaving their end vertex (paired in ascending order at vertices
+    with several gaps), vertex halfedge = smallest outgoing boundary halfedge,
+    else smallest outgoing halfedge.  Returns a dict (complex_edges > 0: no
+    arrays)."""
+    NONE = np.uint32(0xFFFFFFFF)
+    F = np.asarray(faces, np.int64).reshape(-1, 3)
+    nf = len(F)
+    m = 3 * nf
+    a = F.reshape(-1)
+    b = F[:, [1, 2, 0]].reshape(-1)
+    key = (np.minimum(a, b) << 32) | np.maximum(a, b)
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    head = np.ones(m, bool)
+    head[1:] = ks[1:] != ks[:-1]
+    run = np.cumsum(head) - 1
+    starts = np.flatnonzero(head)
+    ne = len(starts)
+    counts = np.diff(np.r_[starts, m])
+    first = order[starts]
+    edge_of_run = np.empty(ne, np.int64)
+    edge_of_run[np.argsort(first, kind="stable")] = np.arange(ne)
+    second = order[np.minimum(starts + 1, m - 1)]
+    complex_ = (counts > 2) | (a[first] == b[first]) | ((counts == 2) & (a[second] == a[first]))
+    out = dict(vertices=int(nv), faces=nf, edges=ne, complex_edges=int(complex_.sum()))
+    if out["complex_edges"]:
+        return out
+    r = order
+    rr = run
+    e = edge_of_run[rr]
+    he_of_ref = np.empty(m, np.int64)
+    he_of_ref[r] = 2 * e + (a[r] != a[first[rr]])
+    he_vertex = np.empty(2 * ne, np.int64)
+    e_of_first = edge_of_run
+    he_vertex[2 * e_of_first] = b[first]
+    he_vertex[2 * e_of_first + 1] = a[first]
+    he_face = np.full(2 * ne, 0xFFFFFFFF, np.int64)
+    he_face[he_of_ref] = np.arange(m) // 3
+    he_next = np.full(2 * ne, 0xFFFFFFFF, np.int64)
+    hr = he_of_ref.reshape(-1, 3)
+    he_next[hr[:, 0]] = hr[:, 1]
+    he_next[hr[:, 1]] = hr[:, 2]
+    he_next[hr[:, 2]] = hr[:, 0]
+    face_he = hr[:, 2].copy()
+    bnd = np.sort(2 * edge_of_run[counts == 1] + 1)
+    frm = he_vertex[bnd ^ 1]
+    to = he_vertex[bnd]
+    out_sorted = bnd[np.argsort(frm, kind="stable")]
+    in_sorted = bnd[np.argsort(to, kind="stable")]
+    fs, ts = frm[np.argsort(frm, kind="stable")], to[np.argsort(to, kind="stable")]
+    out_count = np.bincount(frm, minlength=nv)
+    out_start = np.searchsorted(fs, np.arange(nv))
+    in_start = np.searchsorted(ts, np.arange(nv))
+    rank = np.arange(len(in_sorted)) - in_start[ts]
+    he_next[in_sorted] = out_sorted[out_start[ts] + rank]
+    he_prev = np.full(2 * ne, 0xFFFFFFFF, np.int64)
+    he_prev[he_next] = np.arange(2 * ne)
+    vmin_all = np.full(nv, 0xFFFFFFFF, np.int64)
+    np.minimum.at(vmin_all, he_vertex[np.arange(2 * ne) ^ 1], np.arange(2 * ne))
+    vmin_b = np.full(nv, 0xFFFFFFFF, np.int64)
+    isb = he_face == 0xFFFFFFFF
+    np.minimum.at(vmin_b, he_vertex[np.flatnonzero(isb) ^ 1], np.flatnonzero(isb))
+    vertex_he = np.where(vmin_b != 0xFFFFFFFF, vmin_b, vmin_all)
+    out.update(he_vertex=he_vertex.astype(np.uint32), he_next=he_next.astype(np.uint32),
+               he_prev=he_prev.astype(np.uint32), he_face=he_face.astype(np.uint32),
+               vertex_he=vertex_he.astype(np.uint32), face_he=face_he.astype(np.uint32),
+               boundary_halfedges=len(bnd), complex_vertices=int((out_count > 1).sum()))
+    return out
+
+
 def reconstruct_cells(centers, tsdf, voxelsize, chunk_offsets=None, inner_boxes=None, decomposition="MC"):
     """HashGrid(chunks, innerBoxes, bb, voxelsize) over stored chunk cells,
     then marching cubes (oracle/lvr_oracle.cpp orc_reconstruct_cells).

@@ -197,3 +197,47 @@ def test_merged_grid_reproduces_the_chunk_mesh(oracle_mod):
     got2 = canonical_mesh(m2["vkeys"], m2["vpos"], m2["faces"])
     assert len(m2["cells_all"]) == len(centers)
     assert all(np.array_equal(x, y) for x, y in zip(ref, got2))
+
+
+def test_halfedge_restatement_is_a_valid_pmp_connectivity(oracle_mod):
+    """The canonical half-edge arrays of an open marching-cubes mesh: next and
+    prev are inverse, every face is one 3-cycle in corner order, boundary
+    halfedges form closed loops, halfedge h leaves the vertex h ^ 1 points
+    to, a boundary vertex's halfedge is a boundary one, and edges are numbered
+    by first appearance (pmp's add_face over faces 0..F-1)."""
+    from lvr2_gb300 import synthetic
+    P = synthetic.spheres_tori(20_000, seed=6)
+    P = P[P[:, 0] < 0.5]
+    o = oracle_mod.OracleSurface(P)
+    r = o.reconstruct(o.normals(10, nem=3), voxelsize=0.03, kd=10, decomposition="PMC")
+    F = r["faces"].astype(np.int64)
+    nv = len(r["vpos"])
+    H = oracle_mod.halfedges(F, nv)
+    assert H["complex_edges"] == 0 and H["boundary_halfedges"] > 0
+    nxt, prv, hv, hf = (H[k].astype(np.int64) for k in ("he_next", "he_prev", "he_vertex", "he_face"))
+    nh = 2 * H["edges"]
+    assert np.array_equal(prv[nxt], np.arange(nh)) and np.array_equal(nxt[prv], np.arange(nh))
+    fh = H["face_he"].astype(np.int64)
+    assert np.array_equal(nxt[nxt[nxt[fh]]], fh)
+    assert np.array_equal(hv[fh], F[:, 0]) and np.array_equal(hv[nxt[fh]], F[:, 1])
+    assert np.array_equal(hv[nxt[nxt[fh]]], F[:, 2])
+    assert np.array_equal(hf[fh], np.arange(len(F)))
+    bnd = np.flatnonzero(hf == 0xFFFFFFFF)
+    assert np.all(hf[nxt[bnd]] == 0xFFFFFFFF)  # boundary loops stay on the boundary
+    assert np.array_equal(hv[bnd ^ 1], hv[prv[bnd]])  # consecutive boundary halfedges share a vertex
+    vh = H["vertex_he"].astype(np.int64)
+    used = vh != 0xFFFFFFFF
+    assert np.array_equal(hv[vh[used] ^ 1], np.flatnonzero(used))
+    on_b = np.zeros(nv, bool)
+    on_b[hv[bnd ^ 1]] = True
+    assert np.all(hf[vh[on_b]] == 0xFFFFFFFF)
+    # first-appearance edge numbering
+    seen, order = {}, []
+    for f in F:
+        for c in range(3):
+            k = (min(f[c], f[(c + 1) % 3]), max(f[c], f[(c + 1) % 3]))
+            if k not in seen:
+                seen[k] = len(seen)
+                order.append((f[c], f[(c + 1) % 3]))
+    first = np.array(order)
+    assert np.array_equal(hv[0::2], first[:, 1]) and np.array_equal(hv[1::2], first[:, 0])
