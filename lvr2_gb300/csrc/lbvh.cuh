@@ -149,10 +149,6 @@ struct LaneHeap {
             heapify();
         }
     }
-    __device__ __forceinline__ void offer(float d2, uint32_t idx) {
-        unsigned long long key = make_key(d2, idx);
-        if (key < top) push(key);
-    }
     // In-place heap sort: afterwards h[0..K) is ascending.
     __device__ __forceinline__ void sort_ascending() {
         for (int end = K - 1; end > 0; end--) {
