@@ -25,17 +25,17 @@ def project():
     return pts, np.array(flips, np.float32)
 
 
-@pytest.mark.parametrize("bucket", [32, 16])
-def test_batch_equals_per_scan_surfaces(lib, bucket):
+@pytest.mark.parametrize("bucket,nem", [(32, 3), (16, 3), (32, 0), (32, 2)])
+def test_batch_equals_per_scan_surfaces(lib, bucket, nem):
     import lvr2_gb300
     scans, flips = project()
     ref = []
     for p, f in zip(scans, flips):
-        with lvr2_gb300.Surface(p, kn=10, ki=10, nem=3, flip_point=f, bucket=bucket) as s:
+        with lvr2_gb300.Surface(p, kn=10, ki=10, nem=nem, flip_point=f, bucket=bucket) as s:
             s.calculate_normals()
             ref.append(s.normals())
     ref = np.concatenate(ref)
-    with lvr2_gb300.Batch(scans, flips, kn=10, ki=10, nem=3, bucket=bucket) as b:
+    with lvr2_gb300.Batch(scans, flips, kn=10, ki=10, nem=nem, bucket=bucket) as b:
         b.calculate_normals()
         got = b.normals()
         counters, ms = b.stats()
