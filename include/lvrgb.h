@@ -102,6 +102,15 @@ lvrgb_status lvrgb_surface_set_k(lvrgb_surface s, int32_t kn, int32_t ki, int32_
  * CudaSurface::setFlippoint (CudaSurface.hpp:136). */
 lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, float z);
 
+/* Scan poses (AdaptiveKSearchSurface's posefile argument,
+ * AdaptiveKSearchSurface.tcc:94-139): with poses, each normal is flipped
+ * toward the cloud point whose input index is its nearest pose's index
+ * (m_points[nearestPoseIds[0]], :252-265; lvr2 indexes the cloud with the pose
+ * index), or toward the flip point when that index is not a point.  Nearest =
+ * smallest (float d2, pose index).  poses: np x 3 (host), np <= 8192; np = 0
+ * removes them. */
+lvrgb_status lvrgb_surface_set_scan_poses(lvrgb_surface s, const float* poses, int64_t np);
+
 /* Plane-fit method: AdaptiveKSearchSurface calcMethod / CudaSurface::setMethod
  * (CudaSurface.hpp:144).  nem 1 (RANSAC) returns LVRGB_ERR_UNSUPPORTED; nem 4 is
  * the fit of CudaKSearchSurface (see lvrgb_surface_config). */

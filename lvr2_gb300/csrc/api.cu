@@ -4,10 +4,12 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "lvrgb.h"
 #include "batch.h"
@@ -35,6 +37,7 @@ struct lvrgb_surface_s {
     float4* normals = nullptr;      // final normals, Morton order
     float4* raw_normals = nullptr;  // before interpolation
     int32_t* kused = nullptr;
+    std::vector<float> poses;  // scan poses (x y z each), empty: none
     bool has_normals = false;
     bool has_raw = false;
     GridResult grid;
@@ -381,6 +384,18 @@ lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, flo
     });
 }
 
+lvrgb_status lvrgb_surface_set_scan_poses(lvrgb_surface s, const float* poses, int64_t np) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(np >= 0 && np <= 8192, LVRGB_ERR_INVALID_ARGUMENT, "pose count must be in 0..8192");
+        require(np == 0 || poses != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "poses is NULL");
+        for (int64_t i = 0; i < 3 * np; i++)
+            require(std::isfinite(poses[i]), LVRGB_ERR_INVALID_ARGUMENT, "a pose has a non-finite coordinate");
+        s->poses.assign(poses, poses + 3 * np);
+        s->has_normals = s->has_raw = false;
+    });
+}
+
 lvrgb_status lvrgb_surface_set_method(lvrgb_surface s, int32_t nem) {
     return guarded([&] {
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
@@ -412,6 +427,14 @@ lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
         LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
         check_lbvh_k(s->cfg.kn, s->cfg.nem);
         NormalsConfig c = normals_config(s);
+        if (!s->poses.empty() && s->T.n > 0) {
+            const int np = int(s->poses.size() / 3);
+            float* dp = s->ws.get<float>("api.poses", s->poses.size());
+            LVRGB_CUDA(cudaMemcpyAsync(dp, s->poses.data(), s->poses.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+            float4* targets = s->ws.get<float4>("api.pose_targets", size_t(s->T.n));
+            pose_flip_targets(s->T, dp, np, targets, st);
+            c.flip_target = targets;
+        }
         // The interpolation's kNN(ki) is the first ki of the estimation's
         // kNN (k >= 2kn, or kn for nem 4): keep those lists instead of searching again.
         const bool lists = s->cfg.ki > 0 && s->cfg.ki <= first_search_k(s->cfg.kn, s->cfg.nem);

@@ -139,6 +139,9 @@ struct NormalsArgs {
     // Squared distance of the k-th neighbour of every point that searches
     // again (by Morton position): written by a round, read by the next one.
     float* kth_d2;
+    // Optional per point (Morton position): a flip point of its own when w != 0
+    // (the nearest scan pose's point, AdaptiveKSearchSurface.tcc:252-265).
+    const float4* flip_target;
     int wide_tile;  // queries per warp tile of the one-warp-per-query kernel (1..32)
     unsigned long long* gheap;
     int* err;
@@ -464,6 +467,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
             const int seed = __shfl_sync(kFull, pos, 0) / A.T.bucket;
             knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
         }
+        if (A.flip_target && active) {
+            const float4 t = __ldg(A.flip_target + pos);
+            if (t.w != 0.0f) {
+                fx = t.x; fy = t.y; fz = t.z;
+            }
+        }
         bool retry = false;
         if (active) {
             // Ascending order puts the real entries first (fewer points than K),
@@ -607,6 +616,12 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
                 const SegInfo g = A.segs[scan];
                 root = g.root; blo = g.blo; bhi = g.bhi;
                 fx = g.fx; fy = g.fy; fz = g.fz;
+            }
+            if (A.flip_target) {
+                const float4 t = __ldg(A.flip_target + pos);
+                if (t.w != 0.0f) {
+                    fx = t.x; fy = t.y; fz = t.z;
+                }
             }
             // Search bounds, each exact when at least K points lie within it:
             //  * chain: the previous query's K points lie within
@@ -1229,6 +1244,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.segs = nullptr;
         A.bucket_scan = nullptr;
         A.nq_dev = nullptr;
+        A.flip_target = cfg.flip_target;
         launch_normals(A, nq, ws, s);
         if (last) break;
         compact_retry(flags, list, nq, nullptr, retry, counter, ws, s);
@@ -1283,6 +1299,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.ki = ki;
         A.segs = segs;
         A.bucket_scan = bucket_scan;
+        A.flip_target = nullptr;
         // Later rounds read their query count on the device: launch a fixed
         // grid that strides over however many queries the previous round left.
         launch_normals(A, round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), ws, s);
@@ -1440,6 +1457,37 @@ void list_extent(const uint32_t* cnt, const uint32_t* idx, int nq, int k, Worksp
     LVRGB_CUDA(cudaMemcpyAsync(h, d, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     LVRGB_CUDA(cudaStreamSynchronize(s));
     std::memcpy(out, h, 2 * sizeof(uint32_t));
+}
+
+namespace {
+// Nearest scan pose of every point (canonical (d2, pose index) order, brute
+// force over the poses), and the flip point lvr2 takes from it: the cloud
+// point whose input index is the pose's index (m_points[nearestPoseIds[0]],
+// AdaptiveKSearchSurface.tcc:255-259).  w = 0 when that index is not a point.
+__global__ void pose_target_kernel(Lbvh T, const float* __restrict__ poses, int np, float4* __restrict__ out) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= T.n) return;
+    const float4 q = T.pts[pos];
+    unsigned long long best = kKeyEmpty;
+    for (int j = 0; j < np; j++) {
+        const float d2 = dist2(q.x, q.y, q.z, poses[3 * j], poses[3 * j + 1], poses[3 * j + 2]);
+        const unsigned long long key = make_key(d2, uint32_t(j));
+        if (key < best) best = key;
+    }
+    const uint32_t j = key_idx(best);
+    if (best == kKeyEmpty || j >= uint32_t(T.n)) {
+        out[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const float4 p = T.pts[T.inv[j]];
+    out[pos] = make_float4(p.x, p.y, p.z, 1.0f);
+}
+}  // namespace
+
+void pose_flip_targets(const Lbvh& T, const float* d_poses, int np, float4* out, cudaStream_t s) {
+    if (T.n == 0) return;
+    pose_target_kernel<<<ceil_div(T.n, 128), 128, 0, s>>>(T, d_poses, np, out);
+    LVRGB_LAUNCH_CHECK();
 }
 
 void normals_from_lists(const Lbvh& T, const float* queries, int nq, int k, const uint32_t* cnt, const uint32_t* idx,

@@ -11,6 +11,8 @@ struct NormalsConfig {
     int adaptive = 1;     // k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed
     float flip[3] = {0, 0, 0};
     float gap_threshold = 1e-3f;  // relative eigengap below which the eigensolve runs in FP64
+    // Optional per point (Morton position, device): its own flip point when w != 0.
+    const float4* flip_target = nullptr;
 };
 
 // Device counters written by compute_normals (uint32[16]):
@@ -68,6 +70,12 @@ void knn_rows_smem(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx
 // PointsetSurface::getInterpolatedNormal for sorted queries; out rows float3.
 void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, const float4* qs, int nq,
                               float* out, Workspace& ws, int* d_err, cudaStream_t s);
+
+// Flip points from scan poses (AdaptiveKSearchSurface::parseScanPoses and the
+// pose-tree flip, AdaptiveKSearchSurface.tcc:94-139, 252-265): per point
+// (Morton position) the cloud point indexed by its nearest pose's index, w = 1,
+// or w = 0 when that index is >= n.  d_poses: np x 3 (device).
+void pose_flip_targets(const Lbvh& T, const float* d_poses, int np, float4* out, cudaStream_t s);
 
 // LBVHIndex::calculate_normals: the nem 4 fit from given neighbour lists
 // (device arrays: queries nq x 3, cnt[nq] <= k, idx nq x k input indices < T.n,

@@ -135,6 +135,11 @@ class Surface:
     def set_flip_point(self, x, y, z):
         check(_lib.load().lvrgb_surface_set_flip_point(self._h, x, y, z))
 
+    def set_scan_poses(self, poses):
+        """AdaptiveKSearchSurface's scan poses: (np, 3), or None to remove."""
+        p = np.zeros((0, 3), np.float32) if poses is None else np.ascontiguousarray(poses, np.float32).reshape(-1, 3)
+        check(_lib.load().lvrgb_surface_set_scan_poses(self._h, _ptr(p), len(p)))
+
     def set_method(self, nem):
         check(_lib.load().lvrgb_surface_set_method(self._h, nem))
 

@@ -528,7 +528,7 @@ int orc_knn(const orc_surface* s, const float* q, int64_t nq, int k, int canonic
 }
 
 int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float* flip3,
-                int canonical, float* normals, int32_t* k_used, int threads) {
+                int canonical, float* normals, int32_t* k_used, int threads, const float* flip_targets) {
     if (nem != 0 && nem != 2 && nem != 3) return -1;
     set_threads(threads);
     const std::vector<V3>& P = s->pts;
@@ -555,9 +555,14 @@ int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float
         if (nem == 2) nrm = plane_iterative(P, id, qp);
         else if (nem == 3) nrm = plane_ipca(P, id, qp);
         else nrm = plane_lsq(P, id, qp);
-        // Flip toward the flip point (AdaptiveKSearchSurface.tcc:268-274).
+        // Flip toward the flip point (AdaptiveKSearchSurface.tcc:268-274), or
+        // toward the point the nearest scan pose names (:252-265) when the
+        // caller gives per-point targets (NaN x: none).
         // Normal::operator-() builds a new Normal, which re-normalises.
-        if (nrm.dot(flip - qp) < 0) nrm = V3(-nrm.x, -nrm.y, -nrm.z).normalized();
+        V3 target = flip;
+        if (flip_targets && flip_targets[3 * i] == flip_targets[3 * i])
+            target = V3(flip_targets[3 * i], flip_targets[3 * i + 1], flip_targets[3 * i + 2]);
+        if (nrm.dot(target - qp) < 0) nrm = V3(-nrm.x, -nrm.y, -nrm.z).normalized();
         normals[3 * i] = nrm.x;
         normals[3 * i + 1] = nrm.y;
         normals[3 * i + 2] = nrm.z;

@@ -44,7 +44,8 @@ int orc_knn(const orc_surface* s, const float* q, int64_t nq, int k, int canonic
  * doubling with the bounding-box test.  k_used (optional) receives the k of
  * the search whose neighbours fitted the plane. */
 int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float* flip3,
-                int canonical, float* normals, int32_t* k_used, int threads);
+                int canonical, float* normals, int32_t* k_used, int threads,
+                const float* flip_targets);
 
 /* interpolateSurfaceNormals: out_i = normalize(in_i + sum_{j in kNN(ki)} in_j). */
 int orc_interpolate(const orc_surface* s, int ki, const float* normals_in, float* normals_out,

@@ -47,7 +47,8 @@ def lib():
     L.orc_destroy.argtypes = [_vp]
     L.orc_bbox.argtypes = [_vp, _f32p]
     L.orc_knn.argtypes = [_vp, _f32p, _i64, _int, _int, _u32p, _f32p, _i32p, _int]
-    L.orc_normals.argtypes = [_vp, _int, _int, _int, ctypes.c_void_p, _int, _f32p, ctypes.c_void_p, _int]
+    L.orc_normals.argtypes = [_vp, _int, _int, _int, ctypes.c_void_p, _int, _f32p, ctypes.c_void_p, _int,
+                              ctypes.c_void_p]
     L.orc_interpolate.argtypes = [_vp, _int, _f32p, _f32p, _int, _int]
     L.orc_distance.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _f32p, _int]
     L.orc_interpolated_normal.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _int]
@@ -102,15 +103,21 @@ class OracleSurface:
         lib().orc_knn(self._h, q.reshape(-1), len(q), k, int(canonical), idx, dist, cnt, self.threads)
         return idx, dist, cnt
 
-    def normals(self, kn, nem=3, adaptive=True, flip=None, canonical=True, with_k=False):
+    def normals(self, kn, nem=3, adaptive=True, flip=None, canonical=True, with_k=False, flip_targets=None):
+        """flip_targets: optional (n, 3) per-point flip points (NaN row: use
+        flip), as the scan-pose flip gives them."""
         out = np.empty((self.n, 3), np.float32)
         kused = np.empty(self.n, np.int32) if with_k else None
         fl = None
         if flip is not None:
             fl_arr = np.ascontiguousarray(flip, np.float32)
             fl = fl_arr.ctypes.data_as(ctypes.c_void_p)
+        ft = None
+        if flip_targets is not None:
+            ft_arr = np.ascontiguousarray(flip_targets, np.float32).reshape(self.n, 3)
+            ft = ft_arr.ctypes.data_as(ctypes.c_void_p)
         rc = lib().orc_normals(self._h, kn, nem, int(adaptive), fl, int(canonical), out,
-                               kused.ctypes.data_as(ctypes.c_void_p) if with_k else None, self.threads)
+                               kused.ctypes.data_as(ctypes.c_void_p) if with_k else None, self.threads, ft)
         if rc != 0:
             raise ValueError("oracle normals: unsupported nem %d" % nem)
         return (out, kused) if with_k else out
@@ -341,6 +348,28 @@ def vertex_colors(vpos, point_colors, surface):
     idx, _, cnt = surface.knn(V, 1)
     out = c[idx[:, 0].astype(np.int64)].copy()
     out[cnt <= 0] = 0
+    return out
+
+
+def pose_flip_targets(points, poses):
+    """Per-point flip points of the scan-pose flip
+    (include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:252-265): the cloud
+    point whose input index is the nearest pose's index (lvr2 indexes m_points
+    with the pose index); nearest = smallest (float d2, pose index); NaN rows
+    where that index is not a point."""
+    P = np.asarray(points, np.float32)
+    Q = np.asarray(poses, np.float32).reshape(-1, 3)
+    best = np.full(len(P), np.inf, np.float32)
+    arg = np.zeros(len(P), np.int64)
+    for j, p in enumerate(Q):
+        d = P - p
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        better = d2 < best
+        best[better] = d2[better]
+        arg[better] = j
+    out = np.full((len(P), 3), np.nan, np.float32)
+    ok = arg < len(P)
+    out[ok] = P[arg[ok]]
     return out
 
 
