@@ -91,6 +91,10 @@ class Surface {
     void setKd(int k) { check(lvrgb_surface_set_k(h_, -1, -1, k), "setKd"); }
     void setFlipPoint(const Vec3& p) { check(lvrgb_surface_set_flip_point(h_, p.x, p.y, p.z), "setFlipPoint"); }
     void setCalcMethod(int nem) { check(lvrgb_surface_set_method(h_, nem), "setCalcMethod"); }
+    // The scan poses of AdaptiveKSearchSurface's posefile argument (x y z each).
+    void setScanPoses(const std::vector<float>& poses) {
+        check(lvrgb_surface_set_scan_poses(h_, poses.data(), int64_t(poses.size() / 3)), "setScanPoses");
+    }
 
     // getBoundingBox(): min, max, centroid
     std::array<Vec3, 3> getBoundingBox() const {

@@ -38,6 +38,7 @@ struct Options {
     float flip[3] = {0, 0, 0};
     bool recalc = false;
     bool export_normals = false;
+    std::string pose_file;
     int device = 0;
 };
 
@@ -46,7 +47,7 @@ void usage() {
         "usage: lvr2gb_reconstruct <inputFile> [--voxelsize|-v F] [--intersections|-i N] [--pcm|-p NAME]\n"
         "       [--nem 0|2|3|4] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
         "       [--flipPoint X Y Z] [--recalcNormals|-r] [--exportPointNormals|-e] [--outputFile PATH]\n"
-        "       [--useGPU] [--threads N] [--device N]");
+        "       [--scanPoseFile PATH] [--useGPU] [--threads N] [--device N]");
 }
 
 Options parse(int argc, char** argv) {
@@ -90,6 +91,8 @@ Options parse(int argc, char** argv) {
             o.export_normals = true;
         } else if (a == "--outputFile") {
             need(i, 1); o.output = argv[++i];
+        } else if (a == "--scanPoseFile") {
+            need(i, 1); o.pose_file = argv[++i];
         } else if (a == "--useGPU") {
         } else if (a == "--threads" || a == "--device") {
             need(i, 1);
@@ -145,6 +148,24 @@ void read_ascii(const std::string& path, std::vector<float>& xyz, std::vector<ui
             }
         }
     }
+}
+
+// AdaptiveKSearchSurface::parseScanPoses (AdaptiveKSearchSurface.tcc:94-139):
+// "x y z" triples read while the stream is good; the read that meets the end
+// of the file leaves x, y, z unchanged and still appends them, so the last pose
+// appears twice, as in lvr2's loop.
+std::vector<float> read_poses(const std::string& path) {
+    std::ifstream in(path);
+    if (!in.good()) throw std::runtime_error("cannot open scan pose file " + path);
+    std::vector<float> poses;
+    float x = 0, y = 0, z = 0;
+    while (in.good()) {
+        in >> x >> y >> z;
+        poses.push_back(x);
+        poses.push_back(y);
+        poses.push_back(z);
+    }
+    return poses;
 }
 
 // PLY with vertex float properties x, y, z (and optional nx, ny, nz).
@@ -276,6 +297,11 @@ int main(int argc, char** argv) {
             surface.setFlipPoint(lvr2gb::Vec3{1e6f, 1e6f, 1e6f});
         else
             surface.setFlipPoint(lvr2gb::Vec3{o.flip[0], o.flip[1], o.flip[2]});
+        if (!o.pose_file.empty()) {
+            const std::vector<float> poses = read_poses(o.pose_file);
+            std::printf("[lvr2gb_reconstruct] %zu scan poses from %s\n", poses.size() / 3, o.pose_file.c_str());
+            surface.setScanPoses(poses);
+        }
         const bool have_normals = given_normals.size() == xyz.size() && !given_normals.empty();
         if (!have_normals || o.recalc) {
             surface.calculateSurfaceNormals();

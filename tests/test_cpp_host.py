@@ -125,3 +125,36 @@ def test_cli_colours(built, tmp_path):
         vc = s.vertex_colors(pts[:, 3:].astype(np.uint8))
     assert np.array_equal(np.c_[pv["x"], pv["y"], pv["z"]], v)
     assert np.array_equal(np.c_[pv["red"], pv["green"], pv["blue"]], vc)
+
+
+@pytest.mark.gpu
+def test_cli_scan_pose_file(built, tmp_path):
+    """--scanPoseFile: poses read as lvr2's parseScanPoses reads them (the read
+    that meets the end of the file appends the last pose again), normals
+    flipped as with Surface.set_scan_poses."""
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    cli, _ = built
+    P = synthetic.spheres_tori(20_000, seed=52)
+    src = tmp_path / "cloud.xyz"
+    with open(src, "w") as fh:
+        fh.write("%d\n" % len(P))
+        np.savetxt(fh, P, fmt="%.9g")
+    poses = np.array([[0.1, 0.2, 0.3], [0.9, 0.8, 0.7]], np.float32)
+    pf = tmp_path / "poses.txt"
+    pf.write_text("".join("%g %g %g\n" % tuple(p) for p in poses))
+    r = subprocess.run([str(cli), str(src), "-v", "0.05", "--nem", "3", "-e", "--scanPoseFile", str(pf),
+                        "--outputFile", str(tmp_path / "m.ply")], capture_output=True, text=True, timeout=300,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "3 scan poses" in r.stdout
+    data = (tmp_path / "pointnormals.ply").read_bytes()
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    rec = np.frombuffer(data, np.float32, offset=end).reshape(-1, 6)
+    pts_read = np.loadtxt(src, skiprows=1, dtype=np.float32)
+    lvr_poses = np.concatenate([poses, poses[-1:]]).astype(np.float32)
+    with lvr2_gb300.Surface(pts_read, kn=10, ki=10, kd=5, nem=3, flip_point=(0, 0, 0)) as s:
+        s.set_scan_poses(lvr_poses)
+        s.calculate_normals()
+        n = s.normals()
+    assert np.array_equal(rec[:, 3:], n)
