@@ -241,3 +241,30 @@ def test_halfedge_restatement_is_a_valid_pmp_connectivity(oracle_mod):
                 order.append((f[c], f[(c + 1) % 3]))
     first = np.array(order)
     assert np.array_equal(hv[0::2], first[:, 1]) and np.array_equal(hv[1::2], first[:, 0])
+
+
+def test_halfedge_restatement_topology_cases(oracle_mod):
+    """Complex edges (three faces on an edge, two faces of one orientation)
+    are reported; a bow-tie vertex (two boundary gaps) is counted and its
+    boundary halfedges still form closed loops."""
+    three = np.array([[0, 1, 2], [1, 0, 3], [0, 1, 4]])
+    assert oracle_mod.halfedges(three, 5)["complex_edges"] == 1
+    same = np.array([[0, 1, 2], [0, 1, 3]])
+    assert oracle_mod.halfedges(same, 4)["complex_edges"] == 1
+    bowtie = np.array([[0, 1, 2], [0, 3, 4]])  # two triangles sharing vertex 0 only
+    H = oracle_mod.halfedges(bowtie, 5)
+    assert H["complex_edges"] == 0 and H["complex_vertices"] == 1 and H["boundary_halfedges"] == 6
+    nxt = H["he_next"].astype(np.int64)
+    hf = H["he_face"]
+    bnd = np.flatnonzero(hf == 0xFFFFFFFF)
+    seen = set()
+    for b in bnd:  # every boundary loop closes within the boundary halfedges
+        h, steps = b, 0
+        while True:
+            seen.add(h)
+            h = nxt[h]
+            steps += 1
+            assert hf[h] == 0xFFFFFFFF and steps <= len(bnd)
+            if h == b:
+                break
+    assert seen == set(bnd.tolist())
