@@ -357,6 +357,13 @@ typedef struct lvrgb_halfedge_info {
 lvrgb_status lvrgb_mesh_halfedges(lvrgb_surface s, lvrgb_halfedge_info* info, uint32_t* he_vertex, uint32_t* he_next,
                                   uint32_t* he_prev, uint32_t* he_face, uint32_t* vertex_he, uint32_t* face_he,
                                   int32_t on_device, void* stream);
+/* The same for a caller's triangle list faces (nf x 3 vertex indices < nv),
+ * e.g. a mesh read from a file before PMPMesh construction or a merged
+ * large-scale mesh; s supplies the device and workspace only.  A face that
+ * repeats a vertex counts as a complex edge. */
+lvrgb_status lvrgb_halfedges(lvrgb_surface s, const uint32_t* faces, int64_t nf, int64_t nv, lvrgb_halfedge_info* info,
+                             uint32_t* he_vertex, uint32_t* he_next, uint32_t* he_prev, uint32_t* he_face,
+                             uint32_t* vertex_he, uint32_t* face_he, int32_t on_device, void* stream);
 
 /* HashGrid::toPointBuffer (include/lvr2/reconstruction/HashGrid.tcc:196-233),
  * the per-chunk grid the large-scale reconstruction stores and merges: for

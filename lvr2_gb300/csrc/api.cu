@@ -1008,6 +1008,39 @@ lvrgb_status lvrgb_get_grid(lvrgb_surface s, int32_t* lattice, float* position, 
     });
 }
 
+namespace {
+// Builds the half-edge arrays of faces (device) and copies them out.
+void halfedges_out(lvrgb_surface s, const uint32_t* faces, int nf, int nv, lvrgb_halfedge_info* info,
+                   uint32_t* he_vertex, uint32_t* he_next, uint32_t* he_prev, uint32_t* he_face, uint32_t* vertex_he,
+                   uint32_t* face_he, int32_t on_device, cudaStream_t st) {
+    HalfedgeMesh H;
+    build_halfedges(faces, nf, nv, s->ws, H, st);
+    if (info) {
+        info->vertices = H.nverts;
+        info->faces = H.nfaces;
+        info->edges = H.nedges;
+        info->boundary_halfedges = H.boundary;
+        info->complex_edges = H.complex_edges;
+        info->complex_vertices = H.complex_vertices;
+    }
+    require(H.complex_edges == 0, LVRGB_ERR_TOPOLOGY, "the mesh has complex edges");
+    const size_t nh = size_t(2 * H.nedges);
+    auto out = [&](uint32_t* dst, const uint32_t* src, size_t n, const char* name) {
+        if (!dst || n == 0) return;
+        uint32_t* d = stage_out(s->ws, name, dst, n, on_device);
+        LVRGB_CUDA(cudaMemcpyAsync(d, src, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+        finish_out(dst, d, n, on_device, st);
+    };
+    out(he_vertex, H.he_vertex, nh, "he.out.v");
+    out(he_next, H.he_next, nh, "he.out.n");
+    out(he_prev, H.he_prev, nh, "he.out.p");
+    out(he_face, H.he_face, nh, "he.out.f");
+    out(vertex_he, H.vertex_he, size_t(H.nverts), "he.out.vh");
+    out(face_he, H.face_he, size_t(H.nfaces), "he.out.fh");
+    if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+}
+}  // namespace
+
 lvrgb_status lvrgb_mesh_halfedges(lvrgb_surface s, lvrgb_halfedge_info* info, uint32_t* he_vertex, uint32_t* he_next,
                                   uint32_t* he_prev, uint32_t* he_face, uint32_t* vertex_he, uint32_t* face_he,
                                   int32_t on_device, void* stream) {
@@ -1016,32 +1049,28 @@ lvrgb_status lvrgb_mesh_halfedges(lvrgb_surface s, lvrgb_halfedge_info* info, ui
         require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
         require(s->has_grid, LVRGB_ERR_STATE, "no mesh: call lvrgb_reconstruct");
         DeviceScope dev(s->device);
+        halfedges_out(s, s->grid.faces, int(s->grid.nfaces), int(s->grid.nverts), info, he_vertex, he_next, he_prev,
+                      he_face, vertex_he, face_he, on_device, as_stream(stream));
+    });
+}
+
+lvrgb_status lvrgb_halfedges(lvrgb_surface s, const uint32_t* faces, int64_t nf, int64_t nv, lvrgb_halfedge_info* info,
+                             uint32_t* he_vertex, uint32_t* he_next, uint32_t* he_prev, uint32_t* he_face,
+                             uint32_t* vertex_he, uint32_t* face_he, int32_t on_device, void* stream) {
+    return guarded([&] {
+        NvtxRange nvtx_range("lvrgb.halfedges");
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(nf >= 0 && 3 * nf < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "face count out of range");
+        require(nv >= 0 && nv < (int64_t(1) << 31), LVRGB_ERR_INVALID_ARGUMENT, "vertex count out of range");
+        require(nf == 0 || faces != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL array");
+        DeviceScope dev(s->device);
         cudaStream_t st = as_stream(stream);
-        HalfedgeMesh H;
-        build_halfedges(s->grid.faces, int(s->grid.nfaces), int(s->grid.nverts), s->ws, H, st);
-        if (info) {
-            info->vertices = H.nverts;
-            info->faces = H.nfaces;
-            info->edges = H.nedges;
-            info->boundary_halfedges = H.boundary;
-            info->complex_edges = H.complex_edges;
-            info->complex_vertices = H.complex_vertices;
-        }
-        require(H.complex_edges == 0, LVRGB_ERR_TOPOLOGY, "the mesh has complex edges");
-        const size_t nh = size_t(2 * H.nedges);
-        auto out = [&](uint32_t* dst, const uint32_t* src, size_t n, const char* name) {
-            if (!dst || n == 0) return;
-            uint32_t* d = stage_out(s->ws, name, dst, n, on_device);
-            LVRGB_CUDA(cudaMemcpyAsync(d, src, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-            finish_out(dst, d, n, on_device, st);
-        };
-        out(he_vertex, H.he_vertex, nh, "he.out.v");
-        out(he_next, H.he_next, nh, "he.out.n");
-        out(he_prev, H.he_prev, nh, "he.out.p");
-        out(he_face, H.he_face, nh, "he.out.f");
-        out(vertex_he, H.vertex_he, size_t(H.nverts), "he.out.vh");
-        out(face_he, H.face_he, size_t(H.nfaces), "he.out.fh");
-        if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+        const uint32_t* df = stage_in(s->ws, "he.in.f", faces, size_t(nf) * 3, on_device, st);
+        if (nf > 0)
+            require(max_index(df, size_t(nf) * 3, s->ws, st) < uint64_t(nv), LVRGB_ERR_INVALID_ARGUMENT,
+                    "face index out of range");
+        halfedges_out(s, df, int(nf), int(nv), info, he_vertex, he_next, he_prev, he_face, vertex_he, face_he,
+                      on_device, st);
     });
 }
 

@@ -357,21 +357,31 @@ class Surface:
         self.info = info
         return info
 
-    def halfedges(self):
-        """Half-edge connectivity of the last mesh (pmp::SurfaceMesh layout):
-        dict of he_vertex, he_next, he_prev, he_face (2E), vertex_he (V),
-        face_he (F) and the counts."""
+    def halfedges(self, faces=None, nverts=None):
+        """Half-edge connectivity (pmp::SurfaceMesh layout) of the last mesh,
+        or of the triangles faces (F, 3) over nverts vertices: dict of
+        he_vertex, he_next, he_prev, he_face (2E), vertex_he (V), face_he (F)
+        and the counts."""
         L = _lib.load()
+        if faces is None:
+            def call(info, *arrs):
+                return L.lvrgb_mesh_halfedges(self._h, ctypes.byref(info), *arrs, 0, self._stream)
+        else:
+            f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+            if nverts is None:
+                nverts = int(f.max()) + 1 if len(f) else 0
+
+            def call(info, *arrs):
+                return L.lvrgb_halfedges(self._h, _ptr(f), len(f), int(nverts), ctypes.byref(info), *arrs, 0,
+                                         self._stream)
         info = HalfedgeInfo()
-        check(L.lvrgb_mesh_halfedges(self._h, ctypes.byref(info), None, None, None, None, None, None, 0,
-                                     self._stream))
+        check(call(info, None, None, None, None, None, None))
         nh = 2 * info.edges
         arrs = {k: np.empty(n, np.uint32) for k, n in (("he_vertex", nh), ("he_next", nh), ("he_prev", nh),
                                                        ("he_face", nh), ("vertex_he", info.vertices),
                                                        ("face_he", info.faces))}
-        check(L.lvrgb_mesh_halfedges(self._h, ctypes.byref(info), _ptr(arrs["he_vertex"]), _ptr(arrs["he_next"]),
-                                     _ptr(arrs["he_prev"]), _ptr(arrs["he_face"]), _ptr(arrs["vertex_he"]),
-                                     _ptr(arrs["face_he"]), 0, self._stream))
+        check(call(info, *(_ptr(arrs[k]) for k in ("he_vertex", "he_next", "he_prev", "he_face", "vertex_he",
+                                                    "face_he"))))
         arrs.update(edges=info.edges, boundary_halfedges=info.boundary_halfedges,
                     complex_edges=info.complex_edges, complex_vertices=info.complex_vertices)
         return arrs

@@ -43,3 +43,47 @@ def test_halfedges_need_a_mesh(gb):
         with pytest.raises(gb.LvrgbError) as e:
             s.halfedges()
         assert e.value.status == 5
+
+
+def _grid_mesh(n, rng, holes=0.15):
+    """Triangulated n x n grid with random faces removed (boundary loops,
+    bow-tie vertices where two holes touch) and shuffled face order and
+    orientation-preserving corner rotations."""
+    ij = np.arange(n * n).reshape(n, n)
+    a, b, c, d = ij[:-1, :-1].ravel(), ij[:-1, 1:].ravel(), ij[1:, :-1].ravel(), ij[1:, 1:].ravel()
+    F = np.concatenate([np.stack([a, b, d], 1), np.stack([a, d, c], 1)])
+    F = F[rng.random(len(F)) >= holes]
+    F = F[rng.permutation(len(F))]
+    r = rng.integers(0, 3, len(F))
+    F = np.stack([F[np.arange(len(F)), (r + j) % 3] for j in range(3)], 1)
+    return F.astype(np.uint32), n * n
+
+
+@pytest.mark.parametrize("n,holes,seed", [(2, 0.0, 0), (7, 0.3, 1), (40, 0.15, 2), (300, 0.05, 3)])
+def test_halfedges_of_given_faces_match_oracle(gb, oracle_mod, n, holes, seed):
+    rng = np.random.default_rng(seed)
+    F, nv = _grid_mesh(n, rng, holes)
+    P = rng.random((2000, 3)).astype(np.float32)
+    with gb.Surface(P, kn=10, ki=10, kd=10, nem=3) as s:
+        H = s.halfedges(F, nv + 5)  # trailing isolated vertices
+    ref = oracle_mod.halfedges(F, nv + 5)
+    assert H["complex_edges"] == 0 == ref["complex_edges"]
+    for k in ("edges", "boundary_halfedges", "complex_vertices"):
+        assert H[k] == ref[k], k
+    assert np.all(H["vertex_he"][nv:] == 0xFFFFFFFF)
+    for k in KEYS:
+        assert np.array_equal(H[k], ref[k]), k
+
+
+def test_halfedges_of_given_faces_errors(gb):
+    P = np.random.default_rng(0).random((2000, 3)).astype(np.float32)
+    with gb.Surface(P, kn=10, ki=10, kd=10, nem=3) as s:
+        H = s.halfedges(np.zeros((0, 3), np.uint32), 4)  # no faces: isolated vertices
+        assert H["edges"] == 0 and np.all(H["vertex_he"] == 0xFFFFFFFF)
+        for faces, status in (([[0, 1, 1]], 7),               # repeated vertex
+                              ([[0, 1, 2], [0, 1, 3]], 7),    # two faces of one orientation
+                              ([[0, 1, 2], [1, 0, 3], [0, 1, 4]], 7),  # three faces on an edge
+                              ([[0, 1, 9]], 1)):              # index out of range (nv = 5)
+            with pytest.raises(gb.LvrgbError) as e:
+                s.halfedges(np.array(faces, np.uint32), 5)
+            assert e.value.status == status, faces
