@@ -40,7 +40,7 @@ typedef enum lvrgb_status {
     LVRGB_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, k, voxel size or method */
     LVRGB_ERR_CUDA = 2,             /* a CUDA runtime call failed */
     LVRGB_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed (lvr2 retries smaller chunks) */
-    LVRGB_ERR_UNSUPPORTED = 4,      /* e.g. nem 1 (RANSAC) */
+    LVRGB_ERR_UNSUPPORTED = 4,      /* e.g. nem 1 (RANSAC) on a scan project */
     LVRGB_ERR_STATE = 5,            /* call order: no normals yet, no mesh yet */
     LVRGB_ERR_KERNEL = 6,           /* a kernel reported an internal limit (traversal depth) */
     LVRGB_ERR_TOPOLOGY = 7          /* complex edges: pmp's add_face would throw TopologyException */
@@ -58,11 +58,17 @@ typedef struct lvrgb_surface_config {
     int32_t kn;            /* normal estimation neighbourhood (first search uses 2*kn) */
     int32_t ki;            /* interpolation neighbourhood, 0 = no interpolation */
     int32_t kd;            /* signed-distance neighbourhood */
-    int32_t nem;           /* plane fit: 0 least squares (lvr2 default), 2 iterative, 3 PCA,
+    int32_t nem;           /* plane fit: 0 least squares (lvr2 default), 1 RANSAC, 2 iterative, 3 PCA,
                               4 the LBVH comparator's FP64 fit (LBVHIndex::knn_normals,
                               src/liblvr2/reconstruction/cuda/lbvh/knn_normals_kernel.cu:54-206;
                               CudaKSearchSurface, --pcm LBVH_CUDA): one search with k = kn <= 96,
-                              no adaptive rounds, slot 0 (the query) left out */
+                              no adaptive rounds, slot 0 (the query) left out.
+                              1: calcPlaneRANSAC (AdaptiveKSearchSurface.tcc:689-781) with
+                              lvr2's draws (a default-seeded std::default_random_engine per
+                              call, libstdc++) and indexing (plane points = the cloud's
+                              points at the drawn neighbour ranks); needs min(2kn, n) >= 3.
+                              lvr2 reads the fit's `ok` flag uninitialised (:222-231): the
+                              RANSAC plane is kept here; the fallback reading is nem 0 */
     int32_t adaptive;      /* 1: k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed */
     int32_t flip_set;      /* 0: flip point = bounding-box centroid (AdaptiveKSearchSurface::init) */
     float flip[3];         /* flip point when flip_set != 0 */
@@ -112,8 +118,8 @@ lvrgb_status lvrgb_surface_set_flip_point(lvrgb_surface s, float x, float y, flo
 lvrgb_status lvrgb_surface_set_scan_poses(lvrgb_surface s, const float* poses, int64_t np);
 
 /* Plane-fit method: AdaptiveKSearchSurface calcMethod / CudaSurface::setMethod
- * (CudaSurface.hpp:144).  nem 1 (RANSAC) returns LVRGB_ERR_UNSUPPORTED; nem 4 is
- * the fit of CudaKSearchSurface (see lvrgb_surface_config). */
+ * (CudaSurface.hpp:144), 0..4 as in lvrgb_surface_config; nem 4 is the fit of
+ * CudaKSearchSurface. */
 lvrgb_status lvrgb_surface_set_method(lvrgb_surface s, int32_t nem);
 
 /* PointsetSurface::getBoundingBox (PointsetSurface.hpp:106): out9 = min xyz,
@@ -440,8 +446,8 @@ typedef struct lvrgb_batch_s* lvrgb_batch;
 /* xyz: all scans concatenated (n x 3); scan_offsets: nscans + 1 entries,
  * scan_offsets[0] = 0, strictly increasing; flip_points: nscans x 3 (the
  * scanner positions).  cfg: kn, ki (<= 2 kn), kd (lvrgb_batch_grid_distances),
- * nem, adaptive, bucket, seed_radius, device as for a surface (flip fields
- * ignored).  Host arrays
+ * nem (not 1), adaptive, bucket, seed_radius, device as for a surface (flip
+ * fields ignored).  Host arrays
  * for offsets and flips; xyz on host or device (on_device). */
 lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xyz, const int64_t* scan_offsets,
                                 int32_t nscans, const float* flip_points, int32_t on_device, void* stream,

@@ -252,7 +252,7 @@ class CudaSurface {
     void setKi(int ki) { s_.setKi(ki); }
     void setKd(int kd) { s_.setKd(kd); }
     void setFlippoint(float x, float y, float z) { s_.setFlipPoint(Vec3{x, y, z}); }
-    // "PCA" -> nem 3; "RANSAC" is rejected (LVRGB_ERR_UNSUPPORTED)
+    // "PCA" -> nem 3; "RANSAC" -> nem 1 (calcPlaneRANSAC)
     void setMethod(const std::string& method) { s_.setCalcMethod(method == "RANSAC" ? 1 : 3); }
     void setReconstructionMode(bool) {}
     void distances(std::vector<QueryPoint>& query_points, float voxel_size) {

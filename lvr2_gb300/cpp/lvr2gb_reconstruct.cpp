@@ -45,7 +45,7 @@ struct Options {
 void usage() {
     std::puts(
         "usage: lvr2gb_reconstruct <inputFile> [--voxelsize|-v F] [--intersections|-i N] [--pcm|-p NAME]\n"
-        "       [--nem 0|2|3|4] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
+        "       [--nem 0|1|2|3|4] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
         "       [--flipPoint X Y Z] [--recalcNormals|-r] [--exportPointNormals|-e] [--outputFile PATH]\n"
         "       [--scanPoseFile PATH] [--useGPU] [--threads N] [--device N]");
 }

@@ -139,8 +139,9 @@ void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
     LVRGB_CUDA(cudaStreamSynchronize(st));
     if (h[0]) {
         LVRGB_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int), st));
-        throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack) ? "kNN traversal exceeded its stack depth"
-                                                            : "tree walk exceeded its bound (malformed tree)"};
+        throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack)  ? "kNN traversal exceeded its stack depth"
+                                         : (h[0] & kErrWalk) ? "tree walk exceeded its bound (malformed tree)"
+                                                             : "a neighbour row was shorter than the RANSAC draws"};
     }
 }
 
@@ -220,8 +221,7 @@ NormalsConfig normals_config(const lvrgb_surface_s* s) {
 }
 
 void check_nem(int nem) {
-    require(nem != 1, LVRGB_ERR_UNSUPPORTED, "nem 1 (RANSAC plane fit) is not supported");
-    require(nem == 0 || nem == 2 || nem == 3 || nem == 4, LVRGB_ERR_INVALID_ARGUMENT, "nem must be 0, 2, 3 or 4");
+    require(nem >= 0 && nem <= 4, LVRGB_ERR_INVALID_ARGUMENT, "nem must be 0, 1, 2, 3 or 4");
 }
 
 // k of the first normal search: 2 kn (adaptive k doubles before every
@@ -426,6 +426,8 @@ lvrgb_status lvrgb_calculate_normals(lvrgb_surface s, void* stream) {
         cudaStream_t st = as_stream(stream);
         LVRGB_CUDA(cudaMemsetAsync(s->d_stats, 0, kNormalStats * sizeof(uint32_t), st));
         check_lbvh_k(s->cfg.kn, s->cfg.nem);
+        require(s->cfg.nem != 1 || s->T.n == 0 || std::min<int64_t>(2 * int64_t(s->cfg.kn), s->T.n) >= 3,
+                LVRGB_ERR_INVALID_ARGUMENT, "nem 1 needs at least 3 neighbours (kn >= 2 and 3 points)");
         NormalsConfig c = normals_config(s);
         if (!s->poses.empty() && s->T.n > 0) {
             const int np = int(s->poses.size() / 3);
@@ -1241,6 +1243,7 @@ lvrgb_status lvrgb_batch_create(const lvrgb_surface_config* cfg, const float* xy
         require(nscans >= 1 && nscans <= 65535, LVRGB_ERR_INVALID_ARGUMENT, "nscans must be in 1..65535");
         require(cfg->kn > 0 && cfg->ki >= 0, LVRGB_ERR_INVALID_ARGUMENT, "kn must be > 0, ki >= 0");
         check_nem(cfg->nem);
+        require(cfg->nem != 1, LVRGB_ERR_UNSUPPORTED, "nem 1 (RANSAC) runs on single surfaces, not on scan projects");
         check_lbvh_k(cfg->kn, cfg->nem);
         require(cfg->ki <= first_search_k(cfg->kn, cfg->nem), LVRGB_ERR_UNSUPPORTED,
                 "scan projects interpolate from the estimation's neighbour lists: ki must be <= 2 * kn "

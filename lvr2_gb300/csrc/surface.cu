@@ -3,7 +3,11 @@
 // getInterpolatedNormal, all on the warp-cooperative LBVH traversal.
 #include <algorithm>
 #include <cstring>
+#include <functional>
+#include <random>
 #include <stdexcept>
+#include <unordered_set>
+#include <vector>
 
 #include "primitives.cuh"
 #include "surface.h"
@@ -1202,12 +1206,185 @@ void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) 
     }
 }
 
+// ---------------------------------------------------------------------------
+// nem 1: calcPlaneRANSAC (AdaptiveKSearchSurface.tcc:689-781).
+//
+// The reference default-constructs its engine on every call and binds copies
+// of it and of uniform_int_distribution(0, |id| - 1) (:713-715), so its draws
+// depend on the neighbour count m = |id| alone.  Per iteration: draws into an
+// unordered_set until it holds three values (at most 21 draws), the set's
+// elements in its iteration order, then min(50, m) scoring draws.  The host
+// replays them with the same standard-library types (libstdc++, which lvr2
+// is built with on Linux) into a schedule; ransac_rows_kernel evaluates the
+// iterations per query.  As in the reference, the plane points are
+// m_points[r] for the drawn r -- the cloud's points 0..m-1, not the query's
+// neighbours (:736-738) -- and the scoring points are the neighbours at the
+// drawn ranks (:745-750).  lvr2 reads the `ok` flag without calcPlaneRANSAC
+// setting it (:222-231); the RANSAC plane is kept (the other reading of the
+// flag is calcPlane, nem 0).
+constexpr int kRansacIters = 10;
+constexpr int kRansacScore = 50;
+constexpr int kRansacStride = 3 + kRansacScore;  // plane draws, then scoring draws
+
+std::vector<uint32_t> ransac_schedule(size_t m) {
+    if (m < 3) throw std::invalid_argument("nem 1 needs at least 3 neighbours (kn >= 2 and 3 points)");
+    std::vector<uint32_t> out(size_t(kRansacIters) * kRansacStride, 0u);
+    std::default_random_engine generator;
+    std::uniform_int_distribution<size_t> distribution(0, m - 1);
+    auto number = std::bind(distribution, generator);
+    std::unordered_set<size_t> ids;
+    const int ns = int(std::min<size_t>(kRansacScore, m));
+    for (int t = 0; t < kRansacIters; t++) {
+        uint32_t* row = out.data() + size_t(t) * kRansacStride;
+        ids.clear();
+        int c = 0;
+        do {
+            ids.insert(number());
+            c++;
+        } while (ids.size() < 3 && c <= 20);
+        if (ids.size() < 3)
+            throw std::invalid_argument("nem 1: no three distinct plane draws (lvr2 would read past its draw set)");
+        auto it = ids.begin();
+        for (int j = 0; j < 3; j++, ++it) row[j] = uint32_t(*it);
+        for (int j = 0; j < ns; j++) row[3 + j] = uint32_t(number());
+    }
+    return out;
+}
+
+__device__ __forceinline__ float4 point_of(const Lbvh& T, uint32_t orig) { return __ldg(T.pts + __ldg(T.inv + orig)); }
+
+__device__ __forceinline__ float dot_ieee(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// One thread per query: list[i] = its Morton position, rows + i * K its
+// neighbours (original indices, ascending (d2, index)).  Float arithmetic in
+// the reference's order: BaseVector cross, Normal normalisation (the null
+// vector stays null), dot products left to right.
+__global__ void ransac_rows_kernel(Lbvh T, const uint32_t* __restrict__ list, int nq, const uint32_t* __restrict__ rows,
+                                   int K, const uint32_t* __restrict__ sched, int ns, float fx, float fy, float fz,
+                                   const float4* __restrict__ flip_target, float4* __restrict__ normals,
+                                   int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const int pos = int(list[i]);
+    const uint32_t* row = rows + size_t(i) * size_t(K);
+    float bx = 0.0f, by = 0.0f, bz = 1.0f;  // Normal(0, 0, 1)
+    float best = FLT_MAX;
+    int nonimproving = 0;
+    for (int t = 0; t < kRansacIters && nonimproving < 5; t++) {
+        const uint32_t* S = sched + t * kRansacStride;
+        const float4 p1 = point_of(T, S[0]), p2 = point_of(T, S[1]), p3 = point_of(T, S[2]);
+        const float ux = __fsub_rn(p1.x, p2.x), uy = __fsub_rn(p1.y, p2.y), uz = __fsub_rn(p1.z, p2.z);
+        const float vx = __fsub_rn(p1.x, p3.x), vy = __fsub_rn(p1.y, p3.y), vz = __fsub_rn(p1.z, p3.z);
+        float nx = __fsub_rn(__fmul_rn(uy, vz), __fmul_rn(uz, vy));
+        float ny = __fsub_rn(__fmul_rn(uz, vx), __fmul_rn(ux, vz));
+        float nz = __fsub_rn(__fmul_rn(ux, vy), __fmul_rn(uy, vx));
+        normalize_ieee(nx, ny, nz);
+        const float d1 = dot_ieee(p1.x, p1.y, p1.z, nx, ny, nz);
+        float dist = 0.0f;
+        for (int j = 0; j < ns; j++) {
+            const uint32_t id = row[S[3 + j]];
+            if (id >= uint32_t(T.n)) {
+                atomicOr(err, kErrRows);
+                return;
+            }
+            const float4 r = point_of(T, id);
+            dist = __fadd_rn(dist, fabsf(__fsub_rn(dot_ieee(r.x, r.y, r.z, nx, ny, nz), d1)));
+        }
+        dist = __fdiv_rn(dist, float(ns));
+        if (dist < best) {
+            best = dist;
+            bx = nx; by = ny; bz = nz;
+            nonimproving = 0;
+        } else {
+            nonimproving++;
+        }
+    }
+    const float4 q = __ldg(T.pts + pos);
+    if (flip_target) {
+        const float4 t = __ldg(flip_target + pos);
+        if (t.w != 0.0f) {
+            fx = t.x; fy = t.y; fz = t.z;
+        }
+    }
+    // Flip toward the flip point; Normal::operator-() re-normalises.
+    if (dot_ieee(bx, by, bz, __fsub_rn(fx, q.x), __fsub_rn(fy, q.y), __fsub_rn(fz, q.z)) < 0.0f) {
+        bx = -bx; by = -by; bz = -bz;
+        normalize_ieee(bx, by, bz);
+    }
+    normals[pos] = make_float4(bx, by, bz, 0.0f);
+}
+
+__global__ void kused_flags_kernel(const int32_t* __restrict__ kused, int n, int K, uint8_t* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flags[i] = kused[i] == K ? 1 : 0;
+}
+
+// Queries at the listed Morton positions, row i tagged in w.
+__global__ void list_queries_kernel(const float4* __restrict__ pts, const uint32_t* __restrict__ list, int nq,
+                                    float4* __restrict__ qs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const float4 p = __ldg(pts + list[i]);
+    qs[i] = make_float4(p.x, p.y, p.z, __uint_as_float(uint32_t(i)));
+}
+
+// Replaces the normals of the points fitted with k = K in the adaptive rounds
+// by calcPlaneRANSAC over their sorted K-neighbourhoods.
+void ransac_normals(const Lbvh& T, const NormalsConfig& cfg, const int32_t* kused, float4* normals, Workspace& ws,
+                    int* d_err, cudaStream_t s) {
+    const int n = T.n;
+    std::vector<int> ks;
+    size_t k = size_t(cfg.kn);
+    for (int round = 1; round <= (cfg.adaptive ? 5 : 1); round++) {
+        k *= 2;
+        ks.push_back(int(std::min<size_t>(k, size_t(1) << 20)));
+    }
+    const size_t kRowEntries = size_t(1) << 25;  // neighbour entries per chunk (128 MB of indices)
+    size_t max_entries = 0;
+    for (int K : ks) max_entries = std::max(max_entries, std::min(size_t(n), std::max<size_t>(1, kRowEntries / K)) * K);
+    uint8_t* flags = ws.get<uint8_t>("ransac.flags", size_t(n));
+    uint32_t* list = ws.get<uint32_t>("ransac.list", size_t(n));
+    uint32_t* counter = ws.get<uint32_t>("ransac.count", 1);
+    uint32_t* sched = ws.get<uint32_t>("ransac.sched", size_t(kRansacIters) * kRansacStride);
+    uint32_t* rows = ws.get<uint32_t>("ransac.rows", max_entries);
+    float* dist = ws.get<float>("ransac.dist", max_entries);
+    float4* qs = ws.get<float4>("ransac.qs", std::min(size_t(n), max_entries));
+    uint64_t* h = ws.pinned();
+    for (int K : ks) {
+        const size_t m = std::min(size_t(K), size_t(n));
+        const std::vector<uint32_t> S = ransac_schedule(m);
+        const int ns = int(std::min<size_t>(kRansacScore, m));
+        kused_flags_kernel<<<ceil_div(n, 256), 256, 0, s>>>(kused, n, K, flags);
+        LVRGB_LAUNCH_CHECK();
+        compact_retry(flags, nullptr, n, nullptr, list, counter, ws, s);
+        h[0] = 0;
+        LVRGB_CUDA(cudaMemcpyAsync(h, counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        LVRGB_CUDA(cudaMemcpyAsync(sched, S.data(), S.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        LVRGB_CUDA(cudaStreamSynchronize(s));
+        const int cnt = int(uint32_t(h[0]));
+        const int chunk = int(std::min(size_t(n), std::max<size_t>(1, kRowEntries / K)));
+        for (int off = 0; off < cnt; off += chunk) {
+            const int c = std::min(chunk, cnt - off);
+            list_queries_kernel<<<ceil_div(c, 256), 256, 0, s>>>(T.pts, list + off, c, qs);
+            LVRGB_LAUNCH_CHECK();
+            knn_rows(T, qs, c, K, rows, dist, nullptr, ws, d_err, s);
+            ransac_rows_kernel<<<ceil_div(c, 128), 128, 0, s>>>(T, list + off, c, rows, K, sched, ns, cfg.flip[0],
+                                                                cfg.flip[1], cfg.flip[2], cfg.flip_target, normals,
+                                                                d_err);
+            LVRGB_LAUNCH_CHECK();
+        }
+    }
+}
+
 }  // namespace
 
 void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws,
                      int* d_err, uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki) {
     const int n = T.n;
     if (n == 0) return;
+    if (cfg.nem == 1 && !kused) kused = ws.get<int32_t>("normals.kused", size_t(n));
     uint32_t* lists[2] = {ws.get<uint32_t>("normals.listA", size_t(n)), ws.get<uint32_t>("normals.listB", size_t(n))};
     uint32_t* counter = ws.get<uint32_t>("normals.counter", 2);
     uint8_t* flags = ws.get<uint8_t>("normals.flags", size_t(n));
@@ -1225,7 +1402,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         NormalsArgs A;
         A.T = T;
         A.K = K;
-        A.nem = cfg.nem;
+        A.nem = cfg.nem == 1 ? 0 : cfg.nem;  // nem 1 fits afterwards (ransac_normals)
         A.adaptive = cfg.adaptive;
         A.last_round = last;
         A.round = round;
@@ -1254,6 +1431,8 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         nq = int(uint32_t(h_count[0]));
         list = retry;
     }
+    // nem 1: the rounds above (run as nem 0) fixed each point's k
+    if (cfg.nem == 1) ransac_normals(T, cfg, kused, normals, ws, d_err, s);
 }
 
 void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,

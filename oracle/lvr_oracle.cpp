@@ -25,6 +25,7 @@
  *   include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:337-350  boundingBoxOK
  *   include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:414-457  distance
  *   include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:467-673  plane fits
+ *   include/lvr2/reconstruction/AdaptiveKSearchSurface.tcc:689-781  RANSAC plane fit
  *   include/lvr2/reconstruction/PointsetSurface.tcc:39-74           bbox, getInterpolatedNormal
  *   include/lvr2/geometry/BaseVector.tcc, Normal.tcc, BoundingBox.tcc:158-252
  *   include/lvr2/reconstruction/HashGrid.tcc:48-80, 235-378, HashGrid.hpp:263-287
@@ -35,6 +36,8 @@
 #include "lvr_oracle.h"
 
 #include <algorithm>
+#include <random>
+#include <functional>
 #include <array>
 #include <cfloat>
 #include <cmath>
@@ -384,6 +387,56 @@ static V3 plane_lsq(const std::vector<V3>& P, const std::vector<uint32_t>& id, c
     return diff1.cross(diff2).normalized();
 }
 
+// calcPlaneRANSAC, nem 1 (AdaptiveKSearchSurface.tcc:689-781), as the
+// reference runs it: a default-constructed std::default_random_engine per
+// call, bound by copy with uniform_int_distribution(0, |id| - 1) (:713-715);
+// the three plane points are P[r] for draws r in [0, |id|) -- indices of the
+// whole cloud (:736-738) -- and the scoring points P[id[r]] (:745-750).
+// Returns false where the reference would read past its draw set (fewer than
+// three distinct draws within 21).  The caller keeps the RANSAC plane: lvr2
+// never sets `ok` (:222-231).
+static bool plane_ransac(const std::vector<V3>& P, const std::vector<uint32_t>& id, V3& out) {
+    if (id.size() < 3) return false;
+    V3 best_norm(0, 0, 1);
+    float bestdist = FLT_MAX;
+    int iterations = 0, nonimproving = 0;
+    std::unordered_set<size_t> draws;
+    std::default_random_engine engine;
+    std::uniform_int_distribution<size_t> uniform(0, id.size() - 1);
+    auto next = std::bind(uniform, engine);
+    while (nonimproving < 5 && iterations < 10) {
+        int c = 0;
+        draws.clear();
+        do {
+            draws.insert(next());
+            c++;
+        } while (draws.size() < 3 && c <= 20);
+        if (draws.size() < 3) return false;
+        auto it = draws.begin();
+        const V3 a = P[*it];
+        const V3 b = P[*(++it)];
+        const V3 c3 = P[*(++it)];
+        const V3 n0 = (a - b).cross(a - c3).normalized();
+        float dist = 0;
+        const int n = std::min(50, int(id.size()));
+        for (int i = 0; i < n; i++) {
+            const V3 r = P[id[next()]];
+            dist += std::fabs(r.dot(n0) - a.dot(n0));
+        }
+        if (n != 0) dist /= float(n);
+        if (dist < bestdist) {
+            bestdist = dist;
+            best_norm = n0;
+            nonimproving = 0;
+        } else {
+            nonimproving++;
+        }
+        iterations++;
+    }
+    out = best_norm;
+    return true;
+}
+
 // calcPlaneIterative, nem 2 (AdaptiveKSearchSurface.tcc:522-607)
 static V3 plane_iterative(const std::vector<V3>& P, const std::vector<uint32_t>& id, const V3& q) {
     float xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0;
@@ -529,7 +582,7 @@ int orc_knn(const orc_surface* s, const float* q, int64_t nq, int k, int canonic
 
 int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float* flip3,
                 int canonical, float* normals, int32_t* k_used, int threads, const float* flip_targets) {
-    if (nem != 0 && nem != 2 && nem != 3) return -1;
+    if (nem < 0 || nem > 3) return -1;
     set_threads(threads);
     const std::vector<V3>& P = s->pts;
     const V3 flip = flip3 ? V3(flip3[0], flip3[1], flip3[2]) : s->bb.centroid;
@@ -552,7 +605,9 @@ int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float
         }
         const V3& qp = P[size_t(i)];
         V3 nrm;
-        if (nem == 2) nrm = plane_iterative(P, id, qp);
+        if (nem == 1) {
+            if (!plane_ransac(P, id, nrm)) nrm = V3(NAN, NAN, NAN);
+        } else if (nem == 2) nrm = plane_iterative(P, id, qp);
         else if (nem == 3) nrm = plane_ipca(P, id, qp);
         else nrm = plane_lsq(P, id, qp);
         // Flip toward the flip point (AdaptiveKSearchSurface.tcc:268-274), or

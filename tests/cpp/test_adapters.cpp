@@ -128,13 +128,18 @@ int main() {
     qp[2].m_position = {0.5f, 0.5f, 0.5f};
     gs.distances(qp, 0.02f);
     EXPECT(!qp[0].m_invalid && !qp[1].m_invalid && qp[2].m_invalid);
-    bool threw = false;
-    try {
-        gs.setMethod("RANSAC");
-    } catch (const std::runtime_error&) {
-        threw = true;
+    // setMethod("RANSAC"): calcPlaneRANSAC (nem 1); unit normals, or the null
+    // normal where a degenerate candidate plane wins
+    gs.setMethod("RANSAC");
+    gs.calculateNormals();
+    gs.getNormals(out);
+    size_t unit = 0;
+    for (size_t i = 0; i < n; i++) {
+        const float* v = &out[3 * i];
+        const float len = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        unit += std::fabs(len - 1.0f) < 1e-5f || len == 0.0f;
     }
-    EXPECT(threw);
+    EXPECT(unit == n);
 
     if (failures) {
         std::fprintf(stderr, "%d check(s) failed\n", failures);

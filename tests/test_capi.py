@@ -43,11 +43,11 @@ def test_invalid_arguments_return_status(lib):
     st = lib.lvrgb_surface_create(ctypes.byref(cfg), pts.ctypes.data_as(ctypes.c_void_p), -1, 0, None,
                                   ctypes.byref(h))
     assert st == 1 and h.value is None
-    # RANSAC plane fit is not supported
-    cfg.nem = 1
+    # plane-fit methods are 0..4
+    cfg.nem = 5
     st = lib.lvrgb_surface_create(ctypes.byref(cfg), pts.ctypes.data_as(ctypes.c_void_p), 4, 0, None,
                                   ctypes.byref(h))
-    assert st == 4 and b"RANSAC" in lib.lvrgb_last_error()
+    assert st == 1 and b"nem" in lib.lvrgb_last_error()
     cfg.nem = 3
     cfg.kn = 0
     st = lib.lvrgb_surface_create(ctypes.byref(cfg), pts.ctypes.data_as(ctypes.c_void_p), 4, 0, None,
@@ -61,5 +61,5 @@ def test_invalid_arguments_return_status(lib):
 def test_python_mirror_raises_on_status(lib):
     import lvr2_gb300
     with pytest.raises(lvr2_gb300.LvrgbError) as e:
-        lvr2_gb300.Surface(np.zeros((4, 3), np.float32), nem=1)
-    assert e.value.status == 4
+        lvr2_gb300.Surface(np.zeros((4, 3), np.float32), nem=7)
+    assert e.value.status == 1

@@ -134,7 +134,7 @@ def test_grid_invalid_rule_and_culling(oracle_mod):
 def test_unsupported_method(oracle_mod):
     s = oracle_mod.OracleSurface(GOLD["sphere/points"])
     with pytest.raises(ValueError):
-        s.normals(5, nem=1)
+        s.normals(5, nem=5)
 
 
 def test_lbvh_comparator_fit_restatement(oracle_mod):
@@ -268,3 +268,32 @@ def test_halfedge_restatement_topology_cases(oracle_mod):
             if h == b:
                 break
     assert seen == set(bnd.tolist())
+
+
+def test_ransac_restatement_properties(oracle_mod):
+    """nem 1 (calcPlaneRANSAC): on a plane every candidate plane is the plane
+    itself, so the normals are exactly (0, 0, +-1), oriented to the flip
+    point; the three plane points are the cloud's points at the drawn ranks
+    (lvr2 indexes m_points with them), so with the cloud's first four points
+    on a line and k = 4 every candidate is degenerate: the null normal scores
+    0 and wins everywhere; fewer than three neighbours: no plane (NaN)."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    P = np.zeros((3000, 3), np.float32)
+    P[:, :2] = rng.uniform(-1, 1, (3000, 2))
+    o = oracle_mod.OracleSurface(P)
+    for kn, adaptive in ((10, False), (4, True)):
+        n = o.normals(kn, nem=1, adaptive=adaptive, flip=np.array([0, 0, 5], np.float32))
+        assert np.array_equal(n, np.tile(np.float32([0, 0, 1]), (len(P), 1)))
+    n = o.normals(10, nem=1, adaptive=False, flip=np.array([0, 0, -5], np.float32))
+    assert np.array_equal(n, np.tile(np.float32([0, 0, -1]), (len(P), 1)))
+
+    Q = rng.uniform(-1, 1, (2000, 3)).astype(np.float32)
+    Q[:4] = np.float32([[0, 0, 0], [0.5, 0, 0], [-0.25, 0, 0], [0.75, 0, 0]])
+    n = oracle_mod.OracleSurface(Q).normals(2, nem=1, adaptive=False)
+    assert np.array_equal(n, np.zeros_like(n))
+    # the same cloud with the line moved away from the front: real planes
+    n = oracle_mod.OracleSurface(np.roll(Q, 7, axis=0)).normals(2, nem=1, adaptive=False)
+    assert np.isfinite(n).all() and (np.abs(np.linalg.norm(n, axis=1) - 1) < 1e-6).mean() > 0.9
+
+    n = oracle_mod.OracleSurface(Q).normals(1, nem=1, adaptive=False)  # k = 2 neighbours
+    assert np.isnan(n).all()
