@@ -67,7 +67,7 @@ typedef struct lvrgb_surface_config {
                               lvr2's draws (a default-seeded std::default_random_engine per
                               call, libstdc++) and indexing (plane points = the cloud's
                               points at the drawn neighbour ranks); needs min(2kn, n) >= 3.
-                              lvr2 reads the fit's `ok` flag uninitialised (:222-231): the
+                              lvr2 reads the fit's `ok` flag uninitialised (:223-231): the
                               RANSAC plane is kept here; the fallback reading is nem 0 */
     int32_t adaptive;      /* 1: k = 2kn, 4kn, ... 32kn until the neighbourhood box is well formed */
     int32_t flip_set;      /* 0: flip point = bounding-box centroid (AdaptiveKSearchSurface::init) */

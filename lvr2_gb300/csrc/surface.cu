@@ -1210,7 +1210,7 @@ void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) 
 // nem 1: calcPlaneRANSAC (AdaptiveKSearchSurface.tcc:689-781).
 //
 // The reference default-constructs its engine on every call and binds copies
-// of it and of uniform_int_distribution(0, |id| - 1) (:713-715), so its draws
+// of it and of uniform_int_distribution(0, |id| - 1) (:715-717), so its draws
 // depend on the neighbour count m = |id| alone.  Per iteration: draws into an
 // unordered_set until it holds three values (at most 21 draws), the set's
 // elements in its iteration order, then min(50, m) scoring draws.  The host
@@ -1218,9 +1218,9 @@ void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s) 
 // is built with on Linux) into a schedule; ransac_rows_kernel evaluates the
 // iterations per query.  As in the reference, the plane points are
 // m_points[r] for the drawn r -- the cloud's points 0..m-1, not the query's
-// neighbours (:736-738) -- and the scoring points are the neighbours at the
-// drawn ranks (:745-750).  lvr2 reads the `ok` flag without calcPlaneRANSAC
-// setting it (:222-231); the RANSAC plane is kept (the other reading of the
+// neighbours (:736-740) -- and the scoring points are the neighbours at the
+// drawn ranks (:746-753).  lvr2 reads the `ok` flag without calcPlaneRANSAC
+// setting it (:223-231); the RANSAC plane is kept (the other reading of the
 // flag is calcPlane, nem 0).
 constexpr int kRansacIters = 10;
 constexpr int kRansacScore = 50;

@@ -389,12 +389,12 @@ static V3 plane_lsq(const std::vector<V3>& P, const std::vector<uint32_t>& id, c
 
 // calcPlaneRANSAC, nem 1 (AdaptiveKSearchSurface.tcc:689-781), as the
 // reference runs it: a default-constructed std::default_random_engine per
-// call, bound by copy with uniform_int_distribution(0, |id| - 1) (:713-715);
+// call, bound by copy with uniform_int_distribution(0, |id| - 1) (:715-717);
 // the three plane points are P[r] for draws r in [0, |id|) -- indices of the
-// whole cloud (:736-738) -- and the scoring points P[id[r]] (:745-750).
+// whole cloud (:736-740) -- and the scoring points P[id[r]] (:746-753).
 // Returns false where the reference would read past its draw set (fewer than
 // three distinct draws within 21).  The caller keeps the RANSAC plane: lvr2
-// never sets `ok` (:222-231).
+// never sets `ok` (:223-231).
 static bool plane_ransac(const std::vector<V3>& P, const std::vector<uint32_t>& id, V3& out) {
     if (id.size() < 3) return false;
     V3 best_norm(0, 0, 1);
