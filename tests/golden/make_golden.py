@@ -5,7 +5,7 @@
                                  from the lvr2 headers by `make -C oracle ref`
                                  (run here, where the lvr2 tree is present).
   tests/golden/oracle_small.npz  oracle results on small seeded clouds: kNN
-                                 rows, normals (nem 0/2/3, adaptive k), the
+                                 rows, normals (nem 0/1/2/3, adaptive k), the
                                  interpolation, signed distances, the grid and
                                  the marching-cubes mesh.
 
@@ -56,7 +56,7 @@ def main():
         out[name + "/knn_idx"] = idx
         out[name + "/knn_dist"] = dist
         flip = np.array([0.5, 0.5, 0.5], np.float32) if name == "sphere" else np.zeros(3, np.float32)
-        for nem in (0, 2, 3):
+        for nem in (0, 1, 2, 3):
             n, k = s.normals(5, nem=nem, adaptive=True, flip=flip, with_k=True)
             out["%s/normals_nem%d" % (name, nem)] = n
             out["%s/kused_nem%d" % (name, nem)] = k

@@ -105,3 +105,19 @@ def test_ransac_errors(gb):
     with pytest.raises(gb.LvrgbError) as e:
         gb.Batch([P[:1000], P[1000:2000]], np.zeros((2, 3), np.float32), kn=10, ki=10, nem=1)
     assert e.value.status == 4
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_ransac_golden(gb, name):
+    """The committed frozen oracle outputs (tests/golden/oracle_small.npz,
+    kn = 5, adaptive): on the lattice the cloud's first points are collinear,
+    so many candidate planes are degenerate and null normals win."""
+    from pathlib import Path
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "oracle_small.npz")
+    P = gold[name + "/points"]
+    flip = np.float32([0.5, 0.5, 0.5]) if name == "sphere" else np.zeros(3, np.float32)
+    with gb.Surface(P, kn=5, ki=0, nem=1, flip_point=flip) as s:
+        s.calculate_normals()
+        gn, gk = s.raw_normals()
+    assert (gk == gold[name + "/kused_nem1"]).all()
+    assert bits_equal(gn, gold[name + "/normals_nem1"])

@@ -82,7 +82,7 @@ def test_oracle_reproduces_frozen_outputs(oracle_mod):
         idx, dist, _ = s.knn(pts[::7], 8)
         assert (idx == GOLD[name + "/knn_idx"]).all() and (dist == GOLD[name + "/knn_dist"]).all()
         flip = np.array([0.5, 0.5, 0.5], np.float32) if name == "sphere" else np.zeros(3, np.float32)
-        for nem in (0, 2, 3):
+        for nem in (0, 1, 2, 3):
             n, k = s.normals(5, nem=nem, adaptive=True, flip=flip, with_k=True)
             assert (k == GOLD["%s/kused_nem%d" % (name, nem)]).all()
             assert np.array_equal(n, GOLD["%s/normals_nem%d" % (name, nem)], equal_nan=True)
