@@ -626,6 +626,33 @@ int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float
     return 0;
 }
 
+int orc_ransac_draws(int64_t m, uint32_t* out) {
+    // The draws plane_ransac consumes for a neighbour list of m entries,
+    // all 10 iterations: 3 plane ranks (set order), then min(50, m) scoring
+    // ranks; 53 entries per iteration.  Returns -1 where plane_ransac fails.
+    if (m < 3) return -1;
+    std::unordered_set<size_t> draws;
+    std::default_random_engine engine;
+    std::uniform_int_distribution<size_t> uniform(0, size_t(m) - 1);
+    auto next = std::bind(uniform, engine);
+    const int n = int(std::min<int64_t>(50, m));
+    for (int t = 0; t < 10; t++) {
+        uint32_t* row = out + 53 * t;
+        std::fill(row, row + 53, 0u);
+        int c = 0;
+        draws.clear();
+        do {
+            draws.insert(next());
+            c++;
+        } while (draws.size() < 3 && c <= 20);
+        if (draws.size() < 3) return -1;
+        int j = 0;
+        for (size_t v : draws) row[j++] = uint32_t(v);
+        for (int i = 0; i < n; i++) row[3 + i] = uint32_t(next());
+    }
+    return 0;
+}
+
 int orc_interpolate(const orc_surface* s, int ki, const float* in, float* out, int canonical,
                     int threads) {
     set_threads(threads);

@@ -48,6 +48,10 @@ int orc_normals(const orc_surface* s, int kn, int nem, int adaptive, const float
                 const float* flip_targets);
 
 /* interpolateSurfaceNormals: out_i = normalize(in_i + sum_{j in kNN(ki)} in_j). */
+/* The draw sequence of calcPlaneRANSAC for m neighbours (10 x 53 entries:
+ * 3 plane ranks, then min(50, m) scoring ranks); -1 when it fails. */
+int orc_ransac_draws(int64_t m, uint32_t* out);
+
 int orc_interpolate(const orc_surface* s, int ki, const float* normals_in, float* normals_out,
                     int canonical, int threads);
 

@@ -50,6 +50,7 @@ def lib():
     L.orc_normals.argtypes = [_vp, _int, _int, _int, ctypes.c_void_p, _int, _f32p, ctypes.c_void_p, _int,
                               ctypes.c_void_p]
     L.orc_interpolate.argtypes = [_vp, _int, _f32p, _f32p, _int, _int]
+    L.orc_ransac_draws.argtypes = [_i64, _u32p]
     L.orc_distance.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _f32p, _int]
     L.orc_interpolated_normal.argtypes = [_vp, _f32p, _int, _f32p, _i64, _int, _f32p, _int]
     L.orc_reconstruct.restype = _vp
@@ -348,6 +349,17 @@ def vertex_colors(vpos, point_colors, surface):
     idx, _, cnt = surface.knn(V, 1)
     out = c[idx[:, 0].astype(np.int64)].copy()
     out[cnt <= 0] = 0
+    return out
+
+
+def ransac_draws(m):
+    """calcPlaneRANSAC's draw sequence for m neighbours
+    (AdaptiveKSearchSurface.tcc:715-753), replayed with libstdc++: (10, 53)
+    uint32, per iteration 3 plane ranks in set order, then min(50, m)
+    scoring ranks."""
+    out = np.zeros((10, 53), np.uint32)
+    if lib().orc_ransac_draws(int(m), out) != 0:
+        raise ValueError("no three distinct plane draws for m = %d" % m)
     return out
 
 

@@ -297,3 +297,63 @@ def test_ransac_restatement_properties(oracle_mod):
 
     n = oracle_mod.OracleSurface(Q).normals(1, nem=1, adaptive=False)  # k = 2 neighbours
     assert np.isnan(n).all()
+
+
+def _ransac_numpy(P, rows, draws, q, flip):
+    """calcPlaneRANSAC (AdaptiveKSearchSurface.tcc:689-781) in float32 scalar
+    numpy arithmetic, one rounding per operation in the reference's order,
+    over a neighbour row (ascending (d2, index)) and the draw sequence."""
+    f = np.float32
+    m = len(rows)
+    ns = min(50, m)
+    best = (f(0), f(0), f(1))
+    bestdist = f(np.finfo(np.float32).max)
+    nonimproving = 0
+    for t in range(10):
+        if nonimproving >= 5:
+            break
+        a, b, c = (P[int(i)] for i in draws[t, :3])
+        u = (a[0] - b[0], a[1] - b[1], a[2] - b[2])
+        v = (a[0] - c[0], a[1] - c[1], a[2] - c[2])
+        n = [u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]]
+        if not (n[0] == 0 and n[1] == 0 and n[2] == 0):
+            ln = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
+            n = [n[0] / ln, n[1] / ln, n[2] / ln]
+        d1 = (a[0] * n[0] + a[1] * n[1]) + a[2] * n[2]
+        dist = f(0)
+        for j in draws[t, 3:3 + ns]:
+            p = P[int(rows[int(j)])]
+            dist = dist + abs(((p[0] * n[0] + p[1] * n[1]) + p[2] * n[2]) - d1)
+        dist = dist / f(ns)
+        if dist < bestdist:
+            bestdist, best, nonimproving = dist, tuple(n), 0
+        else:
+            nonimproving += 1
+    n = list(best)
+    t = (flip[0] - q[0], flip[1] - q[1], flip[2] - q[2])
+    if (n[0] * t[0] + n[1] * t[1]) + n[2] * t[2] < 0:
+        n = [-n[0], -n[1], -n[2]]
+        if not (n[0] == 0 and n[1] == 0 and n[2] == 0):
+            ln = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
+            n = [n[0] / ln, n[1] / ln, n[2] / ln]
+    return np.array(n, np.float32)
+
+
+@pytest.mark.parametrize("name", ["sphere", "lattice"])
+def test_ransac_oracle_against_numpy_restatement(oracle_mod, name):
+    """The oracle's nem 1 equals a second, numpy restatement bit for bit,
+    given the same neighbour rows, adaptive k and draw sequence."""
+    P = GOLD[name + "/points"]
+    flip = np.float32([0.5, 0.5, 0.5]) if name == "sphere" else np.zeros(3, np.float32)
+    s = oracle_mod.OracleSurface(P, threads=1)
+    ref, k = s.normals(5, nem=1, adaptive=True, flip=flip, with_k=True)
+    sample = np.arange(0, len(P), max(1, len(P) // 150))
+    draws = {}
+    for i in sample:
+        K = int(k[i])
+        m = min(K, len(P))
+        if m not in draws:
+            draws[m] = oracle_mod.ransac_draws(m)
+        rows, _, cnt = s.knn(P[i:i + 1], K)
+        got = _ransac_numpy(P, rows[0, :int(cnt[0])], draws[m], P[i], flip)
+        assert np.array_equal(got.view(np.uint32), ref[i].view(np.uint32)), (i, got, ref[i])
