@@ -357,3 +357,66 @@ def test_ransac_oracle_against_numpy_restatement(oracle_mod, name):
         rows, _, cnt = s.knn(P[i:i + 1], K)
         got = _ransac_numpy(P, rows[0, :int(cnt[0])], draws[m], P[i], flip)
         assert np.array_equal(got.view(np.uint32), ref[i].view(np.uint32)), (i, got, ref[i])
+
+
+def _pmp_add_faces(faces):
+    """pmp SurfaceMesh::add_face over faces 0..F-1
+    (src/liblvr2/geometry/pmp/SurfaceMesh.cpp:283-460), sequentially, for the
+    parts that do not depend on boundary relinking: an edge is created when a
+    face first meets it, corners in order (new_edge(v_i, v_i+1): halfedge 2e
+    points to v_i+1), the face's halfedges link in a cycle, and the face keeps
+    the halfedge from its last corner to its first."""
+    NONE = 0xFFFFFFFF
+    he_of, he_vertex, he_face, he_next, face_he = {}, [], [], [], []
+    for f, tri in enumerate(faces):
+        vs = [int(v) for v in tri]
+        hs = []
+        for i in range(3):
+            a, b = vs[i], vs[(i + 1) % 3]
+            h = he_of.get((a, b))
+            if h is None:
+                h = len(he_vertex)
+                he_of[(a, b)], he_of[(b, a)] = h, h + 1
+                he_vertex += [b, a]
+                he_face += [NONE, NONE]
+                he_next += [NONE, NONE]
+            hs.append(h)
+        for i, h in enumerate(hs):
+            he_face[h] = f
+            he_next[h] = hs[(i + 1) % 3]
+        face_he.append(hs[2])
+    return (np.array(he_vertex, np.int64), np.array(he_face, np.int64), np.array(he_next, np.int64),
+            np.array(face_he, np.int64))
+
+
+@pytest.mark.parametrize("n,holes,seed", [(2, 0.0, 0), (9, 0.3, 1), (40, 0.1, 2)])
+def test_halfedge_restatement_matches_sequential_add_face(oracle_mod, n, holes, seed):
+    rng = np.random.default_rng(seed)
+    ij = np.arange(n * n).reshape(n, n)
+    a, b, c, d = ij[:-1, :-1].ravel(), ij[:-1, 1:].ravel(), ij[1:, :-1].ravel(), ij[1:, 1:].ravel()
+    F = np.concatenate([np.stack([a, b, d], 1), np.stack([a, d, c], 1)])
+    F = F[rng.random(len(F)) >= holes]
+    F = F[rng.permutation(len(F))]
+    r = rng.integers(0, 3, len(F))
+    F = np.stack([F[np.arange(len(F)), (r + j) % 3] for j in range(3)], 1)
+    H = oracle_mod.halfedges(F, n * n)
+    hv, hf, hn, fh = _pmp_add_faces(F)
+    assert H["complex_edges"] == 0 and H["edges"] * 2 == len(hv)
+    assert np.array_equal(H["he_vertex"], hv) and np.array_equal(H["he_face"], hf)
+    assert np.array_equal(H["face_he"], fh)
+    inner = hf != 0xFFFFFFFF
+    assert np.array_equal(H["he_next"][inner], hn[inner])
+    # where a vertex has a single boundary gap, pmp's choices are forced: the
+    # boundary halfedge into it continues with the one leaving it, and the
+    # vertex keeps that outgoing boundary halfedge (adjust_outgoing_halfedge)
+    bnd = np.flatnonzero(~inner)
+    src = hv[bnd ^ 1]
+    starts, counts = np.unique(src, return_counts=True)
+    single = set(starts[counts == 1].tolist())
+    out_of = {int(v): int(h) for v, h in zip(src, bnd) if int(v) in single}
+    for h in bnd:
+        v = int(hv[h])
+        if v in single:
+            assert H["he_next"][h] == out_of[v]
+    for v, h in out_of.items():
+        assert H["vertex_he"][v] == h
