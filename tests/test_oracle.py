@@ -420,3 +420,17 @@ def test_halfedge_restatement_matches_sequential_add_face(oracle_mod, n, holes, 
             assert H["he_next"][h] == out_of[v]
     for v, h in out_of.items():
         assert H["vertex_he"][v] == h
+
+
+def test_ransac_independent_of_tie_order(oracle_mod):
+    """RANSAC draws neighbours by rank, so it depends on the neighbour order;
+    with the reference kd-tree's own order (double d2, ties in traversal
+    order) in place of (float d2, index) its normals stay bit-identical on
+    the golden clouds, the lattice's many exact ties included."""
+    for name in ("sphere", "scan", "lattice"):
+        P = GOLD[name + "/points"]
+        s = oracle_mod.OracleSurface(P)
+        flip = ((P.min(0) + P.max(0)) / 2).astype(np.float32)
+        a = s.normals(10, nem=1, adaptive=True, flip=flip, canonical=True)
+        b = s.normals(10, nem=1, adaptive=True, flip=flip, canonical=False)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
