@@ -1,9 +1,9 @@
 /*
  * lvr_oracle.cpp -- CPU restatement of the lvr2 reconstruction hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU implementation and the
- * timed CPU baseline.  Nothing in the product (lvr2_gb300/, liblvrgb.so)
- * links or calls this file.
+ * TEST INFRASTRUCTURE ONLY: the oracle that the GPU implementation's tests
+ * compare against, and the timed CPU baseline.  Nothing in the product
+ * (lvr2_gb300/, liblvrgb.so) links or calls this file.
  *
  * Parity status: the reference's CPU path cannot be compiled in this
  * environment (it needs Eigen, Boost and FLANN) and the reference ships no

@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/lvr_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker, and by bench.py for the CPU baseline / reference arm.  The
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+check its result, and by bench.py for the CPU baseline / reference arm.  The
 product path (lvr2_gb300) never imports this module.
 """
 import ctypes
