@@ -18,6 +18,7 @@
 #include <array>
 #include <cstdint>
 #include <memory>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -27,6 +28,20 @@ namespace lvr2gb {
 
 inline void check(lvrgb_status s, const char* what) {
     if (s != LVRGB_OK) throw std::runtime_error(std::string(what) + ": " + lvrgb_last_error());
+}
+
+// HashGrid::saveGrid (HashGrid.tcc:380-397): the cell count, then each cell's
+// centre and the distances at its 8 corners, every number written with
+// operator<< and no separator, as lvr2_reconstruct -g writes fastgrid.grid
+// (Main.cpp:604-607).  centers: 3 per cell, tsdf: 8 per cell.
+inline void writeGrid(std::ostream& out, const std::vector<float>& centers, const std::vector<float>& tsdf) {
+    const unsigned long cells = static_cast<unsigned long>(centers.size() / 3);
+    if (tsdf.size() != 8 * size_t(cells)) throw std::runtime_error("writeGrid: need 8 distances per cell");
+    out << cells;
+    for (size_t i = 0; i < cells; i++) {
+        out << centers[3 * i] << centers[3 * i + 1] << centers[3 * i + 2];
+        for (size_t j = 0; j < 8; j++) out << tsdf[8 * i + j];
+    }
 }
 
 struct Vec3 {
@@ -187,6 +202,7 @@ class Surface {
         Mesh m;
         check(lvrgb_reconstruct(h_, &g, &m.info, nullptr), "reconstruct");
         mesh_vertices_ = m.info.vertices;
+        grid_cells_ = m.info.cells_valid;
         if (g.decomposition == 1 && o.optimizePlanarFaces)
             check(lvrgb_optimize_planar_faces(h_, 5, nullptr, nullptr), "optimizePlanarFaces");
         m.vertices.resize(size_t(3 * m.info.vertices));
@@ -206,12 +222,21 @@ class Surface {
         return out;
     }
 
+    // HashGrid::toPointBuffer of the last grid (culled cells in lattice-key
+    // order): centres (3 per cell) and corner distances (8 per cell).
+    void cellTsdf(std::vector<float>& centers, std::vector<float>& tsdf) const {
+        centers.resize(size_t(3 * grid_cells_));
+        tsdf.resize(size_t(8 * grid_cells_));
+        check(lvrgb_get_cell_tsdf(h_, centers.data(), tsdf.data(), 0, nullptr), "cellTsdf");
+    }
+
     lvrgb_surface handle() const { return h_; }
 
   private:
     lvrgb_surface h_ = nullptr;
     size_t n_ = 0;
     int64_t mesh_vertices_ = 0;  // vertices of the last reconstruct()
+    int64_t grid_cells_ = 0;     // cells kept by the last reconstruct()
 };
 
 // CudaKSearchSurface (include/lvr2/reconstruction/CudaKSearchSurface.hpp,

@@ -38,6 +38,7 @@ struct Options {
     float flip[3] = {0, 0, 0};
     bool recalc = false;
     bool export_normals = false;
+    bool save_grid = false;
     std::string pose_file;
     int device = 0;
 };
@@ -47,7 +48,7 @@ void usage() {
         "usage: lvr2gb_reconstruct <inputFile> [--voxelsize|-v F] [--intersections|-i N] [--pcm|-p NAME]\n"
         "       [--nem 0|1|2|3|4] [--decomposition|-d MC|PMC] [--noExtrusion] [--kd N] [--ki N] [--kn N]\n"
         "       [--flipPoint X Y Z] [--recalcNormals|-r] [--exportPointNormals|-e] [--outputFile PATH]\n"
-        "       [--scanPoseFile PATH] [--useGPU] [--threads N] [--device N]");
+        "       [--saveGrid|-g] [--scanPoseFile PATH] [--useGPU] [--threads N] [--device N]");
 }
 
 Options parse(int argc, char** argv) {
@@ -89,6 +90,8 @@ Options parse(int argc, char** argv) {
             o.recalc = true;
         } else if (a == "--exportPointNormals" || a == "-e") {
             o.export_normals = true;
+        } else if (a == "--saveGrid" || a == "-g") {
+            o.save_grid = true;
         } else if (a == "--outputFile") {
             need(i, 1); o.output = argv[++i];
         } else if (a == "--scanPoseFile") {
@@ -326,6 +329,14 @@ int main(int argc, char** argv) {
                     t2 - t1);
         write_mesh_ply(o.output, mesh);
         if (o.export_normals) write_point_normals_ply("pointnormals.ply", xyz, surface.normals());
+        if (o.save_grid) {
+            // HashGrid::saveGrid after the reconstruction (Main.cpp:604-607)
+            std::vector<float> centers, tsdf;
+            surface.cellTsdf(centers, tsdf);
+            std::ofstream grid("fastgrid.grid", std::ios::out | std::ios::binary);
+            lvr2gb::writeGrid(grid, centers, tsdf);
+            if (!grid) throw std::runtime_error("cannot write fastgrid.grid");
+        }
         std::printf("[lvr2gb_reconstruct] wrote %s\n", o.output.c_str());
     } catch (const std::exception& e) {
         std::fprintf(stderr, "[lvr2gb_reconstruct] error: %s\n", e.what());

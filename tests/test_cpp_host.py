@@ -158,3 +158,24 @@ def test_cli_scan_pose_file(built, tmp_path):
         s.calculate_normals()
         n = s.normals()
     assert np.array_equal(rec[:, 3:], n)
+
+
+def test_save_grid_stream_format(built, tmp_path):
+    """--saveGrid writes HashGrid::saveGrid's stream: the cell count, then each
+    cell's centre and 8 corner distances, every number as operator<< prints
+    a float (%g, 6 significant digits) with no separator."""
+    from lvr2_gb300 import build as B
+    exe = tmp_path / "test_write_grid"
+    B.cpp_compile(ROOT / "tests/cpp/test_write_grid.cpp", exe)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    centers = np.float32([0.5, -1.25, 1e-7, 1234567.0, 0.1, -0.0])
+    tsdf = (np.arange(16) - 7).astype(np.float32) * np.float32(0.3)
+    want = "2"
+    for i in range(2):
+        want += "".join("%g" % float(x) for x in centers[3 * i:3 * i + 3])
+        want += "".join("%g" % float(x) for x in tsdf[8 * i:8 * i + 8])
+    assert r.stdout == want
+    cli, _ = built
+    r = subprocess.run([str(cli), "/nonexistent/scan.pts", "-g"], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr  # -g parsed, the file is missing
