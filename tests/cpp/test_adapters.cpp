@@ -86,6 +86,16 @@ int main() {
     }
     EXPECT(radial > size_t(0.95 * double(m.info.vertices)));
 
+    // HashGrid::toPointBuffer of the kept cells (what -g writes): every corner
+    // of a kept cell is valid, so its distance is finite
+    std::vector<float> centers, tsdf;
+    s.cellTsdf(centers, tsdf);
+    EXPECT(m.info.cells_valid > 0 && centers.size() == size_t(3 * m.info.cells_valid) &&
+           tsdf.size() == size_t(8 * m.info.cells_valid));
+    size_t finite = 0;
+    for (float d : tsdf) finite += std::isfinite(d) ? 1 : 0;
+    EXPECT(finite == tsdf.size());
+
     // CudaKSearchSurface (--pcm LBVH_CUDA): unit normals pointing toward (1e6, 1e6, 1e6)
     {
         lvr2gb::CudaKSearchSurface ks(xyz.data(), n, 20);
