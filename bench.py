@@ -338,9 +338,9 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": config(args.points, {"sample_points": len(sample)}),
         "cpu_baseline": {"value": value, "unit": "normals/s", "cores": cores, "kind": "port",
-                         "sample": "spatial crop of the 10M cloud (%d points, same density); full pipeline: "
+                         "sample": "spatial crop of the %d-point cloud (%d points, same density); full pipeline: "
                                    "kd-tree (leaf 20), adaptive-k PCA normals, ki interpolation, grid + "
-                                   "signed distance + culling, PMC marching cubes" % len(sample)},
+                                   "signed distance + culling, PMC marching cubes" % (len(pts), len(sample))},
         "e2e": {"value": value, "unit": "normals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
