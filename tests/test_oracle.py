@@ -434,3 +434,49 @@ def test_ransac_independent_of_tie_order(oracle_mod):
         a = s.normals(10, nem=1, adaptive=True, flip=flip, canonical=True)
         b = s.normals(10, nem=1, adaptive=True, flip=flip, canonical=False)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
+
+
+def _iterative_numpy(P, rows, q, flip):
+    """calcPlaneIterative, nem 2 (AdaptiveKSearchSurface.tcc:522-607), in
+    float32 scalar numpy arithmetic in the reference's order."""
+    f = np.float32
+    xx = xy = xz = yy = yz = zz = f(0)
+    for j in rows:
+        r = P[int(j)] - q
+        xx = xx + r[0] * r[0]
+        xy = xy + r[0] * r[1]
+        xz = xz + r[0] * r[2]
+        yy = yy + r[1] * r[1]
+        yz = yz + r[1] * r[2]
+        zz = zz + r[2] * r[2]
+    det_x, det_y, det_z = yy * zz - yz * yz, xx * zz - xz * xz, xx * yy - xy * xy
+    if det_x >= det_y and det_x >= det_z:
+        d = (f(1), (xz * yz - xy * zz) / det_x, (xy * yz - xz * yy) / det_x)
+    elif det_y >= det_x and det_y >= det_z:
+        d = ((yz * xz - xy * zz) / det_y, f(1), (xy * xz - yz * xx) / det_y)
+    else:
+        d = ((yz * xy - xz * yy) / det_z, (xz * xy - yz * xx) / det_z, f(1))
+    inv = f(1) / np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+    n = [d[0] * inv, d[1] * inv, d[2] * inv]
+    t = (flip[0] - q[0], flip[1] - q[1], flip[2] - q[2])
+    if (n[0] * t[0] + n[1] * t[1]) + n[2] * t[2] < 0:
+        n = [-n[0], -n[1], -n[2]]
+        if not (n[0] == 0 and n[1] == 0 and n[2] == 0):
+            ln = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
+            n = [n[0] / ln, n[1] / ln, n[2] / ln]
+    return np.array(n, np.float32)
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan"])
+def test_iterative_oracle_against_numpy_restatement(oracle_mod, name):
+    """The oracle's nem 2 equals a second, numpy restatement bit for bit,
+    given the same neighbour rows and adaptive k."""
+    P = GOLD[name + "/points"]
+    flip = np.float32([0.5, 0.5, 0.5]) if name == "sphere" else np.zeros(3, np.float32)
+    s = oracle_mod.OracleSurface(P, threads=1)
+    ref, k = s.normals(5, nem=2, adaptive=True, flip=flip, with_k=True)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for i in np.arange(0, len(P), max(1, len(P) // 200)):
+            rows, _, cnt = s.knn(P[i:i + 1], int(k[i]))
+            got = _iterative_numpy(P, rows[0, :int(cnt[0])], P[i], flip)
+            assert np.array_equal(got.view(np.uint32), ref[i].view(np.uint32)), (i, got, ref[i])
