@@ -480,3 +480,38 @@ def test_iterative_oracle_against_numpy_restatement(oracle_mod, name):
             rows, _, cnt = s.knn(P[i:i + 1], int(k[i]))
             got = _iterative_numpy(P, rows[0, :int(cnt[0])], P[i], flip)
             assert np.array_equal(got.view(np.uint32), ref[i].view(np.uint32)), (i, got, ref[i])
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_distance_oracle_against_numpy_restatement(oracle_mod, name):
+    """AdaptiveKSearchSurface::distance (AdaptiveKSearchSurface.tcc:414-457)
+    restated a second time in float32 numpy scalar arithmetic: running sums
+    of the kd nearest points and normals, both divided by kd, the mean normal
+    normalised (a null mean stays null), then the projected and Euclidean
+    distances.  Equals the oracle bit for bit."""
+    P = GOLD[name + "/points"]
+    N = GOLD[name + "/interp"]
+    Q = GOLD[name + "/dist_q"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    proj, eucl = s.distance(N, 4, Q)
+    assert np.array_equal(proj, GOLD[name + "/dist_proj"], equal_nan=True)
+    f = np.float32
+    rows, _, cnt = s.knn(Q, 4)
+    for i in range(0, len(Q), max(1, len(Q) // 200)):
+        c = [f(0), f(0), f(0)]
+        m = [f(0), f(0), f(0)]
+        for j in rows[i, :int(cnt[i])]:
+            for a in range(3):
+                c[a] = c[a] + P[int(j), a]
+                m[a] = m[a] + N[int(j), a]
+        kf = f(int(cnt[i]))
+        c = [x / kf for x in c]
+        m = [x / kf for x in m]
+        if not (m[0] == 0 and m[1] == 0 and m[2] == 0):
+            ln = np.sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2])
+            m = [x / ln for x in m]
+        d = [Q[i, a] - c[a] for a in range(3)]
+        p_ = (d[0] * m[0] + d[1] * m[1]) + d[2] * m[2]
+        e_ = np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+        assert np.float32(p_).view(np.uint32) == proj[i].view(np.uint32), i
+        assert np.float32(e_).view(np.uint32) == eucl[i].view(np.uint32), i
