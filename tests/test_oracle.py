@@ -515,3 +515,25 @@ def test_distance_oracle_against_numpy_restatement(oracle_mod, name):
         e_ = np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
         assert np.float32(p_).view(np.uint32) == proj[i].view(np.uint32), i
         assert np.float32(e_).view(np.uint32) == eucl[i].view(np.uint32), i
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_interpolation_oracle_against_numpy_restatement(oracle_mod, name):
+    """interpolateSurfaceNormals (AdaptiveKSearchSurface.tcc:293-335) restated
+    a second time in float32 numpy scalar arithmetic: the point's own normal
+    plus the normals of its ki nearest (itself among them), normalised (a
+    null sum stays null).  Equals the oracle bit for bit."""
+    P = GOLD[name + "/points"]
+    N = GOLD[name + "/normals_nem3"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    out = s.interpolate(N, 6)
+    assert np.array_equal(out, GOLD[name + "/interp"], equal_nan=True)
+    rows, _, cnt = s.knn(P, 6)
+    for i in range(0, len(P), max(1, len(P) // 300)):
+        m = [N[i, 0], N[i, 1], N[i, 2]]
+        for j in rows[i, :int(cnt[i])]:
+            m = [m[a] + N[int(j), a] for a in range(3)]
+        if not (m[0] == 0 and m[1] == 0 and m[2] == 0):
+            ln = np.sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2])
+            m = [x / ln for x in m]
+        assert np.array_equal(np.float32(m).view(np.uint32), out[i].view(np.uint32)), i
