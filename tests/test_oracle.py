@@ -537,3 +537,30 @@ def test_interpolation_oracle_against_numpy_restatement(oracle_mod, name):
             ln = np.sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2])
             m = [x / ln for x in m]
         assert np.array_equal(np.float32(m).view(np.uint32), out[i].view(np.uint32)), i
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_mc_vertices_against_numpy_restatement(oracle_mod, name):
+    """FastBox::calcIntersection (FastBox.tcc:133-158) restated a second time:
+    every MC vertex lies on the lattice edge its key names, between the grid
+    vertices at lattice l and l + e_axis, at x2 - d2 (x1 - x2) / (d1 - d2)
+    in float32 (low corner first; an exact zero returns that corner).  Equals
+    the oracle's vertex positions bit for bit."""
+    P = GOLD[name + "/points"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    vs = float(GOLD[name + "/voxelsize"])
+    r = s.reconstruct(GOLD[name + "/interp"], voxelsize=vs, kd=4, decomposition="MC")
+    at = {tuple(l): i for i, l in enumerate(r["qp_lattice"].tolist())}
+    pos, dist = r["qp_pos"], r["qp_dist"]
+    assert len(r["vkeys"]) > 50
+    for key, vp in zip(r["vkeys"], r["vpos"]):
+        l, axis = tuple(int(x) for x in key[:3]), int(key[3])
+        h = list(l)
+        h[axis] += 1
+        a, b = at[l], at[tuple(h)]
+        x1, x2, d1, d2 = pos[a, axis], pos[b, axis], dist[a], dist[b]
+        assert (d1 < 0 < d2) or (d2 < 0 < d1) or d1 == 0 or d2 == 0
+        x = x1 if d1 == 0 else x2 if d2 == 0 else x2 - d2 * (x1 - x2) / (d1 - d2)
+        want = pos[a].copy()
+        want[axis] = x
+        assert np.array_equal(want.view(np.uint32), vp.view(np.uint32)), (key, want, vp)
