@@ -564,3 +564,20 @@ def test_mc_vertices_against_numpy_restatement(oracle_mod, name):
         want = pos[a].copy()
         want[axis] = x
         assert np.array_equal(want.view(np.uint32), vp.view(np.uint32)), (key, want, vp)
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_grid_vertex_positions_against_numpy_restatement(oracle_mod, name):
+    """HashGrid::indexToCenter and addBox (HashGrid.hpp:276-281,
+    HashGrid.tcc:246-249) restated: the grid vertex at lattice L is corner 0
+    (offset (-1, -1, -1)) of cell L, at (L + 0.5f) * vs + (-1) * (vs / 2.0f)
+    in float32 per coordinate.  Equals the oracle's positions bit for bit."""
+    P = GOLD[name + "/points"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    r = s.reconstruct(GOLD[name + "/interp"], voxelsize=float(GOLD[name + "/voxelsize"]), kd=4, decomposition="MC")
+    vs = np.float32(r["voxelsize"])
+    L = r["qp_lattice"]
+    centre = (L.astype(np.float32) + np.float32(0.5)) * vs
+    want = centre + np.float32(-1.0) * (vs / np.float32(2.0))
+    assert want.dtype == np.float32 and len(want) > 100
+    assert np.array_equal(want.view(np.uint32), r["qp_pos"].view(np.uint32))
