@@ -581,3 +581,25 @@ def test_grid_vertex_positions_against_numpy_restatement(oracle_mod, name):
     want = centre + np.float32(-1.0) * (vs / np.float32(2.0))
     assert want.dtype == np.float32 and len(want) > 100
     assert np.array_equal(want.view(np.uint32), r["qp_pos"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_culling_against_numpy_restatement(oracle_mod, name):
+    """PointsetGrid::calcDistanceValues (PointsetGrid.tcc:111-185) restated:
+    a grid vertex is invalid when its Euclidean distance exceeds
+    1.75 * voxelsize, compared in double (1.75 is a double literal); its
+    distance is the projected one; a cell with an invalid corner is erased."""
+    P = GOLD[name + "/points"]
+    N = GOLD[name + "/interp"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    r = s.reconstruct(N, voxelsize=float(GOLD[name + "/voxelsize"]), kd=4, decomposition="MC")
+    proj, eucl = s.distance(N, 4, r["qp_pos"])
+    assert np.array_equal(proj.view(np.uint32), r["qp_dist"].view(np.uint32))
+    invalid = eucl.astype(np.float64) > 1.75 * np.float64(np.float32(r["voxelsize"]))
+    assert np.array_equal(invalid, r["qp_invalid"].astype(bool))
+    bad = {tuple(l) for l, x in zip(r["qp_lattice"].tolist(), invalid) if x}
+    offs = [(i, j, k) for i in (0, 1) for j in (0, 1) for k in (0, 1)]
+    keep = {tuple(c) for c in r["cells_all"].tolist()
+            if not any((c[0] + o[0], c[1] + o[1], c[2] + o[2]) in bad for o in offs)}
+    assert keep == {tuple(c) for c in r["cells_valid"].tolist()}
+    assert 0 < len(keep) < len(r["cells_all"]) or name == "lattice"
