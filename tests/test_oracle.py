@@ -603,3 +603,32 @@ def test_culling_against_numpy_restatement(oracle_mod, name):
             if not any((c[0] + o[0], c[1] + o[1], c[2] + o[2]) in bad for o in offs)}
     assert keep == {tuple(c) for c in r["cells_valid"].tolist()}
     assert 0 < len(keep) < len(r["cells_all"]) or name == "lattice"
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+@pytest.mark.parametrize("extrude", [True, False])
+def test_grid_cells_against_numpy_restatement(oracle_mod, name, extrude):
+    """PointsetGrid's cells (PointsetGrid.tcc:41-109) restated: the cell of a
+    point is floor(p / vs) in float32 (HashGrid::calcIndex), kept when its
+    centre (index + 0.5f) * vs lies in the surface's bounding box (min <= c
+    <= max, BoundingBox::contains; the box given to the constructor, not
+    the grown grid box); extrusion adds the 26 neighbours whose centres lie
+    in that box."""
+    P = GOLD[name + "/points"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    r = s.reconstruct(GOLD[name + "/interp"], voxelsize=float(GOLD[name + "/voxelsize"]), kd=4,
+                      decomposition="MC", extrude=extrude)
+    vs = np.float32(r["voxelsize"])
+    lo, hi, _ = s.bbox()
+
+    def inside(idx):
+        c = (idx.astype(np.float32) + np.float32(0.5)) * vs
+        return np.all((lo <= c) & (c <= hi), axis=1)
+
+    idx = np.floor(P / vs).astype(np.int64)
+    cells = np.unique(idx[inside(idx)], axis=0)
+    if extrude:
+        offs = np.array([(i, j, k) for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)], np.int64)
+        cand = np.unique((cells[:, None, :] + offs[None]).reshape(-1, 3), axis=0)
+        cells = cand[inside(cand)]
+    assert {tuple(c) for c in cells.tolist()} == {tuple(c) for c in r["cells_all"].tolist()}
