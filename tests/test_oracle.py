@@ -632,3 +632,34 @@ def test_grid_cells_against_numpy_restatement(oracle_mod, name, extrude):
         cand = np.unique((cells[:, None, :] + offs[None]).reshape(-1, 3), axis=0)
         cells = cand[inside(cand)]
     assert {tuple(c) for c in cells.tolist()} == {tuple(c) for c in r["cells_all"].tolist()}
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "lattice"])
+def test_adaptive_k_against_numpy_restatement(oracle_mod, name):
+    """The adaptive k of calculateSurfaceNormals (AdaptiveKSearchSurface.tcc:
+    187-216, boundingBoxOK :337-350) restated: k doubles before each of at
+    most 5 searches; the search stops once every side of the neighbourhood's
+    box (max - min, float32) is >= 0.05f times each other side."""
+    P = GOLD[name + "/points"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    kn = 5
+    _, kused = s.normals(kn, nem=3, adaptive=True, flip=np.zeros(3, np.float32), with_k=True)
+    assert (kused == GOLD[name + "/kused_nem3"]).all()
+    e = np.float32(0.05)
+    sample = np.arange(0, len(P), max(1, len(P) // 200))
+    want = np.zeros(len(sample), np.int64)
+    todo = np.ones(len(sample), bool)
+    k = kn
+    for rnd in range(5):
+        k *= 2
+        rows, _, cnt = s.knn(P[sample], k)
+        for t in np.flatnonzero(todo):
+            nb = P[rows[t, :int(cnt[t])].astype(np.int64)]
+            d = nb.max(0) - nb.min(0)
+            ok = all(d[a] >= e * d[b] for a in range(3) for b in range(3) if a != b)
+            if ok or rnd == 4:
+                want[t] = k
+                todo[t] = False
+    assert np.array_equal(want, kused[sample])
+    if name != "lattice":
+        assert (want > 2 * kn).any() or name == "sphere"
