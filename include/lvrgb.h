@@ -205,7 +205,9 @@ lvrgb_status lvrgb_grid_distances(lvrgb_surface s, const float* q, int64_t nq, f
                                   uint8_t* invalid, int32_t on_device, void* stream);
 
 /* PointsetSurface::getInterpolatedNormal (PointsetSurface.tcc:61-74) for nq
- * positions (n x 3 out). */
+ * positions (n x 3 out): ((0, 1, 0) + the sum of the ki nearest points'
+ * normals, each normalised) / ki.  Like lvr2 (whose final
+ * Normal<float>(result) is a copy, :72-73) the mean is not normalised. */
 lvrgb_status lvrgb_interpolated_normal(lvrgb_surface s, const float* q, int64_t nq, float* out,
                                        int32_t on_device, void* stream);
 

@@ -159,7 +159,8 @@ class Surface {
             qp[i].m_invalid = inv[i] != 0;
         }
     }
-    // PointsetSurface::getInterpolatedNormal
+    // PointsetSurface::getInterpolatedNormal: the mean of (0, 1, 0) and the ki
+    // nearest normals, not normalised (as lvr2 returns it)
     Vec3 getInterpolatedNormal(const Vec3& v) const {
         float q[3] = {v.x, v.y, v.z}, o[3];
         check(lvrgb_interpolated_normal(h_, q, 1, o, 0, nullptr), "getInterpolatedNormal");

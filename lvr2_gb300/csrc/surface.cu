@@ -889,7 +889,9 @@ __device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, floa
         if (A.normals) {
             // PointsetSurface::getInterpolatedNormal: accumulator starts as the
             // default Normal (0, 1, 0); neighbour normals are normalised when
-            // read; the sum is divided by ki and normalised.
+            // read; the sum is divided by ki.  The reference returns
+            // Normal<float>(result) with result already a Normal, which is the
+            // copy constructor: the mean is not normalised (PointsetSurface.tcc:72-73).
             float x = 0.0f, y = 1.0f, z = 0.0f;
             for (int s = 0; s < A.K; s++) {
                 unsigned long long key = heap.at(s);
@@ -905,7 +907,6 @@ __device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, floa
             x = __fdiv_rn(x, kf);
             y = __fdiv_rn(y, kf);
             z = __fdiv_rn(z, kf);
-            normalize_ieee(x, y, z);
             A.nout[row * 3 + 0] = x;
             A.nout[row * 3 + 1] = y;
             A.nout[row * 3 + 2] = z;

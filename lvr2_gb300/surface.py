@@ -287,6 +287,9 @@ class Surface:
         return dist, inv
 
     def interpolated_normal(self, queries):
+        """PointsetSurface::getInterpolatedNormal at each query: ((0, 1, 0) +
+        the ki nearest normals, each normalised) / ki, not normalised (as
+        lvr2 returns it)."""
         q, on_dev = _f32x3(queries)
         if on_dev:
             raise ValueError("use host arrays with interpolated_normal()")

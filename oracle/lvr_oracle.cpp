@@ -730,8 +730,9 @@ int orc_interpolated_normal(const orc_surface* s, const float* normals, int ki, 
             uint32_t t = id[j];
             r += V3(normals[3 * t], normals[3 * t + 1], normals[3 * t + 2]).normalized();
         }
+        // `return Normal<float>(result)` copy-constructs from a Normal: the
+        // mean is returned as it is, not normalised (PointsetSurface.tcc:72-73)
         r /= float(ki);
-        r.normalize();
         out[3 * i] = r.x;
         out[3 * i + 1] = r.y;
         out[3 * i + 2] = r.z;

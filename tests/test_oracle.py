@@ -663,3 +663,28 @@ def test_adaptive_k_against_numpy_restatement(oracle_mod, name):
     assert np.array_equal(want, kused[sample])
     if name != "lattice":
         assert (want > 2 * kn).any() or name == "sphere"
+
+
+def test_interpolated_normal_against_numpy_restatement(oracle_mod):
+    """PointsetSurface::getInterpolatedNormal (PointsetSurface.tcc:61-74)
+    restated: the default Normal (0, 1, 0) plus the ki nearest points'
+    normals, each normalised as it is read, divided by ki; the result is
+    returned through the Normal copy constructor, so it is not normalised."""
+    P = GOLD["scan/points"]
+    N = GOLD["scan/interp"]
+    Q = GOLD["scan/dist_q"]
+    s = oracle_mod.OracleSurface(P, threads=1)
+    out = s.interpolated_normal(N, 6, Q)
+    rows, _, cnt = s.knn(Q, 6)
+    f = np.float32
+    for i in range(0, len(Q), max(1, len(Q) // 300)):
+        r = [f(0), f(1), f(0)]
+        for j in rows[i, :int(cnt[i])]:
+            n = [N[int(j), a] for a in range(3)]
+            if not (n[0] == 0 and n[1] == 0 and n[2] == 0):
+                ln = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
+                n = [x / ln for x in n]
+            r = [r[a] + n[a] for a in range(3)]
+        r = [x / f(6) for x in r]
+        assert np.array_equal(np.float32(r).view(np.uint32), out[i].view(np.uint32)), i
+    assert (np.abs(np.linalg.norm(out, axis=1) - 1) > 1e-3).mean() > 0.5  # means, not unit vectors
