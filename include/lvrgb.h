@@ -425,14 +425,17 @@ lvrgb_status lvrgb_debug_fail_allocation(int64_t n);
  *  - Limits: 1 <= n <= 65536, 0 <= nq <= 65536, 1 <= k <= 96; larger inputs
  *    are rejected with LVRGB_ERR_INVALID_ARGUMENT.  Use lvrgb_surface_create
  *    and lvrgb_knn for anything bigger.
+ *  - A point with a NaN or infinite coordinate is rejected with
+ *    LVRGB_ERR_INVALID_ARGUMENT naming the first such point (as
+ *    lvrgb_surface_create does); a query with one gets padding rows.
  *  - Scratch is one 8 MiB static device array that every GPU loading this
  *    library holds until the process exits.  The first call on a device looks
- *    up its address (cudaGetSymbolAddress); make that first call before any
- *    stream capture.
+ *    up its address (cudaGetSymbolAddress).
  *  - All calls share the array: calls that overlap on the GPU (other streams,
  *    other host threads) race and must be serialized by the caller.
- *  - Synchronizes `stream` (one small read of the point bounding box and of
- *    the error flag). */
+ *  - Every call synchronizes `stream` (small reads of the point bounding box,
+ *    the non-finite marker and the error flag into host memory), so it must
+ *    not be called while `stream` is being captured into a CUDA graph. */
 lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float* queries, int64_t nq, int32_t k,
                                      uint32_t* idx, float* dist, void* stream);
 

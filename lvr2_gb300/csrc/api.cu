@@ -1521,14 +1521,29 @@ lvrgb_status lvrgb_knn_small_noalloc(const float* points, int64_t n, const float
         B.box = C.take<float>(8);
         B.err = C.take<int>(4);
         float4* qs = C.take<float4>(size_t(nq > 0 ? nq : 1));
-        // The array keeps the previous call's contents: clear what must start at zero.
+        int* first_bad = C.take<int>(1);
+        // The array keeps the previous call's contents: clear what must start
+        // at zero (the error word) and reset the non-finite marker to "none"
+        // (bytes 0x7f: 0x7f7f7f7f is above every point index allowed here).
         LVRGB_CUDA(cudaMemsetAsync(B.err, 0, 4 * sizeof(int), st));
+        LVRGB_CUDA(cudaMemsetAsync(first_bad, 0x7f, sizeof(int), st));
+        // A NaN or infinite coordinate breaks the tree's ordering, as in
+        // lvrgb_surface_create: find the first such point.  The build below only
+        // does arithmetic on the coordinates, so it runs before the check is read.
+        first_nonfinite_kernel<<<ceil_div(np, 256), 256, 0, st>>>(points, np, first_bad);
+        LVRGB_LAUNCH_CHECK();
         Lbvh T;
         lbvh_build_into(points, np, kNoAllocBucket, B, T, st);
-        // Morton frame of the tree for the search seeds: one 24-byte read of the box.
+        // Morton frame of the tree for the search seeds (one 24-byte read of
+        // the box), read in the same synchronization as the non-finite marker.
         float h[6];
+        int bad = 0;
         LVRGB_CUDA(cudaMemcpyAsync(h, B.box, sizeof(h), cudaMemcpyDeviceToHost, st));
+        LVRGB_CUDA(cudaMemcpyAsync(&bad, first_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
         LVRGB_CUDA(cudaStreamSynchronize(st));
+        if (bad != 0x7f7f7f7f)
+            throw ApiError{LVRGB_ERR_INVALID_ARGUMENT,
+                           "lvrgb_knn_small_noalloc: point " + std::to_string(bad) + " has a non-finite coordinate"};
         const float ext = std::max(std::max(h[3] - h[0], h[4] - h[1]), h[5] - h[2]);
         for (int a = 0; a < 3; a++) T.mn[a] = h[a];
         T.scale = morton_scale(ext);
