@@ -38,9 +38,8 @@ VOXELSIZE = 0.005
 NEM = 3
 CPU_SAMPLE_FRACTION = 0.02
 # DRAM bytes (read + write) per unit of the two kNN kernels, from one ncu
-# capture of the 2M-point case (profiles/normals_kernel_spheres_tori_2M.md,
-# profiles/sdf_kernel_spheres_tori_2M.md); the normal kernel's traffic is
-# per-point I/O (the neighbour gathers hit L2), so it scales with the points.
+# capture of the 2M-point spheres-and-tori case; the normal kernel's traffic
+# is per-point I/O (the neighbour gathers hit L2), so it scales with the points.
 NCU_DRAM_BYTES_PER_NORMAL = (47.202816e6 + 153.4976e6) / 2e6
 NCU_DRAM_BYTES_PER_SDF_VERTEX = (151.558656e6 + 28.21376e6) / 4415248
 

@@ -7,7 +7,7 @@ header once and writes the table in this project's own packed encoding:
 one uint64 per cube index, bits [4*j, 4*j+4) = j-th edge index of the
 triangle list (up to 12 edges), bits [60, 64) = number of triangles.
 
-Usage: python oracle/gen_mc_table.py /root/reference
+Usage: python oracle/gen_mc_table.py <lvr2 source tree>
 The generated file is committed; tests/test_tables.py re-checks it against
 the reference header (compiled by oracle/Makefile into oracle/_ref/).
 """
@@ -56,4 +56,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python oracle/gen_mc_table.py <lvr2 source tree>")
+    main(sys.argv[1])

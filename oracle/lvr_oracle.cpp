@@ -717,7 +717,8 @@ int orc_distance(const orc_surface* s, const float* normals, int kd, const float
 
 // PointsetSurface::getInterpolatedNormal (PointsetSurface.tcc:61-74): the
 // accumulator is a default Normal (0, 1, 0); every neighbour normal is
-// normalised when read; the sum is divided by ki and normalised.
+// normalised when read; the sum is divided by ki.  The return copy-constructs
+// the Normal it already is, so the mean comes back un-normalised.
 int orc_interpolated_normal(const orc_surface* s, const float* normals, int ki, const float* q,
                             int64_t nq, int canonical, float* out, int threads) {
     set_threads(threads);
