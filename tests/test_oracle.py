@@ -19,6 +19,41 @@ def brute_knn(P, Q, k):
     return order.astype(np.uint32), np.sqrt(np.take_along_axis(d2, order, 1))
 
 
+REF_LBVH = np.load(ROOT / "tests/golden/ref_lbvh.npz")
+
+
+@pytest.mark.parametrize("name", ["sphere", "scan", "spheres_tori"])
+def test_oracle_against_lvr2_lbvh_outputs(oracle_mod, name):
+    """The oracle pinned to outputs of lvr2's own code: what LBVHIndex::kSearch
+    and LBVHIndex::knn_normals (src/liblvr2/reconstruction/cuda/LBVHIndex.cu,
+    run unmodified on a GB300 by tests/golden/make_ref_lbvh.py) returned.
+    - kNN: the same neighbour set for every query; lvr2's squared distances
+      (NVRTC contracts them into FMAs) within 2 ulp of the float32 ones, the
+      oracle's Euclidean distances within 2 ulp of their square roots.
+    - nem 4 (the comparator's FP64 plane fit): bit-equal normals."""
+    g = REF_LBVH
+    K = int(g["K"])
+    P, Q = g[name + "_points"], g[name + "_queries"]
+    ridx, rd2 = g[name + "_idx"], g[name + "_dist"]
+    o = oracle_mod.OracleSurface(P)
+    oi, od, oc = o.knn(Q, K)
+    assert (oc == K).all() and (g[name + "_cnt"] == K).all()
+    assert all(set(a) == set(b) for a, b in zip(oi.tolist(), ridx.tolist()))
+    d = P[ridx.astype(np.int64)] - Q[:, None, :]
+    d2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+
+    def ulps(a, b):
+        a = np.asarray(a, np.float32)
+        b = np.asarray(b, np.float32)
+        return np.abs(a.astype(np.float64) - b) / np.spacing(np.maximum(np.abs(a), np.abs(b)))
+
+    assert ulps(d2, rd2).max() <= 2
+    ref_d = np.sqrt(np.sort(rd2, 1).astype(np.float64)).astype(np.float32)
+    assert ulps(np.sort(od, 1), ref_d).max() <= 2
+    n4 = oracle_mod.lbvh_knn_normals(o, K, flip=(1e6, 1e6, 1e6))
+    assert np.array_equal(n4, g[name + "_normals"])
+
+
 @pytest.mark.parametrize("kind", ["uniform", "lattice", "duplicates"])
 def test_canonical_knn_is_exact(oracle_mod, kind):
     rng = np.random.Generator(np.random.PCG64(5))
