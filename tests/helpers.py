@@ -44,3 +44,27 @@ def canonical_mesh(vkeys, vpos, faces):
     f = np.stack([f[rows, m], f[rows, (m + 1) % 3], f[rows, (m + 2) % 3]], axis=1)
     fo = np.lexsort((f[:, 2], f[:, 1], f[:, 0]))
     return vkeys[order], np.asarray(vpos)[order], f[fo]
+
+
+def fp64_pca_normals_rows(points, queries_idx, nbr, flip, chunk=200_000):
+    """Vectorised fp64_pca_normals for rows of one width: nbr is an (m, k)
+    array of neighbour indices (all real).  Returns (normals, relative
+    eigengap (l2 - l1) / l3 of each covariance, eigenvalues ascending)."""
+    P = np.asarray(points, np.float32)
+    flip = np.asarray(flip, np.float64)
+    m = len(queries_idx)
+    out = np.empty((m, 3))
+    gap = np.empty(m)
+    for a in range(0, m, chunk):
+        qi = np.asarray(queries_idx[a:a + chunk], np.int64)
+        nb = np.asarray(nbr[a:a + chunk], np.int64)
+        S = np.concatenate([P[qi][:, None, :], P[nb]], axis=1).astype(np.float64)
+        S -= S.mean(axis=1, keepdims=True)
+        C = np.einsum("mki,mkj->mij", S, S) / S.shape[1]
+        w, V = np.linalg.eigh(C)
+        n = V[:, :, 0]
+        flipdir = flip[None, :] - P[qi].astype(np.float64)
+        n = np.where((np.sum(n * flipdir, axis=1) < 0)[:, None], -n, n)
+        out[a:a + chunk] = n
+        gap[a:a + chunk] = (w[:, 1] - w[:, 0]) / np.maximum(w[:, 2], 1e-300)
+    return out, gap
