@@ -36,6 +36,7 @@ METRIC = "normals/s, SDF evals/s @10M pts; plain vs batched/adjoint form, ≤0.5
 KN = KI = KD = 20
 VOXELSIZE = 0.005
 NEM = 3
+PLANAR_KC = 5  # FastReconstruction::getMesh runs optimizePlanarFaces(mesh, 5) for PMC
 CPU_SAMPLE_FRACTION = 0.02
 # DRAM bytes (read + write) per unit of the two kNN kernels, from one ncu
 # capture of the 2M-point spheres-and-tori case; the normal kernel's traffic
@@ -61,6 +62,9 @@ def parse():
     ap.add_argument("--adjoint-scale", type=float, default=1.0, help="scale of the 30M-point terrain")
     ap.add_argument("--no-precision", action="store_true", help="skip the folded-sheets precision measurement")
     ap.add_argument("--precision-scale", type=float, default=1.0, help="scale of the 20M-point folded sheets")
+    ap.add_argument("--no-scan-scene", action="store_true", help="skip the 289,252-point scan-scene record")
+    ap.add_argument("--no-full-form", action="store_true", help="skip the full-form (graph + Newton) record")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip lvr2's own LBVH on this GPU")
     return ap.parse_args()
 
 
@@ -80,7 +84,7 @@ def workload(n):
 def config(n, extra=None):
     c = {"workload": "spheres_tori_%dM" % (n // 1_000_000) if n >= 1_000_000 else "spheres_tori_%d" % n,
          "points": n, "kn": KN, "ki": KI, "kd": KD, "nem": NEM, "adaptive_k": True, "voxelsize": VOXELSIZE,
-         "decomposition": "PMC", "flip_point": "bbox centroid",
+         "decomposition": "PMC", "planar_post_pass_kc": PLANAR_KC, "flip_point": "bbox centroid",
          "l2": "inputs and per-step working set (>1 GB) larger than L2"}
     if extra:
         c.update(extra)
@@ -297,6 +301,220 @@ def precision_measurement(args, steps):
                                   "max": float(ang.max()), "sample": len(idx)}}
 
 
+README_SCAN_MS = {"normals_with_interpolation": 161, "grid_signed_distance_culling": 125, "pmc_with_planar_pass": 47}
+
+
+def scan_scene_measurement(args, steps):
+    """The plain CPU-runnable reconstruction at its full size, both arms on
+    the same points: 289,252 points of the seeded scan-shaped scene, kn = ki
+    = 10, kd = 5, voxel size 10, PMC with optimizePlanarFaces(5), flip point
+    (0, 0, 0), nem 0 (lvr2_reconstruct's default plane fit).  GPU stages
+    (device events) beside the oracle's reference-faithful CPU run on all host
+    cores and beside the stage times of lvr2's README run (16 threads, its
+    scan.pts, which is not in the lvr2 tree)."""
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import synthetic
+    from oracle import oracle as O
+    P, _ = synthetic.scan_scene()
+    n = len(P)
+    d = torch.from_numpy(P).cuda()
+    flip = np.zeros(3, np.float32)
+    with lvr2_gb300.Surface(d, kn=10, ki=10, kd=5, nem=0, flip_point=flip) as s:
+        def step():
+            s.set_points(d)
+            s.calculate_normals()
+            info = s.reconstruct(voxelsize=10.0, decomposition="PMC")
+            return info, s.optimize_planar_faces(PLANAR_KC)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        stage = np.zeros(8)
+        ev[0].record()
+        for _ in range(max(steps, 1)):
+            info, moved = step()
+            stage += s.timings()
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / max(steps, 1)
+        stage /= max(steps, 1)
+    O.build()
+    best = None
+    for _ in range(2):
+        t = {}
+        t0 = time.perf_counter()
+        o = O.OracleSurface(P, leaf_size=20)
+        t["tree"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        nr = o.normals(10, nem=0, adaptive=True, flip=flip, canonical=False)
+        t["normals"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        nr = o.interpolate(nr, 10, canonical=False)
+        t["interpolation"] = time.perf_counter() - t0
+        r = o.reconstruct(nr, voxelsize=10.0, kd=5, decomposition="PMC", canonical=False, planar_kc=PLANAR_KC)
+        t["grid_signed_distance_culling_mc"] = r["seconds_reconstruct"]
+        t["planar_pass"] = r["seconds_planar"]
+        if best is None or sum(t.values()) < sum(best.values()):
+            best = t
+        del o
+    cpu_ms = 1000 * sum(best.values())
+    gs = {"lbvh_build": stage[0], "normals": stage[1], "interpolation": stage[2], "grid_build": stage[3],
+          "signed_distance": stage[4], "culling": stage[5], "marching_cubes": stage[6], "planar_pass": stage[7]}
+    return {"workload": "scan_scene_289k", "points": n, "same_config": True, "kn": 10, "ki": 10, "kd": 5,
+            "voxelsize": 10.0, "nem": 0, "decomposition": "PMC", "planar_post_pass_kc": PLANAR_KC,
+            "flip_point": [0.0, 0.0, 0.0],
+            "gpu_ms_per_step": ms, "gpu_normals_per_s": n / (ms / 1000.0),
+            "gpu_stages_ms": {k: float(v) for k, v in gs.items()},
+            "cpu_ms_per_step": cpu_ms, "cpu_normals_per_s": n / (cpu_ms / 1000.0), "cpu_cores": os.cpu_count(),
+            "cpu_kind": "port", "cpu_stages_ms": {k: 1000 * v for k, v in best.items()},
+            "gpu_over_cpu": cpu_ms / ms,
+            "readme_stages_ms": dict(README_SCAN_MS, note="lvr2 README.md:113-124, 16 threads, CPU unstated, "
+                                                          "its own scan.pts (289,252 points), not this scene"),
+            "counts": {"cells_valid": int(info.cells_valid), "vertices": int(info.vertices),
+                       "faces": int(info.faces), "planar_moved": int(moved),
+                       "readme_counts": {"cells": 30040, "vertices": 20157, "faces": 36416}}}
+
+
+def full_form_measurement(d_pts, flip, plain_ms, steps):
+    """The spec form on the same 10M-point cloud as the plain step: the
+    normals through the scan-project path (one segmented LBVH, CUDA graph
+    replay, FP32 PCA with the FP64 eigen fallback), then grid, signed
+    distance, culling, PMC and its planar pass, then three Newton steps of
+    every mesh vertex onto the zero level with analytic normals.  Device
+    buffers throughout; timed with CUDA events."""
+    import ctypes
+
+    import torch
+
+    import lvr2_gb300
+    from lvr2_gb300 import _lib
+    L = _lib.load()
+    n = int(d_pts.shape[0])
+    nrm = torch.empty((n, 3), dtype=torch.float32, device=d_pts.device)
+    with lvr2_gb300.Batch([d_pts], [flip], kn=KN, ki=KI, nem=NEM) as b, \
+            lvr2_gb300.Surface(d_pts, kn=KN, ki=KI, kd=KD, nem=NEM, flip_point=flip) as s:
+        def step():
+            b.calculate_normals(use_graph=True)
+            _lib.check(L.lvrgb_batch_get_normals(b._h, ctypes.c_void_p(nrm.data_ptr()), 1, None))
+            s.set_normals(nrm)
+            info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+            s.optimize_planar_faces(PLANAR_KC)
+            v = torch.empty((int(info.vertices), 3), dtype=torch.float32, device=d_pts.device)
+            f = torch.empty((int(info.faces), 3), dtype=torch.int32, device=d_pts.device)
+            _lib.check(L.lvrgb_get_mesh(s._h, ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(f.data_ptr()), None,
+                                        1, None))
+            pos, vn = s.project_to_surface(v, steps=3)
+            return info
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(max(steps, 1)):
+            info = step()
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / max(steps, 1)
+        counters, _ = b.stats()
+    return {"workload": "spheres_tori_10M", "points": n, "ms_per_step": ms, "normals_per_s": n / (ms / 1000.0),
+            "plain_ms_per_step": plain_ms, "full_over_plain_time": ms / plain_ms,
+            "mesh_vertices_projected": int(info.vertices), "newton_steps": 3,
+            "fp64_eigensolves": int(counters[5]), "graph": True,
+            "note": "does the plain step's work plus the Newton projection, with the same kernels; the speed-up "
+                    "against a plain GPU implementation is reference_gpu (lvr2's own LBVH on this GPU)"}
+
+
+def ours_lbvh_calls(P, k=20, reps=3):
+    """This library on the calls lvr2's LBVH comparator makes: tree build,
+    kNN of every point (lvrgb_knn) and the comparator's normals (nem 4, one
+    search with k = kn, flip point (1e6, 1e6, 1e6)).  Wall-clock per call
+    with host arrays in and out (as LBVHIndex::kSearch / knn_normals take
+    them), and device time with the points resident."""
+    import torch
+
+    import lvr2_gb300
+    n = len(P)
+    d = torch.from_numpy(P).cuda()
+    out = {}
+    with lvr2_gb300.Surface(d, kn=k, ki=0, kd=5, nem=4, adaptive=False, flip_point=(1e6, 1e6, 1e6)) as s:
+        for _ in range(2):
+            s.set_points(d)
+            s.knn(d, k)
+            s.calculate_normals()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        torch.cuda.synchronize()
+        ev[0].record()
+        for _ in range(reps):
+            s.set_points(d)
+        ev[1].record()
+        for _ in range(reps):
+            s.knn(d, k)
+        ev[2].record()
+        for _ in range(reps):
+            s.calculate_normals()
+        ev[3].record()
+        torch.cuda.synchronize()
+        out["device_build_ms"] = ev[0].elapsed_time(ev[1]) / reps
+        out["device_knn_ms"] = ev[1].elapsed_time(ev[2]) / reps
+        out["device_normals_ms"] = ev[2].elapsed_time(ev[3]) / reps
+        # host arrays in and out, as the comparator's calls take them
+        t0 = time.perf_counter()
+        s.set_points(P)
+        out["host_build_ms"] = 1000 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        s.knn(P, k)
+        out["host_knn_ms"] = 1000 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        s.calculate_normals()
+        s.normals()
+        out["host_normals_ms"] = 1000 * (time.perf_counter() - t0)
+    return out
+
+
+def reference_gpu_measurement(sizes=(2_000_000, 10_000_000)):
+    """lvr2's own CUDA LBVH (LBVHIndex::build, kSearch, knn_normals; K = 20;
+    leaf size 1), unmodified, built from the lvr2 sources by oracle/Makefile
+    when they are present: wall-clock times per call, NVRTC compilation
+    included; beside it this library on the same calls (ours_lbvh_calls)."""
+    exe = ROOT / "oracle" / "_ref" / "ref_lbvh"
+    if not exe.exists():
+        return {"unavailable": "oracle/_ref/ref_lbvh not built (needs the lvr2 LBVH sources copied by "
+                               "`make -C oracle ref-lbvh-src`)"}
+    import tempfile
+
+    from lvr2_gb300 import synthetic
+    out = {"kind": "lvr2 LBVHIndex (src/liblvr2/reconstruction/cuda/LBVHIndex.cu), sm_103a, NVRTC kernels",
+           "K": 20, "runs": []}
+    for n in sizes:
+        P = synthetic.spheres_tori(int(n), seed=2)
+        ours = ours_lbvh_calls(P)
+        with tempfile.TemporaryDirectory() as tmp:
+            pf = Path(tmp) / "pts.bin"
+            with open(pf, "wb") as f:
+                f.write(np.int64(len(P)).tobytes())
+                f.write(np.ascontiguousarray(P, np.float32).tobytes())
+            try:
+                r = subprocess.run([str(exe), "run", str(pf), "-", "20"], capture_output=True, text=True,
+                                   timeout=600)
+            except subprocess.TimeoutExpired:
+                out["runs"].append({"points": int(n), "unavailable": "timed out", "ours": ours})
+                continue
+        if r.returncode != 0:
+            out["runs"].append({"points": int(n), "unavailable": "exit %d" % r.returncode, "ours": ours})
+            continue
+        ref = json.loads(r.stdout.strip().splitlines()[-1])
+        ref["ours"] = ours
+        ref["knn_speedup_host_calls"] = ref["ksearch_ms"] / ours["host_knn_ms"]
+        ref["normals_speedup_host_calls"] = (ref["normals_build_ms"] + ref["knn_normals_ms"]) / (
+            ours["host_build_ms"] + ours["host_normals_ms"])
+        out["runs"].append(ref)
+    return out
+
+
 def cpu_reference_step(points, threads=0, canonical=False):
     """One pass of the reference algorithm on the host (oracle/)."""
     from oracle import oracle as O
@@ -305,7 +523,8 @@ def cpu_reference_step(points, threads=0, canonical=False):
     lo, hi, c = s.bbox()
     n = s.normals(KN, nem=NEM, adaptive=True, flip=c, canonical=canonical)
     n = s.interpolate(n, KI, canonical=canonical)
-    r = s.reconstruct(n, voxelsize=VOXELSIZE, kd=KD, decomposition="PMC", canonical=canonical)
+    r = s.reconstruct(n, voxelsize=VOXELSIZE, kd=KD, decomposition="PMC", canonical=canonical,
+                      planar_kc=PLANAR_KC)
     dt = time.perf_counter() - t0
     return dt, r
 
@@ -339,7 +558,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "normals/s", "cores": cores, "kind": "port",
                          "sample": "spatial crop of the %d-point cloud (%d points, same density); full pipeline: "
                                    "kd-tree (leaf 20), adaptive-k PCA normals, ki interpolation, grid + "
-                                   "signed distance + culling, PMC marching cubes" % (len(pts), len(sample))},
+                                   "signed distance + culling, PMC marching cubes + optimizePlanarFaces(5)"
+                                   % (len(pts), len(sample))},
         "e2e": {"value": value, "unit": "normals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -370,7 +590,9 @@ def run_gpu(args):
     def step():
         s.set_points(d_pts)
         s.calculate_normals()
-        return s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+        info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+        s.optimize_planar_faces(PLANAR_KC)
+        return info
 
     for _ in range(args.warmup):
         step()
@@ -378,7 +600,7 @@ def run_gpu(args):
     if dist:
         dist.barrier()
     l0 = kernel_launches()
-    stage = np.zeros(7)
+    stage = np.zeros(8)
     stats_acc = np.zeros(16)
     infos = []
     with ClockSampler(local) as clocks:
@@ -414,6 +636,7 @@ def run_gpu(args):
         s.set_points(pts_h)
         s.calculate_normals()
         info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+        s.optimize_planar_faces(PLANAR_KC)
         cap_v, cap_f = 2 * int(info.vertices) + 1024, 2 * int(info.faces) + 1024
         h_v = torch.empty((cap_v, 3), dtype=torch.float32).pin_memory().numpy()
         h_f = torch.empty((cap_f, 3), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
@@ -421,6 +644,7 @@ def run_gpu(args):
             s.set_points(pts_h)
             s.calculate_normals()
             s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+            s.optimize_planar_faces(PLANAR_KC)
             s.normals(out=h_norm)
             s.mesh(with_edges=False, out_vertices=h_v, out_faces=h_f)
         torch.cuda.synchronize()
@@ -430,6 +654,7 @@ def run_gpu(args):
             s.set_points(pts_h)
             s.calculate_normals()
             info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
+            s.optimize_planar_faces(PLANAR_KC)
             out_n = s.normals(out=h_norm)
             v, f, _ = s.mesh(with_edges=False, out_vertices=h_v, out_faces=h_f)
             d2h = out_n.nbytes + v.nbytes + f.nbytes
@@ -462,10 +687,11 @@ def run_gpu(args):
                              "seed_radius": args.seed_radius}),
         "stages_ms": {"lbvh_build": float(stage[0]), "normals": normals_ms, "interpolation": float(stage[2]),
                       "grid_build": float(stage[3]), "signed_distance": sdf_ms, "culling": float(stage[5]),
-                      "marching_cubes": float(stage[6])},
+                      "marching_cubes": float(stage[6]), "planar_post_pass": float(stage[7])},
         "rates": {"normals_per_s_stage": n / ((stage[0] + stage[1] + stage[2]) / 1000.0),
                   "sdf_evals_per_s_stage": nq / (sdf_ms / 1000.0),
-                  "mc_cells_per_s_stage": ncv / (stage[6] / 1000.0) if stage[6] > 0 else None},
+                  "mc_cells_per_s_stage": ncv / (stage[6] / 1000.0) if stage[6] > 0 else None,
+                  "pmc_cells_per_s_stage": ncv / ((stage[6] + stage[7]) / 1000.0) if stage[6] > 0 else None},
         "counts": {"grid_vertices": int(nq), "cells_valid": int(ncv), "faces": int(nf), "vertices": int(nv),
                    "fitted_per_round": [int(x) for x in stats[:5]], "fp64_eigensolves": int(stats[5]),
                    "normals_buckets_per_warp": float(stats[8]) / max(1.0, n / 32.0),
@@ -493,12 +719,19 @@ def run_gpu(args):
         "clocks": clocks.summary(),
         "e2e": e2e,
     }
+    if not args.no_full_form:
+        _, _, centroid = s.bounding_box()
+        line["full_form"] = full_form_measurement(d_pts, centroid, ms, args.steps)
+    if not args.no_scan_scene:
+        line["scan_scene"] = scan_scene_measurement(args, args.steps)
     if not args.no_batched:
         line["batched"] = batched_measurement(args, args.steps)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(args, args.steps)
     if not args.no_precision:
         line["precision"] = precision_measurement(args, args.steps)
+    if not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_measurement()
     if not args.no_cpu_baseline:
         sample = cpu_sample(pts)
         dt, _ = cpu_reference_step(sample)

@@ -398,9 +398,10 @@ lvrgb_status lvrgb_surface_set_points(lvrgb_surface s, const float* xyz, int64_t
 
 /* Device time in ms of the handle's last calls: out[0] search-structure
  * build, [1] normal estimation, [2] interpolation, [3] grid build, [4]
- * signed distance, [5] culling, [6] marching cubes; [7] unused.  These are the
- * stage boundaries of lvr2_reconstruct's log lines (README.md:118-124).  No
- * lvr2 counterpart beyond those log lines. */
+ * signed distance, [5] culling, [6] marching cubes, [7] the PMC planar
+ * post-pass (lvrgb_optimize_planar_faces on the last mesh; 0 if none).  These
+ * are the stage boundaries of lvr2_reconstruct's log lines
+ * (README.md:118-124).  No lvr2 counterpart beyond those log lines. */
 lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]);
 
 /* Number of kernels this library has launched in the process (diagnostics;

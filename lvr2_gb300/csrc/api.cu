@@ -42,9 +42,10 @@ struct lvrgb_surface_s {
     bool has_raw = false;
     GridResult grid;
     bool has_grid = false;
-    // device-time events: LBVH build, normal estimation, interpolation
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    bool ev_used[3] = {false, false, false};
+    // device-time events: LBVH build, normal estimation, interpolation, PMC
+    // planar post-pass
+    cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool ev_used[4] = {false, false, false, false};
     float grid_ms[4] = {0, 0, 0, 0};
     ~lvrgb_surface_s() {
         for (auto& e : ev)
@@ -778,6 +779,7 @@ lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrg
         c.decomposition = g->decomposition;
         GridTimings tm;
         s->has_grid = false;
+        s->ev_used[3] = false;  // a new mesh has had no planar pass yet
         grid_reconstruct(s->T, s->normals, s->bb, c, s->ws, s->grid, s->d_err, st, &tm);
         for (int i = 0; i < 4; i++) s->grid_ms[i] = tm.ms[i];
         check_kernel_error(s, st);
@@ -834,6 +836,7 @@ lvrgb_status lvrgb_reconstruct_cells(lvrgb_surface s, float voxel_size, int32_t 
                                        st));
         }
         s->has_grid = false;
+        s->ev_used[3] = false;  // a new mesh has had no planar pass yet
         grid_from_cells(dc, dt, n, doff, nchunks, dbox, voxel_size, decomposition, s->ws, s->grid, s->d_err, st);
         LVRGB_CUDA(cudaStreamSynchronize(st));  // the host offsets and boxes are read by then
         check_kernel_error(s, st);
@@ -858,7 +861,10 @@ lvrgb_status lvrgb_optimize_planar_faces(lvrgb_surface s, int32_t kc, int64_t* m
         require(kc >= 1 && kc <= kSmemHeapMax, LVRGB_ERR_INVALID_ARGUMENT, "kc must be in 1..96");
         DeviceScope dev(s->device);
         cudaStream_t st = as_stream(stream);
+        record(s, 6, st);
         const long long m = optimize_planar_faces(s->T, s->d_box, s->grid, kc, s->ws, s->d_err, st);
+        record(s, 7, st);
+        s->ev_used[3] = true;
         check_kernel_error(s, st);
         if (moved) *moved = m;
     });
@@ -1146,6 +1152,10 @@ lvrgb_status lvrgb_surface_timings(lvrgb_surface s, float out[8]) {
             LVRGB_CUDA(cudaEventElapsedTime(&out[k], s->ev[2 * k], s->ev[2 * k + 1]));
         }
         for (int i = 0; i < 4; i++) out[3 + i] = s->grid_ms[i];
+        if (s->ev_used[3]) {
+            LVRGB_CUDA(cudaEventSynchronize(s->ev[7]));
+            LVRGB_CUDA(cudaEventElapsedTime(&out[7], s->ev[6], s->ev[7]));
+        }
     });
 }
 

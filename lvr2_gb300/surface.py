@@ -117,10 +117,10 @@ class Surface:
 
     def timings(self):
         """Device ms of the last calls: build, normals, interpolation, grid,
-        signed distance, culling, marching cubes."""
+        signed distance, culling, marching cubes, PMC planar post-pass."""
         out = np.zeros(8, np.float32)
         check(_lib.load().lvrgb_surface_timings(self._h, _ptr(out)))
-        return out[:7]
+        return out
 
     # ---- parameters (PointsetSurface::setKn/setKi/setKd/setFlipPoint) ------
     def set_k(self, kn=-1, ki=-1, kd=-1):

@@ -7,6 +7,7 @@ product path (lvr2_gb300) never imports this module.
 import ctypes
 import os
 import subprocess
+import time
 from pathlib import Path
 
 import numpy as np
@@ -166,8 +167,10 @@ class OracleSurface:
             args = [keep[0].ctypes.data_as(ctypes.c_void_p), keep[1].ctypes.data_as(ctypes.c_void_p),
                     keep[2].ctypes.data_as(ctypes.c_void_p), len(keep[1])]
         L = lib()
+        t0 = time.perf_counter()
         h = L.orc_reconstruct(self._h, nrm.reshape(-1), res, isvs, int(extrude), kd, dec,
                               int(canonical), *args, self.threads)
+        t1 = time.perf_counter()
         try:
             moved = 0
             if planar_kc > 0:
@@ -175,8 +178,13 @@ class OracleSurface:
         except BaseException:
             L.orc_recon_destroy(h)
             raise
+        t2 = time.perf_counter()
         out = _recon_result(h)
         out["planar_moved"] = moved
+        # wall-clock of the two library calls (grid + distances + culling +
+        # marching cubes; the planar pass), for the CPU baseline's stages
+        out["seconds_reconstruct"] = t1 - t0
+        out["seconds_planar"] = t2 - t1
         return out
 
 
