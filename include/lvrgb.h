@@ -484,6 +484,12 @@ lvrgb_status lvrgb_batch_grid_distances(lvrgb_batch b, const float* q, const int
  * on this project and keeps the fastest; returns the choice. */
 lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_radius, void* stream);
 
+/* Device time in ms of each of the five search rounds (k = 2kn ... 32kn;
+ * 0 for rounds that did not run) of the last eager (non-graph) run, which
+ * lvrgb_batch_calculate_normals(use_graph = 0) and lvrgb_batch_autotune make.
+ * Diagnostics; no lvr2 counterpart. */
+lvrgb_status lvrgb_batch_round_times(lvrgb_batch b, float ms[5]);
+
 /* Counters of the last run (layout of lvrgb_normal_stats) and device ms:
  * ms[0] tree, ms[1] normals, ms[2] interpolation (eager runs), ms[3] total. */
 lvrgb_status lvrgb_batch_stats(lvrgb_batch b, uint32_t counters[16], float ms[4]);

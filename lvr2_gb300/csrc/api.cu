@@ -1187,12 +1187,17 @@ struct lvrgb_batch_s {
     uint32_t* d_stats = nullptr;
     cudaStream_t bs = nullptr;  // the batch's own stream (graphs need a non-default stream)
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // per search round of the last timed eager run (lvrgb_batch_round_times)
+    cudaEvent_t round_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool rounds_timed = false;
     cudaGraphExec_t exec = nullptr;
     bool ran = false;
     float ms[4] = {0, 0, 0, 0};
     ~lvrgb_batch_s() {
         if (exec) cudaGraphExecDestroy(exec);
         for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        for (auto& e : round_ev)
             if (e) cudaEventDestroy(e);
         if (bs) cudaStreamDestroy(bs);
     }
@@ -1212,8 +1217,12 @@ NormalsConfig batch_config(const lvrgb_batch_s* b) {
 void batch_run_eager(lvrgb_batch b, bool timed) {
     if (b->R.prepared_bucket != b->cfg.bucket)
         batch_prepare(b->offsets, b->flips, batch_config(b), b->cfg.ki, b->cfg.bucket, b->ws, b->R, b->bs);
+    if (timed)
+        for (auto& e : b->round_ev)
+            if (!e) LVRGB_CUDA(cudaEventCreate(&e));
     batch_pipeline(b->d_xyz, batch_config(b), b->cfg.ki, b->cfg.seed_radius, b->ws, b->R, b->d_err, b->d_stats, b->bs,
-                   timed ? b->ev : nullptr);
+                   timed ? b->ev : nullptr, timed ? b->round_ev : nullptr);
+    if (timed) b->rounds_timed = true;
     b->ran = true;
 }
 
@@ -1426,6 +1435,17 @@ lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_
         batch_check(b);
         if (bucket) *bucket = bb;
         if (seed_radius) *seed_radius = br;
+    });
+}
+
+lvrgb_status lvrgb_batch_round_times(lvrgb_batch b, float ms[5]) {
+    return guarded([&] {
+        require(b != nullptr && ms != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        DeviceScope dev(b->device);
+        for (int i = 0; i < 5; i++) ms[i] = 0.0f;
+        if (!b->rounds_timed) return;
+        LVRGB_CUDA(cudaEventSynchronize(b->round_ev[5]));
+        for (int i = 0; i < 5; i++) LVRGB_CUDA(cudaEventElapsedTime(&ms[i], b->round_ev[i], b->round_ev[i + 1]));
     });
 }
 

@@ -1438,7 +1438,7 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
 
 void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
                                const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
-                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki) {
+                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki, cudaEvent_t* round_ev) {
     const int n = T.n;
     if (n == 0) return;
     if (g_num_sms == 0) {
@@ -1454,6 +1454,7 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
     const bool lbvh = cfg.nem == 4;  // LBVHIndex::knn_normals: one search with k = kn
     const int rounds = (cfg.adaptive && !lbvh) ? 5 : 1;
     size_t k = size_t(cfg.kn);
+    if (round_ev) LVRGB_CUDA(cudaEventRecord(round_ev[0], s));
     for (int round = 1; round <= rounds; round++) {
         if (!lbvh) k *= 2;  // the reference doubles k before every search
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
@@ -1485,7 +1486,10 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         launch_normals(A, round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), ws, s);
         if (round < rounds)
             compact_retry(flags, A.list, n, A.nq_dev, lists[(round + 1) & 1], counters + (round - 1), ws, s);
+        if (round_ev) LVRGB_CUDA(cudaEventRecord(round_ev[round], s));
     }
+    if (round_ev)
+        for (int r = rounds + 1; r <= 5; r++) LVRGB_CUDA(cudaEventRecord(round_ev[r], s));
 }
 
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,

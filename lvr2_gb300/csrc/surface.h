@@ -44,9 +44,12 @@ void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in
 // flip points).  All rounds are launched without host synchronisation: each
 // later round reads the previous round's retry count on the device, so the
 // sequence can be captured in a CUDA graph.
+// round_ev (optional, 6 events): recorded before round 1 and after each round
+// that runs (rounds that do not run get the previous round's event).
 void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
                                const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
-                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki);
+                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki,
+                               cudaEvent_t* round_ev = nullptr);
 
 // out_i = normalize(in_i + sum_{j in kNN_ki(p_i)} in_j), Morton order.
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,

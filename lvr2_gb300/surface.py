@@ -521,6 +521,12 @@ class Batch:
         check(_lib.load().lvrgb_batch_stats(self._h, _ptr(c), _ptr(ms)))
         return c, ms
 
+    def round_times(self):
+        """Device ms of each search round of the last eager run."""
+        ms = np.zeros(5, np.float32)
+        check(_lib.load().lvrgb_batch_round_times(self._h, _ptr(ms)))
+        return ms
+
 
 def kernel_launches():
     """Kernels launched by liblvrgb.so in this process."""
