@@ -415,6 +415,17 @@ lvrgb_status lvrgb_kernel_launches(uint64_t* out);
  * turns it off.  The handle stays usable after such a failure. */
 lvrgb_status lvrgb_debug_fail_allocation(int64_t n);
 
+/* Round collapsing of the adaptive normal search (on by default).  lvr2
+ * searches k = 2kn, 4kn, ... 32kn until the neighbourhood box passes
+ * (AdaptiveKSearchSurface.tcc:187-216); on scans, points on axis-aligned
+ * walls fail every round.  When almost nothing fits in round 2 or 3, the
+ * library searches once with the last round's k and tests the rounds in
+ * between on the prefixes of that sorted kNN, since kNN(k) is the first k of
+ * kNN(32 kn): the same normals and rounds with fewer searches.  enable = 0
+ * runs every round on its own (for tests that compare the two).  No lvr2
+ * counterpart. */
+lvrgb_status lvrgb_debug_round_collapse(int32_t enable);
+
 /* k nearest neighbours of nq queries among n points WITHOUT ANY DEVICE
  * ALLOCATION.  No counterpart in lvr2: it exists for callers that cannot
  * call cudaMalloc during a call (real-time loops or driver callbacks where an

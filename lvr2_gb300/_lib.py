@@ -27,7 +27,7 @@ EXPORTS = [
     "lvrgb_surface_num_points", "lvrgb_calculate_normals", "lvrgb_get_normals", "lvrgb_get_raw_normals",
     "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance",
     "lvrgb_distance_adjoint", "lvrgb_project_to_surface", "lvrgb_grid_distances",
-    "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_optimize_planar_faces", "lvrgb_mesh_vertex_normals", "lvrgb_vertex_normals", "lvrgb_mesh_vertex_colors", "lvrgb_get_cell_tsdf", "lvrgb_reconstruct_cells", "lvrgb_radius_search", "lvrgb_normals_from_neighbors", "lvrgb_debug_fail_allocation", "lvrgb_mesh_halfedges", "lvrgb_halfedges", "lvrgb_surface_set_scan_poses", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
+    "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_optimize_planar_faces", "lvrgb_mesh_vertex_normals", "lvrgb_vertex_normals", "lvrgb_mesh_vertex_colors", "lvrgb_get_cell_tsdf", "lvrgb_reconstruct_cells", "lvrgb_radius_search", "lvrgb_normals_from_neighbors", "lvrgb_debug_fail_allocation", "lvrgb_debug_round_collapse", "lvrgb_mesh_halfedges", "lvrgb_halfedges", "lvrgb_surface_set_scan_poses", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
     "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches", "lvrgb_knn_small_noalloc",
     "lvrgb_batch_create", "lvrgb_batch_destroy", "lvrgb_batch_calculate_normals", "lvrgb_batch_get_normals",
     "lvrgb_batch_grid_distances", "lvrgb_batch_autotune", "lvrgb_batch_stats", "lvrgb_batch_round_times",
@@ -106,6 +106,7 @@ def load(path=None):
     L.lvrgb_optimize_planar_faces.argtypes = [vp, i32, ctypes.POINTER(i64), vp]
     L.lvrgb_mesh_vertex_normals.argtypes = [vp, vp, i32, vp]
     L.lvrgb_debug_fail_allocation.argtypes = [i64]
+    L.lvrgb_debug_round_collapse.argtypes = [i32]
     L.lvrgb_surface_set_scan_poses.argtypes = [vp, vp, i64]
     L.lvrgb_mesh_halfedges.argtypes = [vp, ctypes.POINTER(HalfedgeInfo), vp, vp, vp, vp, vp, vp, i32, vp]
     L.lvrgb_halfedges.argtypes = [vp, vp, i64, i64, ctypes.POINTER(HalfedgeInfo), vp, vp, vp, vp, vp, vp, i32, vp]

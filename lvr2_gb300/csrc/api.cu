@@ -142,6 +142,7 @@ void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
         LVRGB_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int), st));
         throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack)  ? "kNN traversal exceeded its stack depth"
                                          : (h[0] & kErrWalk) ? "tree walk exceeded its bound (malformed tree)"
+                                         : (h[0] & kErrTma)  ? "a TMA copy of marching cubes did not complete"
                                                              : "a neighbour row was shorter than the RANSAC draws"};
     }
 }
@@ -1170,6 +1171,11 @@ lvrgb_status lvrgb_debug_fail_allocation(int64_t n) {
     return LVRGB_OK;
 }
 
+lvrgb_status lvrgb_debug_round_collapse(int32_t enable) {
+    g_round_collapse.store(enable ? 1 : 0);
+    return LVRGB_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1190,6 +1196,9 @@ struct lvrgb_batch_s {
     // per search round of the last timed eager run (lvrgb_batch_round_times)
     cudaEvent_t round_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool rounds_timed = false;
+    // search rounds collapsed after this one (0: none), chosen from the
+    // fitted-per-round counts of the previous eager run
+    int collapse_after = 0;
     cudaGraphExec_t exec = nullptr;
     bool ran = false;
     float ms[4] = {0, 0, 0, 0};
@@ -1221,7 +1230,7 @@ void batch_run_eager(lvrgb_batch b, bool timed) {
         for (auto& e : b->round_ev)
             if (!e) LVRGB_CUDA(cudaEventCreate(&e));
     batch_pipeline(b->d_xyz, batch_config(b), b->cfg.ki, b->cfg.seed_radius, b->ws, b->R, b->d_err, b->d_stats, b->bs,
-                   timed ? b->ev : nullptr, timed ? b->round_ev : nullptr);
+                   timed ? b->ev : nullptr, timed ? b->round_ev : nullptr, b->collapse_after);
     if (timed) b->rounds_timed = true;
     b->ran = true;
 }
@@ -1310,6 +1319,17 @@ lvrgb_status lvrgb_batch_destroy(lvrgb_batch b) {
     });
 }
 
+// After an eager run: collapse the search rounds from which almost nothing
+// fits (same results, fewer searches).  The choice is made from the counts of
+// that run and used by the following runs and the captured graph.
+void choose_collapse(lvrgb_batch b) {
+    uint32_t fitted[kNormalStats];
+    LVRGB_CUDA(cudaMemcpy(fitted, b->d_stats, sizeof(fitted), cudaMemcpyDeviceToHost));
+    int64_t n = 0;
+    for (int r = 0; r < 5; r++) n += fitted[r];
+    b->collapse_after = collapse_after_round(b->cfg.kn, b->cfg.nem, b->cfg.adaptive, fitted, n);
+}
+
 lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, void* stream) {
     return guarded([&] {
         NvtxRange nvtx_range("lvrgb.batch_calculate_normals");
@@ -1319,6 +1339,7 @@ lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, voi
         if (!use_graph) {
             on_batch_stream(b, caller, [&] { batch_run_eager(b, true); });
             batch_check(b);
+            choose_collapse(b);
             for (int i = 0; i < 3; i++) LVRGB_CUDA(cudaEventElapsedTime(&b->ms[i], b->ev[i], b->ev[i + 1]));
             LVRGB_CUDA(cudaEventElapsedTime(&b->ms[3], b->ev[0], b->ev[3]));
             return;
@@ -1326,6 +1347,10 @@ lvrgb_status lvrgb_batch_calculate_normals(lvrgb_batch b, int32_t use_graph, voi
         if (!b->exec) {
             // An eager pass sizes every buffer and sets kernel attributes, then
             // the same launch sequence is captured once.
+            on_batch_stream(b, caller, [&] { batch_run_eager(b, false); });
+            batch_check(b);
+            choose_collapse(b);
+            // and once more with that choice, so the capture finds every buffer sized
             on_batch_stream(b, caller, [&] { batch_run_eager(b, false); });
             batch_check(b);
             cudaGraph_t g = nullptr;

@@ -38,7 +38,7 @@ void batch_prepare(const std::vector<int64_t>& offsets, const std::vector<float>
 
 void batch_pipeline(const float* d_xyz, const NormalsConfig& cfg, int ki, int seed_radius, Workspace& ws,
                     BatchRun& R, int* d_err, uint32_t* d_stats, cudaStream_t s, cudaEvent_t* ev,
-                    cudaEvent_t* round_ev) {
+                    cudaEvent_t* round_ev, int collapse_after) {
     if (ev) LVRGB_CUDA(cudaEventRecord(ev[0], s));
     LVRGB_CUDA(cudaMemsetAsync(d_stats, 0, kNormalStats * sizeof(uint32_t), s));
     lbvh_segmented_build(d_xyz, R.tree, d_err, s);
@@ -46,7 +46,7 @@ void batch_pipeline(const float* d_xyz, const NormalsConfig& cfg, int ki, int se
     if (ev) LVRGB_CUDA(cudaEventRecord(ev[1], s));
     const size_t np = size_t(R.tree.T.n);
     compute_normals_segmented(R.tree.T, R.tree.segs, R.tree.bucket_scan, cfg, R.raw, R.kused, ws, d_err, d_stats, s,
-                              R.nbr, ki, round_ev);
+                              R.nbr, ki, round_ev, collapse_after);
     if (ev) LVRGB_CUDA(cudaEventRecord(ev[2], s));
     if (ki > 0)
         interpolate_from_lists(int(np), ki, R.nbr, R.raw, R.normals, s, R.tree.T.pts);

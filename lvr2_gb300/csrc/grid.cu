@@ -8,9 +8,12 @@
 // vertices form the 32-query groups of the signed-distance kNN.
 #include <algorithm>
 #include <climits>
-#include <optional>
 #include <cmath>
+#include <mutex>
+#include <optional>
 #include <stdexcept>
+
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
 
 #include "grid.h"
 #include "nvtx.h"
@@ -315,16 +318,12 @@ __device__ __forceinline__ void edge_vertex(const McCell& C, const Frame& F, int
 __device__ __forceinline__ bool same3(const float* a, const float* b) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
 
 // FastBox::getSurface / BilinearFastBox::getSurface: count (emit == false)
-// or write (emit == true) the faces of one valid cell.
+// or write (emit == true) the faces of valid cell t (index into the valid list).
 template <bool kEmit>
-__global__ void mc_kernel(const uint64_t* __restrict__ cell_keys, const uint32_t* __restrict__ corner,
-                          const float* __restrict__ qp_dist, const uint32_t* __restrict__ valid, int nvalid, Frame F,
-                          int pmc, uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
-                          uint64_t* __restrict__ ref_key, uint32_t* __restrict__ ref_val, float4* __restrict__ ref_pos) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nvalid) return;
-    McCell C;
-    load_cell(cell_keys, corner, qp_dist, valid[t], F, C);
+__device__ __forceinline__ void mc_cell(const McCell& C, const Frame& F, int pmc, uint32_t t,
+                                        uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
+                                        uint64_t* __restrict__ ref_key, uint32_t* __restrict__ ref_val,
+                                        float4* __restrict__ ref_pos) {
     const unsigned long long word = c_mc[C.index];
     const int ntri = int(word >> 60);
     uint32_t f = kEmit ? offsets[t] : 0u;
@@ -349,6 +348,172 @@ __global__ void mc_kernel(const uint64_t* __restrict__ cell_keys, const uint32_t
     }
     if (!kEmit) counts[t] = uint32_t(count);
 }
+
+template <bool kEmit>
+__global__ void mc_kernel(const uint64_t* __restrict__ cell_keys, const uint32_t* __restrict__ corner,
+                          const float* __restrict__ qp_dist, const uint32_t* __restrict__ valid, int nvalid, Frame F,
+                          int pmc, uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
+                          uint64_t* __restrict__ ref_key, uint32_t* __restrict__ ref_val, float4* __restrict__ ref_pos) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nvalid) return;
+    McCell C;
+    load_cell(cell_keys, corner, qp_dist, valid[t], F, C);
+    mc_cell<kEmit>(C, F, pmc, uint32_t(t), counts, offsets, ref_key, ref_val, ref_pos);
+}
+
+// ---- marching cubes over TMA-staged distance slabs ------------------------
+// When the box of grid vertices is small enough, their distances are
+// scattered into a dense volume D[z][y][x] (x padded to a multiple of 4, so
+// every row starts on a 16-byte boundary).  The valid cells of one 8x8x8
+// brick are a contiguous run of the valid list (lattice keys are Morton
+// codes, so key >> 9 names the brick); one CTA takes a run: a 3-D TMA tile
+// copy (cp.async.bulk.tensor, box 12 x 9 x 9 floats: the 9 x 9 x 9 corners of
+// the brick, the inner extent rounded up to a multiple of 16 bytes) brings its
+// corner distances into shared memory, completion is signalled on an
+// mbarrier, and every cell reads its eight corners from there instead of
+// gathering them through the corner-id array.  The faces are those of
+// mc_kernel, at the same places (counts and offsets by valid-list index).
+constexpr int kSlabX = 12, kSlabY = 9, kSlabZ = 9;
+constexpr uint32_t kSlabBytes = uint32_t(kSlabX * kSlabY * kSlabZ * sizeof(float));
+// try_wait polls (each may suspend for a while in hardware) before the copy
+// is reported as lost; a 3.9 KB tile copy needs a few microseconds.
+constexpr int kTmaWaitIters = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ bool mbar_wait_parity(uint32_t bar, uint32_t parity, int max_iters) {
+    for (int it = 0; it < max_iters; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n"
+            " .reg .pred P;\n"
+            " mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, P;\n"
+            "}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <bool kEmit>
+__global__ void __launch_bounds__(128) mc_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                     const uint64_t* __restrict__ cell_keys,
+                                                     const uint32_t* __restrict__ valid,
+                                                     const uint32_t* __restrict__ runs, Frame F, int pmc,
+                                                     uint32_t* __restrict__ counts,
+                                                     const uint32_t* __restrict__ offsets,
+                                                     uint64_t* __restrict__ ref_key, uint32_t* __restrict__ ref_val,
+                                                     float4* __restrict__ ref_pos, int* __restrict__ err) {
+    __shared__ __align__(128) float slab[kSlabZ * kSlabY * kSlabX];
+    __shared__ __align__(8) unsigned long long bar;
+    const uint32_t t0 = runs[blockIdx.x], t1 = runs[blockIdx.x + 1];
+    uint32_t bx, by, bz;
+    lattice_decode(cell_keys[valid[t0]], bx, by, bz);
+    bx &= ~7u;
+    by &= ~7u;
+    bz &= ~7u;
+    const uint32_t sbar = smem_addr(&bar), sdst = smem_addr(slab);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(kSlabBytes)
+                     : "memory");
+        // x = bx is a multiple of 8 floats: the copy starts on a 32-byte boundary
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];" ::"r"(sdst),
+            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(int(bx)), "r"(int(by)), "r"(int(bz)), "r"(sbar)
+            : "memory");
+    }
+    if (!mbar_wait_parity(sbar, 0, kTmaWaitIters)) {
+        if (threadIdx.x == 0) atomicOr(err, kErrTma);
+        // one more bounded wait for the copy in flight before the block leaves
+        mbar_wait_parity(sbar, 0, kTmaWaitIters);
+        return;
+    }
+    for (uint32_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        McCell C;
+        lattice_decode(cell_keys[valid[t]], C.rel[0], C.rel[1], C.rel[2]);
+        C.L[0] = int(C.rel[0]) + F.bx;
+        C.L[1] = int(C.rel[1]) + F.by;
+        C.L[2] = int(C.rel[2]) + F.bz;
+        const int lx = int(C.rel[0] - bx), ly = int(C.rel[1] - by), lz = int(C.rel[2] - bz);
+        C.index = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            C.d[k] = slab[((lz + c_corner[k][2]) * kSlabY + (ly + c_corner[k][1])) * kSlabX + lx + c_corner[k][0]];
+            if (C.d[k] > 0.0f) C.index |= 1 << k;
+        }
+        mc_cell<kEmit>(C, F, pmc, t, counts, offsets, ref_key, ref_val, ref_pos);
+    }
+}
+
+// Distances of the grid vertices into the dense volume (x fastest).
+__global__ void dense_volume_kernel(const uint64_t* __restrict__ qp_keys, const float* __restrict__ qp_dist, int n,
+                                    int X, int Y, int Z, float* __restrict__ D, int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t x, y, z;
+    lattice_decode(qp_keys[i], x, y, z);
+    if (x >= uint32_t(X) || y >= uint32_t(Y) || z >= uint32_t(Z)) {  // outside the planned box: not written
+        atomicOr(err, kErrTma);
+        return;
+    }
+    D[(size_t(z) * Y + y) * X + x] = qp_dist[i];
+}
+
+// Brick runs of the valid list: run r covers valid[runs[r], runs[r + 1]).
+__global__ void brick_flags_kernel(const uint64_t* __restrict__ cell_keys, const uint32_t* __restrict__ valid, int n,
+                                   uint32_t* __restrict__ flags) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    flags[t] = (t == 0 || (cell_keys[valid[t]] >> 9) != (cell_keys[valid[t - 1]] >> 9)) ? 1u : 0u;
+}
+__global__ void brick_runs_kernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, int n,
+                                  uint32_t* __restrict__ runs) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > n) return;
+    if (t == n) runs[pos[n]] = uint32_t(n);
+    else if (flags[t]) runs[pos[t]] = uint32_t(t);
+}
+
+using TensorMapEncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                          const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                          CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                          CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (null when it is not available, in
+// which case marching cubes gathers its corners as before).
+TensorMapEncodeTiled tensor_map_encoder() {
+    static std::once_flag once;
+    static TensorMapEncodeTiled fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<TensorMapEncodeTiled>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// The dense-slab plan of mc_stage: volume extents and the TMA descriptor.
+struct SlabPlan {
+    bool on = false;
+    int X = 0, Y = 0, Z = 0;
+    float* D = nullptr;
+    uint32_t* runs = nullptr;
+    int nruns = 0;
+    CUtensorMap map;
+};
 
 __global__ void vertex_out_kernel(const uint32_t* __restrict__ first_ref, int nv, const float4* __restrict__ ref_pos,
                                   float* __restrict__ verts) {
@@ -453,7 +618,55 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
 namespace {
 // Marching cubes over the valid cells of R (FastReconstruction::getMesh with
 // FastBox / BilinearFastBox): count, scan, emit, deduplicate the vertices.
-void mc_stage(GridResult& R, const Frame& F, int kbits, int decomposition, Workspace& ws, cudaStream_t s) {
+// The dense volume, the brick runs and the TMA descriptor of the slab path,
+// when the box of grid vertices (ext: vertices per axis, relative to the
+// base) holds at most 16 volume entries per vertex (plus 1M) and 2^28 in all,
+// spans at least one slab in every direction, and the driver encodes
+// tensor maps.  Otherwise on = false and marching cubes gathers its corners.
+SlabPlan plan_slabs(const GridResult& R, const int ext[3], size_t nvalid, Workspace& ws, int* d_err, cudaStream_t s) {
+    SlabPlan P;
+    if (nvalid == 0 || R.nqp == 0) return P;
+    const TensorMapEncodeTiled enc = tensor_map_encoder();
+    if (!enc) return P;
+    const size_t X = (size_t(std::max(ext[0], 1)) + 3) & ~size_t(3), Y = size_t(std::max(ext[1], 1)),
+                 Z = size_t(std::max(ext[2], 1));
+    const size_t vol = X * Y * Z;
+    if (X < size_t(kSlabX) || Y < size_t(kSlabY) || Z < size_t(kSlabZ)) return P;
+    if (vol > (size_t(1) << 28) || vol > 16 * size_t(R.nqp) + (size_t(1) << 20)) return P;
+    float* D = ws.get<float>("mc.dense", vol);
+    cuuint64_t dims[3] = {cuuint64_t(X), cuuint64_t(Y), cuuint64_t(Z)};
+    cuuint64_t strides[2] = {cuuint64_t(X * sizeof(float)), cuuint64_t(X * Y * sizeof(float))};
+    cuuint32_t box[3] = {cuuint32_t(kSlabX), cuuint32_t(kSlabY), cuuint32_t(kSlabZ)};
+    cuuint32_t elem[3] = {1, 1, 1};
+    if (enc(&P.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, D, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+        return SlabPlan();
+    // entries that are no grid vertex keep whatever the buffer held: they are
+    // never read, since the eight corners of a valid cell are grid vertices
+    dense_volume_kernel<<<ceil_div(size_t(R.nqp), 256), 256, 0, s>>>(R.qp_keys, R.qp_dist, int(R.nqp), int(X),
+                                                                      int(Y), int(Z), D, d_err);
+    LVRGB_LAUNCH_CHECK();
+    uint32_t* flags = ws.get<uint32_t>("mc.bflags", nvalid);
+    uint32_t* pos = ws.get<uint32_t>("mc.bpos", nvalid + 1);
+    brick_flags_kernel<<<ceil_div(nvalid, 256), 256, 0, s>>>(R.cell_keys, R.valid_cells, int(nvalid), flags);
+    LVRGB_LAUNCH_CHECK();
+    void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nvalid));
+    exclusive_scan_u32(flags, pos, nvalid, stmp, pos + nvalid, s);
+    P.nruns = int(uint32_t(read_u64(ws, pos + nvalid, sizeof(uint32_t), s)));
+    P.runs = ws.get<uint32_t>("mc.runs", size_t(P.nruns) + 1);
+    brick_runs_kernel<<<ceil_div(nvalid + 1, 256), 256, 0, s>>>(flags, pos, int(nvalid), P.runs);
+    LVRGB_LAUNCH_CHECK();
+    P.X = int(X);
+    P.Y = int(Y);
+    P.Z = int(Z);
+    P.D = D;
+    P.on = true;
+    return P;
+}
+
+void mc_stage(GridResult& R, const Frame& F, int kbits, const int ext[3], int decomposition, Workspace& ws,
+              int* d_err, cudaStream_t s) {
     const uint64_t* ck = R.cell_keys;
     const uint32_t* cell_corner = R.cell_corner;
     const uint32_t* valid = R.valid_cells;
@@ -463,11 +676,30 @@ void mc_stage(GridResult& R, const Frame& F, int kbits, int decomposition, Works
     size_t nf = 0;
     uint32_t* fcount = ws.get<uint32_t>("mc.count", nvalid);
     uint32_t* foff = ws.get<uint32_t>("mc.off", nvalid + 1);
-    if (nvalid) {
-        mc_kernel<false><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                               cfg.decomposition == 1, fcount, nullptr, nullptr,
-                                                               nullptr, nullptr);
+    const SlabPlan slabs = plan_slabs(R, ext, nvalid, ws, d_err, s);
+    // count (kEmit false) or emit the faces of every valid cell
+    auto mc_pass = [&](bool emit, uint64_t* rk, uint32_t* rv, float4* rp) {
+        if (slabs.on) {
+            if (emit)
+                mc_tma_kernel<true><<<slabs.nruns, 128, 0, s>>>(slabs.map, ck, valid, slabs.runs, F,
+                                                                 cfg.decomposition == 1, nullptr, foff, rk, rv, rp,
+                                                                 d_err);
+            else
+                mc_tma_kernel<false><<<slabs.nruns, 128, 0, s>>>(slabs.map, ck, valid, slabs.runs, F,
+                                                                  cfg.decomposition == 1, fcount, nullptr, nullptr,
+                                                                  nullptr, nullptr, d_err);
+        } else if (emit) {
+            mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
+                                                                  cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
+        } else {
+            mc_kernel<false><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid),
+                                                                   F, cfg.decomposition == 1, fcount, nullptr,
+                                                                   nullptr, nullptr, nullptr);
+        }
         LVRGB_LAUNCH_CHECK();
+    };
+    if (nvalid) {
+        mc_pass(false, nullptr, nullptr, nullptr);
         void* stmp = ws.get<unsigned char>("grid.scantmp", scan_temp_bytes(nvalid));
         exclusive_scan_u32(fcount, foff, nvalid, stmp, foff + nvalid, s);
         nf = size_t(uint32_t(read_u64(ws, foff + nvalid, sizeof(uint32_t), s)));
@@ -482,9 +714,7 @@ void mc_stage(GridResult& R, const Frame& F, int kbits, int decomposition, Works
     const bool dense_edges = use_dense(kbits + 2, nref);
     float* verts = nullptr;
     if (nf && dense_edges) {
-        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
-        LVRGB_LAUNCH_CHECK();
+        mc_pass(true, rk, rv, rp);
         const size_t NE = size_t(1) << (kbits + 2);
         uint32_t* eflags = ws.get<uint32_t>("mc.dflags", NE);
         uint32_t* epos = ws.get<uint32_t>("mc.dpos", NE + 1);
@@ -501,9 +731,7 @@ void mc_stage(GridResult& R, const Frame& F, int kbits, int decomposition, Works
         uint64_t* rk2 = ws.get<uint64_t>("mc.rk2", nref);
         uint32_t* rv2 = ws.get<uint32_t>("mc.rv2", nref);
         uint32_t* first = ws.get<uint32_t>("mc.first", nref);
-        mc_kernel<true><<<ceil_div(nvalid, 128), 128, 0, s>>>(ck, cell_corner, R.qp_dist, valid, int(nvalid), F,
-                                                              cfg.decomposition == 1, nullptr, foff, rk, rv, rp);
-        LVRGB_LAUNCH_CHECK();
+        mc_pass(true, rk, rv, rp);
         void* tmp = ws.get<unsigned char>("grid.sorttmp", radix_sort_temp_bytes<uint64_t>(nref));
         if (radix_sort_pairs<uint64_t>(rk, rv, rk2, rv2, nref, 0, kbits + 2, tmp, s)) {
             std::swap(rk, rk2);
@@ -682,7 +910,8 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     timer.mark(3, s);
     stage.emplace("lvrgb.marching_cubes");
 
-    mc_stage(R, F, kbits, cfg.decomposition, ws, s);
+    const int ext[3] = {top[0] + 1, top[1] + 1, top[2] + 1};
+    mc_stage(R, F, kbits, ext, cfg.decomposition, ws, d_err, s);
     timer.mark(4, s);
     stage.reset();
     timer.finish(timings, s);
@@ -896,7 +1125,8 @@ void grid_from_cells(const float* centers, const float* tsdf, int n, const int64
     if (nc) iota_u32(valid, nc, s);
     R.ncells_valid = (long long)nc;
     R.valid_cells = valid;
-    mc_stage(R, F, kbits, decomposition, ws, s);
+    const int ext[3] = {rng[3] - R.base[0] + 3, rng[4] - R.base[1] + 3, rng[5] - R.base[2] + 3};
+    mc_stage(R, F, kbits, ext, decomposition, ws, d_err, s);
 }
 
 namespace {

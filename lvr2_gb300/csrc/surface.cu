@@ -2,6 +2,7 @@
 // calculateSurfaceNormals), normal interpolation, kNN rows and
 // getInterpolatedNormal, all on the warp-cooperative LBVH traversal.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <functional>
 #include <random>
@@ -157,7 +158,21 @@ struct NormalsArgs {
     const SegInfo* segs;
     const uint16_t* bucket_scan;
     const uint32_t* nq_dev;
+    // Collapsed rounds (one-warp-per-query kernel only): this launch is the
+    // last round's search (K = 32 kn) standing in for rounds round_prefix0 ..
+    // 5.  kNN(k) is the first k of kNN(K) in (d2, index) order, so the first
+    // kprefix[p] neighbours are exactly the search of round round_prefix0 + p;
+    // the first of them whose box test passes is fitted, as the round-by-round
+    // sequence would.  nprefix = 0: a plain round.
+    int nprefix = 0;
+    int kprefix[3] = {0, 0, 0};
+    int round_prefix0 = 0;
+    // Scale from the previous round's k-th squared distance to a search bound:
+    // 2.5 per doubling of k (the squared k-th distance grows by 2 on a surface,
+    // 4 along a line; above 2 most searches need no second pass).
+    float bound_growth = 2.5f;
 };
+
 
 // BaseVector::normalize with IEEE operations (null vector unchanged).
 __device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
@@ -177,8 +192,9 @@ struct NbrPass {
     float r[6];        // sums of (p - q)(p - q)^T in IEEE order (nem 2)
 };
 
-template <int kNem>
-__device__ __forceinline__ void neighbour_pass(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, NbrPass& P) {
+// key_at(s): the s-th neighbour key, ascending (d2, index) order.
+template <int kNem, class KeyAt>
+__device__ __forceinline__ void neighbour_pass(const Lbvh& T, KeyAt key_at, int cnt, float4 q, NbrPass& P) {
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         P.lo[a] = FLT_MAX; P.hi[a] = -FLT_MAX; P.s[a] = 0.0f; P.c[a] = 0.0f;
@@ -187,7 +203,7 @@ __device__ __forceinline__ void neighbour_pass(const Lbvh& T, const LaneHeap& he
     for (int a = 0; a < 6; a++) P.r[a] = 0.0f;
 #pragma unroll 4
     for (int s = 0; s < cnt; s++) {
-        const float4 p = neighbour_point(T, heap.at(s));
+        const float4 p = neighbour_point(T, key_at(s));
         P.lo[0] = fminf(p.x, P.lo[0]); P.lo[1] = fminf(p.y, P.lo[1]); P.lo[2] = fminf(p.z, P.lo[2]);
         P.hi[0] = fmaxf(p.x, P.hi[0]); P.hi[1] = fmaxf(p.y, P.hi[1]); P.hi[2] = fmaxf(p.z, P.hi[2]);
         if (kNem == 4) {
@@ -291,9 +307,9 @@ __device__ __forceinline__ void solve_plane(float gap_thr, float4 q, const float
 }
 
 // Second pass over a lane's heap: the centred sums of nem 3 / nem 0.
-template <int kNem>
-__device__ __forceinline__ void centred_sums(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q,
-                                             const float mean[3], float S[6]) {
+template <int kNem, class KeyAt>
+__device__ __forceinline__ void centred_sums(const Lbvh& T, KeyAt key_at, int cnt, float4 q, const float mean[3],
+                                             float S[6]) {
     const float mx = mean[0], my = mean[1], mz = mean[2];
     float C[6] = {0, 0, 0, 0, 0, 0};
     if (kNem == 3) {
@@ -304,7 +320,7 @@ __device__ __forceinline__ void centred_sums(const Lbvh& T, const LaneHeap& heap
     }
 #pragma unroll 4
     for (int s = 0; s < cnt; s++) {
-        const float4 p = neighbour_point(T, heap.at(s));
+        const float4 p = neighbour_point(T, key_at(s));
         const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
         if (kNem == 3) {
             kahan_add(S[0], C[0], ex * ex);
@@ -323,13 +339,13 @@ __device__ __forceinline__ void centred_sums(const Lbvh& T, const LaneHeap& heap
     }
 }
 
-template <int kNem>
-__device__ __forceinline__ void fit_plane(const NormalsArgs& A, const LaneHeap& heap, int cnt, float4 q,
-                                          const NbrPass& P, float n[3], bool& fp64) {
+template <int kNem, class KeyAt>
+__device__ __forceinline__ void fit_plane(const NormalsArgs& A, KeyAt key_at, int cnt, float4 q, const NbrPass& P,
+                                          float n[3], bool& fp64) {
     float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0};
     if (kNem != 2) {
         plane_mean<kNem>(P.s, cnt, mean);
-        centred_sums<kNem>(A.T, heap, cnt, q, mean, S);
+        centred_sums<kNem>(A.T, key_at, cnt, q, mean, S);
     }
     solve_plane<kNem>(A.gap_thr, q, mean, S, P.r, n, fp64);
 }
@@ -486,7 +502,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
             const int cnt = heap.real;
             heap.sort_ascending();
             NbrPass P;
-            neighbour_pass<kNem>(A.T, heap, cnt, q, P);
+            const auto key_at = [&](int s) { return heap.at(s); };
+            neighbour_pass<kNem>(A.T, key_at, cnt, q, P);
             bool fit = true;
             if (A.adaptive && !A.last_round) {
                 // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
@@ -502,7 +519,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
                 if (kNem == 4) {
                     lbvh_knn_normal(A.T, heap, cnt, q, fx, fy, fz, n);
                 } else {
-                    fit_plane<kNem>(A, heap, cnt, q, P, n, fp64);
+                    fit_plane<kNem>(A, key_at, cnt, q, P, n, fp64);
                     // Flip toward the flip point; Normal::operator-() re-normalises.
                     const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
                     const float dot =
@@ -543,7 +560,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
 // normals_kernel for K > kSmemHeapMax: one warp per query (wide.cuh), the
 // neighbourhood sums reduced across the warp.  The neighbour set, the box
 // test and therefore the round in which a point is fitted are the same as in
-// the per-lane kernel.
+// the per-lane kernel.  With collapsed rounds (A.nprefix > 0) the launch is
+// the last round's search, and the rounds it stands in for are tested on the
+// prefixes of its kNN; a prefix of at most kSmemHeapMax keys is fitted with
+// the per-lane kernel's arithmetic, a longer one with this kernel's, as the
+// rounds would have been run one by one.
 // x * 2^e, exact unless the result leaves the normal range.
 __device__ __forceinline__ float mul_pow2(float x, int e) {
     while (e > 126) {
@@ -583,13 +604,13 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 }
 
 constexpr int kWideWarps = 8;  // warps per block
-// Growth of the squared k-th neighbour distance when k doubles: 2 on a
-// surface, 4 along a line; above 2 most searches need no second pass.
-constexpr float kBoundGrowth = 2.5f;
 constexpr int kWideTileMax = 32;  // queries per warp tile (consecutive queries chain their bounds)
 
-template <int kNem>
+// kPrefix: compiled with the collapsed-round code (A.nprefix read); without
+// it the kernel keeps the registers of a plain round.
+template <int kNem, bool kPrefix>
 __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(NormalsArgs A) {
+    const int nprefix = kPrefix ? A.nprefix : 0;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WideState W;
@@ -648,7 +669,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
             float estimate = inf;
             if (A.round > 1 && A.kth_d2) {
                 const float prev = A.kth_d2[pos];
-                if (prev < FLT_MAX) estimate = __fmul_rn(prev, kBoundGrowth);
+                if (prev < FLT_MAX) estimate = __fmul_rn(prev, A.bound_growth);
             }
             float bound = fminf(chain, estimate);
             for (int attempt = 0; attempt < 3; attempt++) {
@@ -670,100 +691,151 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
                 cx = q.x; cy = q.y; cz = q.z;
                 cscan = scan;
             }
-            // pass 1: neighbourhood box (min / max: exact in any order)
-            float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-            for (int i = lane; i < cnt; i += 32) {
-                const float4 p = neighbour_point(A.T, W.keys[i]);
-                lo[0] = fminf(p.x, lo[0]); lo[1] = fminf(p.y, lo[1]); lo[2] = fminf(p.z, lo[2]);
-                hi[0] = fmaxf(p.x, hi[0]); hi[1] = fmaxf(p.y, hi[1]); hi[2] = fmaxf(p.z, hi[2]);
-            }
+            // The neighbourhood that is fitted: with collapsed rounds the first
+            // kprefix[p] keys (those at or below their k-th key, use_thr) of
+            // the first round whose box test passes, else all cnt keys.
+            int use_cnt = cnt, fit_round = A.round, kfit = A.K;
+            unsigned long long use_thr = ~0ull;
+            float lo[3], hi[3];
+            bool fit = false;
+            for (int pr = 0; pr <= nprefix && !fit; pr++) {
+                const bool full = pr == nprefix;
+                const int m = full ? cnt : min(A.kprefix[pr], cnt);
+                const unsigned long long thr = (m == cnt || m <= 0) ? ~0ull : warp_select(W.keys, cnt, m, W.hist);
+                // neighbourhood box (min / max: exact in any order)
+                lo[0] = lo[1] = lo[2] = FLT_MAX;
+                hi[0] = hi[1] = hi[2] = -FLT_MAX;
+                for (int i = lane; i < cnt; i += 32) {
+                    const unsigned long long key = W.keys[i];
+                    if (key > thr) continue;
+                    const float4 p = neighbour_point(A.T, key);
+                    lo[0] = fminf(p.x, lo[0]); lo[1] = fminf(p.y, lo[1]); lo[2] = fminf(p.z, lo[2]);
+                    hi[0] = fmaxf(p.x, hi[0]); hi[1] = fmaxf(p.y, hi[1]); hi[2] = fmaxf(p.z, hi[2]);
+                }
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                lo[a] = warp_min_f(lo[a]);
-                hi[a] = warp_max_f(hi[a]);
-            }
-            bool fit = true;
-            if (A.adaptive && !A.last_round) {
-                // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
-                const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
-                const float e = 0.05f;
-                fit = dx >= __fmul_rn(e, dy) && dx >= __fmul_rn(e, dz) && dy >= __fmul_rn(e, dx) &&
-                      dy >= __fmul_rn(e, dz) && dz >= __fmul_rn(e, dx) && dz >= __fmul_rn(e, dy);
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = warp_min_f(lo[a]);
+                    hi[a] = warp_max_f(hi[a]);
+                }
+                fit = true;
+                if (A.adaptive && !(full && A.last_round)) {
+                    // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
+                    const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]),
+                                dz = __fsub_rn(hi[2], lo[2]);
+                    const float e = 0.05f;
+                    fit = dx >= __fmul_rn(e, dy) && dx >= __fmul_rn(e, dz) && dy >= __fmul_rn(e, dx) &&
+                          dy >= __fmul_rn(e, dz) && dz >= __fmul_rn(e, dx) && dz >= __fmul_rn(e, dy);
+                }
+                if (fit && !full) {
+                    use_cnt = m;
+                    use_thr = thr;
+                    fit_round = A.round_prefix0 + pr;
+                    kfit = A.kprefix[pr];
+                }
             }
             if (!fit) {
                 retry |= 1u << j;
                 if (A.kth_d2 && lane == 0) A.kth_d2[pos] = ctau;
                 continue;
             }
-            // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
-            // box), accumulated in 64-bit fixed point: exact and independent
-            // of the order in which the search left the neighbours, so every
-            // tree layout of the same points gives the same normal.
-            const int E = box_exponent(lo, hi, q);
-            float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0}, r[6] = {0, 0, 0, 0, 0, 0};
-            if (kNem == 2) {
-                long long acc[6] = {0, 0, 0, 0, 0, 0};
-                for (int i = lane; i < cnt; i += 32) {
-                    const float4 p = neighbour_point(A.T, W.keys[i]);
-                    const float ux = mul_pow2(__fsub_rn(p.x, q.x), -E), uy = mul_pow2(__fsub_rn(p.y, q.y), -E),
-                                uz = mul_pow2(__fsub_rn(p.z, q.z), -E);
-                    acc[0] += to_fixed(__fmul_rn(ux, ux));
-                    acc[1] += to_fixed(__fmul_rn(ux, uy));
-                    acc[2] += to_fixed(__fmul_rn(ux, uz));
-                    acc[3] += to_fixed(__fmul_rn(uy, uy));
-                    acc[4] += to_fixed(__fmul_rn(uy, uz));
-                    acc[5] += to_fixed(__fmul_rn(uz, uz));
-                }
-#pragma unroll
-                for (int a = 0; a < 6; a++) r[a] = from_fixed(warp_sum_ll(acc[a]));
-            } else {
-                long long acc1[3] = {0, 0, 0};
-                for (int i = lane; i < cnt; i += 32) {
-                    const float4 p = neighbour_point(A.T, W.keys[i]);
-                    acc1[0] += to_fixed(mul_pow2(__fsub_rn(p.x, q.x), -E));
-                    acc1[1] += to_fixed(mul_pow2(__fsub_rn(p.y, q.y), -E));
-                    acc1[2] += to_fixed(mul_pow2(__fsub_rn(p.z, q.z), -E));
-                }
-                float su[3], mu[3];
-#pragma unroll
-                for (int a = 0; a < 3; a++) su[a] = from_fixed(warp_sum_ll(acc1[a]));
-                plane_mean<kNem>(su, cnt, mu);
-                long long acc[6] = {0, 0, 0, 0, 0, 0};
-                for (int i = lane; i < cnt; i += 32) {
-                    const float4 p = neighbour_point(A.T, W.keys[i]);
-                    const float ex = __fsub_rn(mul_pow2(__fsub_rn(p.x, q.x), -E), mu[0]);
-                    const float ey = __fsub_rn(mul_pow2(__fsub_rn(p.y, q.y), -E), mu[1]);
-                    const float ez = __fsub_rn(mul_pow2(__fsub_rn(p.z, q.z), -E), mu[2]);
-                    if (kNem == 3) {
-                        acc[0] += to_fixed(__fmul_rn(ex, ex));
-                        acc[1] += to_fixed(__fmul_rn(ex, ey));
-                        acc[2] += to_fixed(__fmul_rn(ex, ez));
-                        acc[3] += to_fixed(__fmul_rn(ey, ey));
-                        acc[4] += to_fixed(__fmul_rn(ey, ez));
-                        acc[5] += to_fixed(__fmul_rn(ez, ez));
-                    } else {
-                        acc[0] += to_fixed(__fmul_rn(ex, ex));
-                        acc[1] += to_fixed(__fmul_rn(ex, ez));
-                        acc[2] += to_fixed(__fmul_rn(ez, ez));
-                        acc[3] += to_fixed(__fmul_rn(ex, ey));
-                        acc[4] += to_fixed(__fmul_rn(ez, ey));
-                    }
-                }
-                // nem 3: the query point's own term (its offset from the mean is -mu)
-                const float own[6] = {__fmul_rn(mu[0], mu[0]), __fmul_rn(mu[0], mu[1]), __fmul_rn(mu[0], mu[2]),
-                                      __fmul_rn(mu[1], mu[1]), __fmul_rn(mu[1], mu[2]), __fmul_rn(mu[2], mu[2])};
-#pragma unroll
-                for (int a = 0; a < 6; a++) {
-                    const long long own_fx = (kNem == 3) ? to_fixed(own[a]) : 0ll;
-                    S[a] = from_fixed(warp_sum_ll(acc[a]) + own_fx);
-                }
-                // the plane offset of nem 0 needs the mean in world units
-#pragma unroll
-                for (int a = 0; a < 3; a++) mean[a] = mul_pow2(mu[a], E);
-            }
             float n[3];
             bool fp64;
-            solve_plane<kNem>(A.gap_thr, q, mean, S, r, n, fp64);
+            if (kPrefix && nprefix && use_cnt <= kSmemHeapMax && kfit <= kSmemHeapMax) {
+                // A prefix of at most kSmemHeapMax keys stands for a round the
+                // per-lane kernel runs when rounds are not collapsed: it is fitted
+                // with that kernel's arithmetic (sums in ascending (d2, index)
+                // order), so the normal does not depend on the collapse.
+                unsigned long long* sorted = W.keys + (W.cap - kSmemHeapMax);
+                wide_sorted_prefix(W, use_cnt, [&](int rank, unsigned long long key) { sorted[rank] = key; });
+                __syncwarp();
+                float nn[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (lane == 0) {
+                    const auto key_at = [&](int s) { return sorted[s]; };
+                    NbrPass P;
+                    neighbour_pass<kNem>(A.T, key_at, use_cnt, q, P);
+                    bool f64 = false;
+                    fit_plane<kNem>(A, key_at, use_cnt, q, P, nn, f64);
+                    nn[3] = f64 ? 1.0f : 0.0f;
+                }
+#pragma unroll
+                for (int a = 0; a < 3; a++) n[a] = __shfl_sync(kFull, nn[a], 0);
+                fp64 = __shfl_sync(kFull, nn[3], 0) != 0.0f;
+                __syncwarp();
+            } else {
+                // Sums in the frame u = (p - q) * 2^-E with |u| < 1 (E from the
+                // box), accumulated in 64-bit fixed point: exact and independent
+                // of the order in which the search left the neighbours, so every
+                // tree layout of the same points gives the same normal.
+                const int E = box_exponent(lo, hi, q);
+                float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0}, r[6] = {0, 0, 0, 0, 0, 0};
+                if (kNem == 2) {
+                    long long acc[6] = {0, 0, 0, 0, 0, 0};
+                    for (int i = lane; i < cnt; i += 32) {
+                        const unsigned long long key = W.keys[i];
+                        if (key > use_thr) continue;
+                        const float4 p = neighbour_point(A.T, key);
+                        const float ux = mul_pow2(__fsub_rn(p.x, q.x), -E), uy = mul_pow2(__fsub_rn(p.y, q.y), -E),
+                                    uz = mul_pow2(__fsub_rn(p.z, q.z), -E);
+                        acc[0] += to_fixed(__fmul_rn(ux, ux));
+                        acc[1] += to_fixed(__fmul_rn(ux, uy));
+                        acc[2] += to_fixed(__fmul_rn(ux, uz));
+                        acc[3] += to_fixed(__fmul_rn(uy, uy));
+                        acc[4] += to_fixed(__fmul_rn(uy, uz));
+                        acc[5] += to_fixed(__fmul_rn(uz, uz));
+                    }
+    #pragma unroll
+                    for (int a = 0; a < 6; a++) r[a] = from_fixed(warp_sum_ll(acc[a]));
+                } else {
+                    long long acc1[3] = {0, 0, 0};
+                    for (int i = lane; i < cnt; i += 32) {
+                        const unsigned long long key = W.keys[i];
+                        if (key > use_thr) continue;
+                        const float4 p = neighbour_point(A.T, key);
+                        acc1[0] += to_fixed(mul_pow2(__fsub_rn(p.x, q.x), -E));
+                        acc1[1] += to_fixed(mul_pow2(__fsub_rn(p.y, q.y), -E));
+                        acc1[2] += to_fixed(mul_pow2(__fsub_rn(p.z, q.z), -E));
+                    }
+                    float su[3], mu[3];
+    #pragma unroll
+                    for (int a = 0; a < 3; a++) su[a] = from_fixed(warp_sum_ll(acc1[a]));
+                    plane_mean<kNem>(su, use_cnt, mu);
+                    long long acc[6] = {0, 0, 0, 0, 0, 0};
+                    for (int i = lane; i < cnt; i += 32) {
+                        const unsigned long long key = W.keys[i];
+                        if (key > use_thr) continue;
+                        const float4 p = neighbour_point(A.T, key);
+                        const float ex = __fsub_rn(mul_pow2(__fsub_rn(p.x, q.x), -E), mu[0]);
+                        const float ey = __fsub_rn(mul_pow2(__fsub_rn(p.y, q.y), -E), mu[1]);
+                        const float ez = __fsub_rn(mul_pow2(__fsub_rn(p.z, q.z), -E), mu[2]);
+                        if (kNem == 3) {
+                            acc[0] += to_fixed(__fmul_rn(ex, ex));
+                            acc[1] += to_fixed(__fmul_rn(ex, ey));
+                            acc[2] += to_fixed(__fmul_rn(ex, ez));
+                            acc[3] += to_fixed(__fmul_rn(ey, ey));
+                            acc[4] += to_fixed(__fmul_rn(ey, ez));
+                            acc[5] += to_fixed(__fmul_rn(ez, ez));
+                        } else {
+                            acc[0] += to_fixed(__fmul_rn(ex, ex));
+                            acc[1] += to_fixed(__fmul_rn(ex, ez));
+                            acc[2] += to_fixed(__fmul_rn(ez, ez));
+                            acc[3] += to_fixed(__fmul_rn(ex, ey));
+                            acc[4] += to_fixed(__fmul_rn(ez, ey));
+                        }
+                    }
+                    // nem 3: the query point's own term (its offset from the mean is -mu)
+                    const float own[6] = {__fmul_rn(mu[0], mu[0]), __fmul_rn(mu[0], mu[1]), __fmul_rn(mu[0], mu[2]),
+                                          __fmul_rn(mu[1], mu[1]), __fmul_rn(mu[1], mu[2]), __fmul_rn(mu[2], mu[2])};
+    #pragma unroll
+                    for (int a = 0; a < 6; a++) {
+                        const long long own_fx = (kNem == 3) ? to_fixed(own[a]) : 0ll;
+                        S[a] = from_fixed(warp_sum_ll(acc[a]) + own_fx);
+                    }
+                    // the plane offset of nem 0 needs the mean in world units
+    #pragma unroll
+                    for (int a = 0; a < 3; a++) mean[a] = mul_pow2(mu[a], E);
+                }
+                solve_plane<kNem>(A.gap_thr, q, mean, S, r, n, fp64);
+            }
             // Flip toward the flip point; Normal::operator-() re-normalises.
             const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
             const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n[0], tx), __fmul_rn(n[1], ty)), __fmul_rn(n[2], tz));
@@ -773,12 +845,13 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
             }
             if (lane == 0) {
                 A.normals[pos] = make_float4(n[0], n[1], n[2], 0.0f);
-                if (A.kused) A.kused[pos] = A.K;
+                if (A.kused) A.kused[pos] = kfit;
                 if (fp64) atomicAdd(A.stats + 5, 1u);
+                if (nprefix) atomicAdd(A.stats + (fit_round - 1), 1u);
             }
             if (A.nbr) {
                 // kNN(ki) of the interpolation = the first ki of this kNN(K >= ki)
-                const int m = min(A.ki, cnt);
+                const int m = min(A.ki, use_cnt);
                 uint32_t* col = A.nbr + pos;
                 const size_t stride = size_t(A.T.n);
                 const uint32_t* inv = A.T.inv;
@@ -787,7 +860,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
                 });
                 for (int t = m + lane; t < A.ki; t += 32) col[size_t(t) * stride] = 0xffffffffu;
             }
-            fitted |= 1u << j;
+            if (!nprefix) fitted |= 1u << j;
         }
         if (lane == 0 && fitted) atomicAdd(A.stats + (A.round - 1), uint32_t(__popc(fitted)));
         if (lane < nt) A.flags[tile * TQ + lane] = uint8_t((retry >> lane) & 1u);
@@ -1089,6 +1162,20 @@ void launch_normals(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t s);
 
 }  // namespace
 
+std::atomic<int> g_round_collapse{1};
+
+int collapse_after_round(int kn, int nem, int adaptive, const uint32_t fitted[5], int64_t n) {
+    if (!adaptive || nem == 4 || nem == 1 || !g_round_collapse.load()) return 0;
+    if (int64_t(kn) * 32 <= kSmemHeapMax) return 0;  // the last round needs the one-warp-per-query kernel
+    int64_t left = n;
+    for (int r = 1; r <= 3; r++) {
+        const int64_t q = left;  // queries of round r
+        left -= int64_t(fitted[r - 1]);
+        if (r >= 2 && left > 0 && 10 * int64_t(fitted[r - 1]) < q) return r;
+    }
+    return 0;
+}
+
 HeapPlan plan_heap(int nq, int K, Workspace& ws) {
     if (g_num_sms == 0) {
         int dev = 0;
@@ -1163,8 +1250,13 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
     const WidePlan P = plan_wide(grid_nq, A.K, ws);
     A.wide_tile = P.tile;
     A.gheap = P.gbuf;
-    set_smem(normals_wide_kernel<kNem>, P.smem);
-    normals_wide_kernel<kNem><<<P.blocks, kWideWarps * 32, P.smem, s>>>(A);
+    if (A.nprefix) {
+        set_smem(normals_wide_kernel<kNem, true>, P.smem);
+        normals_wide_kernel<kNem, true><<<P.blocks, kWideWarps * 32, P.smem, s>>>(A);
+    } else {
+        set_smem(normals_wide_kernel<kNem, false>, P.smem);
+        normals_wide_kernel<kNem, false><<<P.blocks, kWideWarps * 32, P.smem, s>>>(A);
+    }
     LVRGB_LAUNCH_CHECK();
 }
 
@@ -1395,8 +1487,13 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
     const uint32_t* list = nullptr;
     size_t k = size_t(cfg.kn);
     const bool lbvh = cfg.nem == 4;  // LBVHIndex::knn_normals: one search with k = kn
+    bool collapse = false;  // this launch stands in for every remaining round
     for (int round = 1; round <= 5 && nq > 0; round++) {
         if (!lbvh) k *= 2;  // the reference doubles k before every search
+        const int round0 = round;
+        if (collapse) {
+            for (; round < 5; round++) k *= 2;
+        }
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
         const int last = (!cfg.adaptive || lbvh || round == 5) ? 1 : 0;
         uint32_t* retry = lists[round & 1];
@@ -1423,13 +1520,27 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.bucket_scan = nullptr;
         A.nq_dev = nullptr;
         A.flip_target = cfg.flip_target;
+        if (collapse) {
+            A.nprefix = round - round0;
+            A.round_prefix0 = round0;
+            for (int p = 0; p < A.nprefix; p++) A.kprefix[p] = int(std::min<size_t>(size_t(cfg.kn) << (round0 + p), size_t(1) << 20));
+            A.bound_growth = 1.0f;
+            for (int d = round0; d <= round; d++) A.bound_growth *= 2.5f;
+        }
         launch_normals(A, nq, ws, s);
         if (last) break;
         compact_retry(flags, list, nq, nullptr, retry, counter, ws, s);
         h_count[0] = 0;
         LVRGB_CUDA(cudaMemcpyAsync(h_count, counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         LVRGB_CUDA(cudaStreamSynchronize(s));
-        nq = int(uint32_t(h_count[0]));
+        const int next = int(uint32_t(h_count[0]));
+        // Almost nothing fitted in this round (scans: points on axis-aligned
+        // walls and floors fail the box test in every round): search once with
+        // the last round's k and test the rounds in between on its prefixes.
+        if (cfg.adaptive && !lbvh && cfg.nem != 1 && g_round_collapse.load() && round >= 2 && round <= 3 &&
+            next > 0 && 10 * int64_t(nq - next) < int64_t(nq) && int64_t(cfg.kn) * 32 > kSmemHeapMax)
+            collapse = true;
+        nq = next;
         list = retry;
     }
     // nem 1: the rounds above (run as nem 0) fixed each point's k
@@ -1438,7 +1549,8 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
 
 void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
                                const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
-                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki, cudaEvent_t* round_ev) {
+                               uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki, cudaEvent_t* round_ev,
+                               int collapse_after) {
     const int n = T.n;
     if (n == 0) return;
     if (g_num_sms == 0) {
@@ -1453,10 +1565,18 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
     LVRGB_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s));
     const bool lbvh = cfg.nem == 4;  // LBVHIndex::knn_normals: one search with k = kn
     const int rounds = (cfg.adaptive && !lbvh) ? 5 : 1;
+    if (rounds == 1 || int64_t(cfg.kn) * 32 <= kSmemHeapMax || collapse_after < 2 || collapse_after > 3)
+        collapse_after = 0;
     size_t k = size_t(cfg.kn);
     if (round_ev) LVRGB_CUDA(cudaEventRecord(round_ev[0], s));
     for (int round = 1; round <= rounds; round++) {
         if (!lbvh) k *= 2;  // the reference doubles k before every search
+        // With collapse_after = r, the launch after round r is the last
+        // round's search standing in for rounds r + 1 .. 5.
+        const int round0 = round;
+        const bool collapse = collapse_after && round == collapse_after + 1;
+        if (collapse)
+            for (; round < rounds; round++) k *= 2;
         const int K = int(std::min<size_t>(k, size_t(1) << 20));
         NormalsArgs A;
         A.T = T;
@@ -1481,12 +1601,23 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.segs = segs;
         A.bucket_scan = bucket_scan;
         A.flip_target = nullptr;
+        if (collapse) {
+            // the list and count of the round the collapsed launch starts at
+            A.list = lists[round0 & 1];
+            A.nq_dev = counters + (round0 - 2);
+            A.nprefix = round - round0;
+            A.round_prefix0 = round0;
+            for (int p = 0; p < A.nprefix; p++) A.kprefix[p] = int(std::min<size_t>(size_t(cfg.kn) << (round0 + p), size_t(1) << 20));
+            A.bound_growth = 1.0f;
+            for (int d = round0; d <= round; d++) A.bound_growth *= 2.5f;
+        }
         // Later rounds read their query count on the device: launch a fixed
         // grid that strides over however many queries the previous round left.
         launch_normals(A, round == 1 ? n : std::min(n, g_num_sms * 8 * kWarpsPerBlock * 32), ws, s);
         if (round < rounds)
             compact_retry(flags, A.list, n, A.nq_dev, lists[(round + 1) & 1], counters + (round - 1), ws, s);
-        if (round_ev) LVRGB_CUDA(cudaEventRecord(round_ev[round], s));
+        if (round_ev)
+            for (int r = round0; r <= round; r++) LVRGB_CUDA(cudaEventRecord(round_ev[r], s));
     }
     if (round_ev)
         for (int r = rounds + 1; r <= 5; r++) LVRGB_CUDA(cudaEventRecord(round_ev[r], s));

@@ -1,5 +1,6 @@
 // surface.h -- host launchers of the point-surface kernels (surface.cu).
 #pragma once
+#include <atomic>
 #include "lbvh.cuh"
 #include "workspace.h"
 
@@ -45,11 +46,20 @@ void interpolate_from_lists(int n, int ki, const uint32_t* nbr, const float4* in
 // later round reads the previous round's retry count on the device, so the
 // sequence can be captured in a CUDA graph.
 // round_ev (optional, 6 events): recorded before round 1 and after each round
-// that runs (rounds that do not run get the previous round's event).
+// that runs (rounds that do not run get the previous round's event; a
+// collapsed launch's time falls on its first round).
+// collapse_after = r (2 or 3): one search with the last round's k stands in
+// for rounds r + 1 .. 5, which are tested on its prefixes (same results);
+// 0: round by round.  collapse_after_round picks r from a previous run's
+// fitted-per-round counts.
 void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_t* bucket_scan,
                                const NormalsConfig& cfg, float4* normals, int32_t* kused, Workspace& ws, int* d_err,
                                uint32_t* d_stats, cudaStream_t s, uint32_t* nbr, int ki,
-                               cudaEvent_t* round_ev = nullptr);
+                               cudaEvent_t* round_ev = nullptr, int collapse_after = 0);
+int collapse_after_round(int kn, int nem, int adaptive, const uint32_t fitted[5], int64_t n);
+
+// Whether compute_normals* may collapse rounds (lvrgb_debug_round_collapse).
+extern std::atomic<int> g_round_collapse;
 
 // out_i = normalize(in_i + sum_{j in kNN_ki(p_i)} in_j), Morton order.
 void interpolate_normals(const Lbvh& T, int ki, const float4* in, float4* out, Workspace& ws, int* d_err,

@@ -5,7 +5,9 @@ Checks: the forward values equal lvrgb_distance bit for bit; d/dq against
 central finite differences (h = 1e-3, samples whose kd-neighbourhood changes
 within +-h are masked and counted); d/dpoints and d/dnormals against a float64
 restatement of the analytic gradient over the same neighbourhoods; d/dnormals
-against finite differences of the normals; projection lands on the zero level.
+against finite differences of the normals; projection lands on the zero level,
+bit-exact against a float32 restatement of its operations and within float32
+rounding of a float64 projection over the same neighbourhoods.
 """
 import numpy as np
 import pytest
@@ -158,6 +160,70 @@ def test_projection_reaches_zero_level(scene):
     _, _, gq, _, _ = s.distance_adjoint(Q, np.ones(len(Q), np.float32), None, want_points=False, want_normals=False)
     ref = Q - d0[:, None] * gq
     assert np.abs(p1 - ref).max() <= 1e-6
+
+
+def project_restatement(oracle_surface, P, N, Q, steps, dtype):
+    """Newton projection x <- x - d(x) n(x) restated in numpy: at each step the
+    kd nearest points of x (the oracle's kNN rows, ascending (d2, index)), the
+    mean point and the normalised mean normal summed in that order, d the
+    projected distance.  dtype float32 repeats the kernel's operations one by
+    one (each rounded on its own); float64 is the reference projection.
+    Also returns, per query, the last step's sum of |n_j| over |sum of n_j|:
+    how much the normalisation of the mean normal amplifies rounding."""
+    f = np.dtype(dtype).type
+    x = Q.astype(dtype)
+    nh = np.zeros_like(x)
+    amp = np.ones(len(Q))
+    for _ in range(steps):
+        rows, _, cnt = oracle_surface.knn(x.astype(np.float32), KD)
+        assert (cnt == KD).all()
+        p = np.zeros_like(x)
+        m = np.zeros_like(x)
+        mag = np.zeros(len(Q))
+        for j in range(KD):
+            p = p + P[rows[:, j].astype(np.int64)].astype(dtype)
+            m = m + N[rows[:, j].astype(np.int64)].astype(dtype)
+            mag += np.linalg.norm(N[rows[:, j].astype(np.int64)].astype(np.float64), axis=1)
+        c = f(KD)
+        p = p / c
+        m = m / c
+        ln = np.sqrt((m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1]) + m[:, 2] * m[:, 2])
+        n = np.where(ln[:, None] > 0, m / np.where(ln > 0, ln, f(1))[:, None], m)
+        r = x - p
+        d = (r[:, 0] * n[:, 0] + r[:, 1] * n[:, 1]) + r[:, 2] * n[:, 2]
+        x = x - d[:, None] * n
+        nh = n
+        amp = mag / np.maximum(np.linalg.norm(m.astype(np.float64), axis=1) * KD, 1e-300)
+    return x, nh, amp
+
+
+def test_projection_against_restatements(scene, oracle_mod):
+    """Three Newton steps: bit-exact against the float32 restatement of the
+    kernel's operations, and within 2e-6 (a few float32 ulps of the unit-cube
+    coordinates) of the float64 projection over the same neighbourhoods,
+    wherever the float32 and float64 paths meet the same neighbours; the
+    normals within float32 rounding amplified by the normalisation of the
+    mean normal (1e-6 rad times sum |n_j| / |sum n_j|)."""
+    s, P, N, Q = scene
+    o = oracle_mod.OracleSurface(P)
+    pos, nrm = s.project_to_surface(Q, steps=3)
+    x32, n32, _ = project_restatement(o, P, N, Q, 3, np.float32)
+    assert np.array_equal(pos, x32) and np.array_equal(nrm, n32)
+    x64, n64, amp = project_restatement(o, P, N, Q, 3, np.float64)
+    # a float32 rounding can move a position across a kNN tie between steps;
+    # compare where the last step's neighbourhoods agree
+    r32, _, _ = o.knn(pos, KD)
+    r64, _, _ = o.knn(x64.astype(np.float32), KD)
+    same = np.all(np.sort(r32, 1) == np.sort(r64, 1), axis=1)
+    assert same.mean() > 0.99
+    err = np.linalg.norm(pos.astype(np.float64) - x64, axis=1)[same]
+    assert np.percentile(err, 99.9) <= 2e-6, np.percentile(err, [50, 99.9, 100])
+    # both normalised in float64 first: a float32 unit vector is 1 only to an ulp
+    a = nrm.astype(np.float64)
+    a /= np.linalg.norm(a, axis=1, keepdims=True)
+    b = n64 / np.linalg.norm(n64, axis=1, keepdims=True)
+    ang = np.arccos(np.clip(np.abs(np.sum(a * b, axis=1)), -1, 1))[same]
+    assert (ang <= 1e-6 * amp[same] + 1e-7).all(), np.percentile(np.degrees(ang), [50, 99.9, 100])
 
 
 def test_reconstructed_vertices_project(gb):

@@ -113,9 +113,13 @@ def test_normals_against_oracle(gb, oracle_mod, name, nem):
     assert stats[:5].sum() == len(P)
     good = np.isfinite(on).all(1) & np.isfinite(gn).all(1)
     if nem == 0:
-        # least-squares y = f(x, z) is ill-conditioned for planes parallel to y:
-        # compare where the normal is not within 25 degrees of horizontal
-        good &= np.abs(on[:, 1]) > 0.42
+        # least-squares y = f(x, z) cannot represent a plane parallel to y, and
+        # its solution's error grows like 1 / |n_y| towards one: compare where
+        # the normal is more than 6 degrees from horizontal (|n_y| > 0.1)
+        steep = np.abs(on[:, 1]) <= 0.1
+        print("nem 0 on %s: %.2f%% of normals within 6 degrees of horizontal left out"
+              % (name, 100 * np.mean(steep & good)))
+        good &= ~steep
     ang = angle_deg(gn[good], on[good])
     assert np.percentile(ang, 99.9) <= ANGLE_P999_DEG, np.percentile(ang, [50, 99, 99.9, 100])
     # sign consistency: same orientation wherever the flip direction is not
