@@ -184,6 +184,7 @@ def batched_measurement(args, steps):
     plain_ms = ev0.elapsed_time(ev1)
     with lvr2_gb300.Batch(scans, flips, kn=10, ki=10, nem=3) as b:
         bucket, radius = b.autotune()
+        tuning = b.tuning()
         b.calculate_normals(use_graph=True)
         times = []
         for _ in range(max(steps, 1)):
@@ -197,7 +198,8 @@ def batched_measurement(args, steps):
     return {"workload": "scan_project_64", "scans": 64, "points": n, "kn": 10, "ki": 10, "nem": 3,
             "plain_ms": plain_ms, "plain_normals_per_s": n / (plain_ms / 1000.0),
             "batched_ms": batched_ms, "batched_normals_per_s": n / (batched_ms / 1000.0),
-            "speedup_vs_plain": plain_ms / batched_ms, "autotuned": {"bucket": bucket, "seed_radius": radius},
+            "speedup_vs_plain": plain_ms / batched_ms,
+            "autotuned": dict(zip(["bucket", "seed_radius", "wide_tile", "wide_buffer_slack"], tuning)),
             "batched_stage_ms": {"tree": float(stage[0]), "normals": float(stage[1]), "interpolation": float(stage[2])},
             "fitted_per_round": [int(x) for x in counters[:5]],
             "normals_ms_per_round": [float(x) for x in round_ms],

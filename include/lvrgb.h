@@ -491,9 +491,18 @@ lvrgb_status lvrgb_batch_get_normals(lvrgb_batch b, float* normals, int32_t on_d
 lvrgb_status lvrgb_batch_grid_distances(lvrgb_batch b, const float* q, const int64_t* q_offsets, float voxel_size,
                                         float* distance, uint8_t* invalid, int32_t on_device, void* stream);
 
-/* Times the pipeline for each candidate (LBVH bucket 16/32, seed radius 1/2)
- * on this project and keeps the fastest; returns the choice. */
+/* Times the pipeline on this project and keeps the fastest candidate, stage
+ * by stage: LBVH bucket 16/32 with seed radius 1/2; then the queries per warp
+ * tile of the one-warp-per-query searches (automatic, 4, 16, 32); then their
+ * key buffer size (2, 3 or 4 times k).  Returns the bucket and seed radius;
+ * lvrgb_batch_tuning reports all four. */
 lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_radius, void* stream);
+
+/* The launch shape the batch uses (what lvrgb_batch_autotune chose): out[0]
+ * LBVH bucket size, [1] seed radius, [2] queries per warp tile of the
+ * one-warp-per-query searches (k > 96; 0 = chosen from the query count),
+ * [3] their key buffer size in units of k.  No lvr2 counterpart. */
+lvrgb_status lvrgb_batch_tuning(lvrgb_batch b, int32_t out[4]);
 
 /* Device time in ms of each of the five search rounds (k = 2kn ... 32kn;
  * 0 for rounds that did not run) of the last eager (non-graph) run, which

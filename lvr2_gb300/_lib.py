@@ -30,7 +30,7 @@ EXPORTS = [
     "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_optimize_planar_faces", "lvrgb_mesh_vertex_normals", "lvrgb_vertex_normals", "lvrgb_mesh_vertex_colors", "lvrgb_get_cell_tsdf", "lvrgb_reconstruct_cells", "lvrgb_radius_search", "lvrgb_normals_from_neighbors", "lvrgb_debug_fail_allocation", "lvrgb_debug_round_collapse", "lvrgb_mesh_halfedges", "lvrgb_halfedges", "lvrgb_surface_set_scan_poses", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
     "lvrgb_surface_set_points", "lvrgb_surface_timings", "lvrgb_kernel_launches", "lvrgb_knn_small_noalloc",
     "lvrgb_batch_create", "lvrgb_batch_destroy", "lvrgb_batch_calculate_normals", "lvrgb_batch_get_normals",
-    "lvrgb_batch_grid_distances", "lvrgb_batch_autotune", "lvrgb_batch_stats", "lvrgb_batch_round_times",
+    "lvrgb_batch_grid_distances", "lvrgb_batch_autotune", "lvrgb_batch_stats", "lvrgb_batch_round_times", "lvrgb_batch_tuning",
     "lvrgb_last_error", "lvrgb_version",
 ]
 
@@ -132,6 +132,7 @@ def load(path=None):
     L.lvrgb_batch_autotune.argtypes = [vp, vp, vp, vp]
     L.lvrgb_batch_stats.argtypes = [vp, vp, vp]
     L.lvrgb_batch_round_times.argtypes = [vp, vp]
+    L.lvrgb_batch_tuning.argtypes = [vp, vp]
     L.lvrgb_last_error.restype = ctypes.c_char_p
     L.lvrgb_version.restype = ctypes.c_char_p
     for name in EXPORTS:

@@ -1199,6 +1199,8 @@ struct lvrgb_batch_s {
     // search rounds collapsed after this one (0: none), chosen from the
     // fitted-per-round counts of the previous eager run
     int collapse_after = 0;
+    // launch shape of the one-warp-per-query searches (lvrgb_batch_autotune)
+    int wide_tile = 0, wide_slack = 2;
     cudaGraphExec_t exec = nullptr;
     bool ran = false;
     float ms[4] = {0, 0, 0, 0};
@@ -1220,6 +1222,8 @@ NormalsConfig batch_config(const lvrgb_batch_s* b) {
     c.nem = b->cfg.nem;
     c.adaptive = b->cfg.adaptive;
     c.gap_threshold = b->cfg.gap_threshold > 0 ? b->cfg.gap_threshold : 1e-3f;
+    c.wide_tile = b->wide_tile;
+    c.wide_slack = b->wide_slack;
     return c;
 }
 
@@ -1430,20 +1434,26 @@ lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_
         require(b != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "batch is NULL");
         DeviceScope dev(b->device);
         cudaStream_t caller = as_stream(stream);
-        // Candidate tile shapes: LBVH bucket size and seed radius.  Each runs
-        // the whole pipeline twice; the second run is timed.
-        const int cands[4][2] = {{32, 1}, {32, 2}, {16, 1}, {16, 2}};
-        float best = 1e30f;
-        int bb = b->cfg.bucket, br = b->cfg.seed_radius;
-        for (const auto& c : cands) {
-            b->cfg.bucket = c[0];
-            b->cfg.seed_radius = c[1];
+        // Staged search, each candidate running the whole pipeline twice (the
+        // second run timed): LBVH bucket size and seed radius, then the
+        // one-warp-per-query kernel's queries per warp tile, then its key
+        // buffer size (in units of k).
+        auto timed_run = [&]() {
             float t = 0;
             for (int rep = 0; rep < 2; rep++) {
                 on_batch_stream(b, caller, [&] { batch_run_eager(b, true); });
                 batch_check(b);
                 LVRGB_CUDA(cudaEventElapsedTime(&t, b->ev[0], b->ev[3]));
             }
+            return t;
+        };
+        const int cands[4][2] = {{32, 1}, {32, 2}, {16, 1}, {16, 2}};
+        float best = 1e30f;
+        int bb = b->cfg.bucket, br = b->cfg.seed_radius;
+        for (const auto& c : cands) {
+            b->cfg.bucket = c[0];
+            b->cfg.seed_radius = c[1];
+            const float t = timed_run();
             if (t < best) {
                 best = t;
                 bb = c[0];
@@ -1452,6 +1462,29 @@ lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_
         }
         b->cfg.bucket = bb;
         b->cfg.seed_radius = br;
+        choose_collapse(b);
+        best = 1e30f;
+        int bt = 0;
+        for (int tile : {0, 4, 16, 32}) {
+            b->wide_tile = tile;
+            const float t = timed_run();
+            if (t < best) {
+                best = t;
+                bt = tile;
+            }
+        }
+        b->wide_tile = bt;
+        best = 1e30f;
+        int bs = 2;
+        for (int slack : {2, 3, 4}) {
+            b->wide_slack = slack;
+            const float t = timed_run();
+            if (t < best) {
+                best = t;
+                bs = slack;
+            }
+        }
+        b->wide_slack = bs;
         if (b->exec) {
             cudaGraphExecDestroy(b->exec);
             b->exec = nullptr;
@@ -1460,6 +1493,16 @@ lvrgb_status lvrgb_batch_autotune(lvrgb_batch b, int32_t* bucket, int32_t* seed_
         batch_check(b);
         if (bucket) *bucket = bb;
         if (seed_radius) *seed_radius = br;
+    });
+}
+
+lvrgb_status lvrgb_batch_tuning(lvrgb_batch b, int32_t out[4]) {
+    return guarded([&] {
+        require(b != nullptr && out != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        out[0] = b->cfg.bucket;
+        out[1] = b->cfg.seed_radius;
+        out[2] = b->wide_tile;
+        out[3] = b->wide_slack;
     });
 }
 

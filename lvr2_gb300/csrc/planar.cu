@@ -1,8 +1,9 @@
 // planar.cu -- BilinearFastBox::optimizePlanarFaces (BilinearFastBox.tcc:140-212),
 // the post-pass FastReconstruction::getMesh runs on every cell with kc = 5 for
 // PMC (FastReconstruction.tcc:158-168), on the whole mesh at once:
-//   1. every face edge as an undirected key (min vertex, max vertex), sorted;
-//      an edge whose key occurs once belongs to one face: a border edge,
+//   1. every face edge as an undirected key (min vertex, max vertex), packed
+//      into 2 x (bits of the vertex count) bits and sorted; an edge whose key
+//      occurs once belongs to one face: a border edge,
 //   2. one thread per valid cell counts the border edges of its faces and,
 //      for 1 or 2, marks both end vertices of each,
 //   3. the marked vertices, compacted and Morton-sorted, take the centroid of
@@ -21,13 +22,13 @@ namespace lvrgb {
 
 namespace {
 
-__global__ void edge_keys_kernel(const uint32_t* __restrict__ faces, int nf, uint64_t* __restrict__ keys,
+__global__ void edge_keys_kernel(const uint32_t* __restrict__ faces, int nf, int vbits, uint64_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3 * nf) return;
     const int f = i / 3, e = i - 3 * f;
     const uint64_t a = faces[3 * size_t(f) + e], b = faces[3 * size_t(f) + (e == 2 ? 0 : e + 1)];
-    keys[i] = a < b ? (a << 32) | b : (b << 32) | a;
+    keys[i] = a < b ? (a << vbits) | b : (b << vbits) | a;
     vals[i] = uint32_t(i);
 }
 
@@ -106,12 +107,12 @@ long long optimize_planar_faces(const Lbvh& T, const float* d_box, GridResult& R
     uint64_t* keys2 = ws.get<uint64_t>("planar.keys2", size_t(m3));
     uint32_t* vals = ws.get<uint32_t>("planar.vals", size_t(m3));
     uint32_t* vals2 = ws.get<uint32_t>("planar.vals2", size_t(m3));
-    edge_keys_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(R.faces, nf, keys, vals);
-    LVRGB_LAUNCH_CHECK();
     int vbits = 1;
     while (vbits < 32 && (uint64_t(1) << vbits) < uint64_t(nv)) vbits++;
+    edge_keys_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(R.faces, nf, vbits, keys, vals);
+    LVRGB_LAUNCH_CHECK();
     void* tmp = ws.get<unsigned char>("planar.sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(m3)));
-    if (radix_sort_pairs<uint64_t>(keys, vals, keys2, vals2, size_t(m3), 0, 32 + vbits, tmp, s)) {
+    if (radix_sort_pairs<uint64_t>(keys, vals, keys2, vals2, size_t(m3), 0, 2 * vbits, tmp, s)) {
         std::swap(keys, keys2);
         std::swap(vals, vals2);
     }

@@ -167,6 +167,10 @@ struct NormalsArgs {
     int nprefix = 0;
     int kprefix[3] = {0, 0, 0};
     int round_prefix0 = 0;
+    // one-warp-per-query launch shape requested by the caller (0: automatic)
+    // and its key-buffer size in units of K
+    int wide_tile_req = 0;
+    int wide_slack = 2;
     // Scale from the previous round's k-th squared distance to a search bound:
     // 2.5 per doubling of k (the squared k-th distance grows by 2 on a surface,
     // 4 along a line; above 2 most searches need no second pass).
@@ -192,9 +196,9 @@ struct NbrPass {
     float r[6];        // sums of (p - q)(p - q)^T in IEEE order (nem 2)
 };
 
-// key_at(s): the s-th neighbour key, ascending (d2, index) order.
-template <int kNem, class KeyAt>
-__device__ __forceinline__ void neighbour_pass(const Lbvh& T, KeyAt key_at, int cnt, float4 q, NbrPass& P) {
+// point_at(s): the s-th neighbour's point, ascending (d2, index) order.
+template <int kNem, class PointAt>
+__device__ __forceinline__ void neighbour_pass(PointAt point_at, int cnt, float4 q, NbrPass& P) {
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         P.lo[a] = FLT_MAX; P.hi[a] = -FLT_MAX; P.s[a] = 0.0f; P.c[a] = 0.0f;
@@ -203,11 +207,11 @@ __device__ __forceinline__ void neighbour_pass(const Lbvh& T, KeyAt key_at, int 
     for (int a = 0; a < 6; a++) P.r[a] = 0.0f;
 #pragma unroll 4
     for (int s = 0; s < cnt; s++) {
-        const float4 p = neighbour_point(T, key_at(s));
+        const float4 p = point_at(s);
         P.lo[0] = fminf(p.x, P.lo[0]); P.lo[1] = fminf(p.y, P.lo[1]); P.lo[2] = fminf(p.z, P.lo[2]);
         P.hi[0] = fmaxf(p.x, P.hi[0]); P.hi[1] = fmaxf(p.y, P.hi[1]); P.hi[2] = fmaxf(p.z, P.hi[2]);
         if (kNem == 4) {
-            // the box only (nem 4 sums in FP64 in lbvh_knn_normal)
+            // the box only (nem 4 sums in FP64 in lbvh_plane_fit)
         } else if (kNem == 2) {
             const float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
             P.r[0] = __fadd_rn(P.r[0], __fmul_rn(rx, rx));
@@ -307,9 +311,8 @@ __device__ __forceinline__ void solve_plane(float gap_thr, float4 q, const float
 }
 
 // Second pass over a lane's heap: the centred sums of nem 3 / nem 0.
-template <int kNem, class KeyAt>
-__device__ __forceinline__ void centred_sums(const Lbvh& T, KeyAt key_at, int cnt, float4 q, const float mean[3],
-                                             float S[6]) {
+template <int kNem, class PointAt>
+__device__ __forceinline__ void centred_sums(PointAt point_at, int cnt, float4 q, const float mean[3], float S[6]) {
     const float mx = mean[0], my = mean[1], mz = mean[2];
     float C[6] = {0, 0, 0, 0, 0, 0};
     if (kNem == 3) {
@@ -320,7 +323,7 @@ __device__ __forceinline__ void centred_sums(const Lbvh& T, KeyAt key_at, int cn
     }
 #pragma unroll 4
     for (int s = 0; s < cnt; s++) {
-        const float4 p = neighbour_point(T, key_at(s));
+        const float4 p = point_at(s);
         const float ex = (p.x - q.x) - mx, ey = (p.y - q.y) - my, ez = (p.z - q.z) - mz;
         if (kNem == 3) {
             kahan_add(S[0], C[0], ex * ex);
@@ -339,13 +342,13 @@ __device__ __forceinline__ void centred_sums(const Lbvh& T, KeyAt key_at, int cn
     }
 }
 
-template <int kNem, class KeyAt>
-__device__ __forceinline__ void fit_plane(const NormalsArgs& A, KeyAt key_at, int cnt, float4 q, const NbrPass& P,
+template <int kNem, class PointAt>
+__device__ __forceinline__ void fit_plane(const NormalsArgs& A, PointAt point_at, int cnt, float4 q, const NbrPass& P,
                                           float n[3], bool& fp64) {
     float mean[3] = {0, 0, 0}, S[6] = {0, 0, 0, 0, 0, 0};
     if (kNem != 2) {
         plane_mean<kNem>(P.s, cnt, mean);
-        centred_sums<kNem>(A.T, key_at, cnt, q, mean, S);
+        centred_sums<kNem>(point_at, cnt, q, mean, S);
     }
     solve_plane<kNem>(A.gap_thr, q, mean, S, P.r, n, fp64);
 }
@@ -418,11 +421,6 @@ __device__ __forceinline__ void lbvh_plane_fit(Point point, int cnt, float qx, f
     n[0] = float(wx);
     n[1] = float(wy);
     n[2] = float(wz);
-}
-
-__device__ __forceinline__ void lbvh_knn_normal(const Lbvh& T, const LaneHeap& heap, int cnt, float4 q, float fx,
-                                                float fy, float fz, float n[3]) {
-    lbvh_plane_fit([&](int s) { return neighbour_point(T, heap.at(s)); }, cnt, q.x, q.y, q.z, fx, fy, fz, n);
 }
 
 // LBVHIndex::calculate_normals (src/liblvr2/reconstruction/cuda/LBVHIndex.cu:586-642,
@@ -502,8 +500,18 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
             const int cnt = heap.real;
             heap.sort_ascending();
             NbrPass P;
-            const auto key_at = [&](int s) { return heap.at(s); };
-            neighbour_pass<kNem>(A.T, key_at, cnt, q, P);
+            // The first pass looks each neighbour's Morton position up once and
+            // keeps it in the low word of its key (the order is already fixed),
+            // so the later passes and the interpolation lists read it directly.
+            unsigned long long* hk = heap.h;
+            const auto first_point = [&](int s) {
+                const unsigned long long k = hk[s * 32];
+                const uint32_t at = __ldg(A.T.inv + key_idx(k));
+                hk[s * 32] = (k & 0xffffffff00000000ull) | at;
+                return __ldg(A.T.pts + at);
+            };
+            const auto point_at = [&](int s) { return __ldg(A.T.pts + key_idx(hk[s * 32])); };
+            neighbour_pass<kNem>(first_point, cnt, q, P);
             bool fit = true;
             if (A.adaptive && !A.last_round) {
                 // boundingBoxOK over the neighbourhood (AdaptiveKSearchSurface.tcc:337-350)
@@ -517,9 +525,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
                 float n[3];
                 bool fp64 = false;
                 if (kNem == 4) {
-                    lbvh_knn_normal(A.T, heap, cnt, q, fx, fy, fz, n);
+                    lbvh_plane_fit(point_at, cnt, q.x, q.y, q.z, fx, fy, fz, n);
                 } else {
-                    fit_plane<kNem>(A, key_at, cnt, q, P, n, fp64);
+                    fit_plane<kNem>(A, point_at, cnt, q, P, n, fp64);
                     // Flip toward the flip point; Normal::operator-() re-normalises.
                     const float tx = __fsub_rn(fx, q.x), ty = __fsub_rn(fy, q.y), tz = __fsub_rn(fz, q.z);
                     const float dot =
@@ -534,7 +542,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
                 if (A.nbr) {
                     // kNN(ki) of the interpolation = the first ki of this kNN(K >= ki)
                     for (int j = 0; j < A.ki; j++)
-                        A.nbr[size_t(j) * A.T.n + pos] = j < cnt ? __ldg(A.T.inv + key_idx(heap.at(j))) : 0xffffffffu;
+                        A.nbr[size_t(j) * A.T.n + pos] = j < cnt ? key_idx(hk[j * 32]) : 0xffffffffu;
                 }
                 if (fp64) atomicAdd(A.stats + 5, 1u);
             } else {
@@ -615,7 +623,7 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WideState W;
     W.K = A.K;
-    W.cap = wide_capacity(A.K);
+    W.cap = wide_capacity(A.K, A.wide_slack);
     W.hist = reinterpret_cast<uint32_t*>(smem) + wib * 256;
     W.keys = A.gheap ? A.gheap + (size_t(blockIdx.x) * kWideWarps + wib) * size_t(W.cap)
                      : reinterpret_cast<unsigned long long*>(smem + kWideWarps * 1024) + size_t(wib) * W.cap;
@@ -750,11 +758,11 @@ __global__ void __launch_bounds__(kWideWarps * 32, 4) normals_wide_kernel(Normal
                 __syncwarp();
                 float nn[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 if (lane == 0) {
-                    const auto key_at = [&](int s) { return sorted[s]; };
+                    const auto point_at = [&](int s) { return neighbour_point(A.T, sorted[s]); };
                     NbrPass P;
-                    neighbour_pass<kNem>(A.T, key_at, use_cnt, q, P);
+                    neighbour_pass<kNem>(point_at, use_cnt, q, P);
                     bool f64 = false;
-                    fit_plane<kNem>(A, key_at, use_cnt, q, P, nn, f64);
+                    fit_plane<kNem>(A, point_at, use_cnt, q, P, nn, f64);
                     nn[3] = f64 ? 1.0f : 0.0f;
                 }
 #pragma unroll
@@ -1209,10 +1217,11 @@ struct WidePlan {
     size_t smem;
     unsigned long long* gbuf;
 };
-WidePlan plan_wide(int grid_nq, int K, Workspace& ws) {
+WidePlan plan_wide(int grid_nq, int K, Workspace& ws, int tile_req = 0, int slack = 2) {
     WidePlan P;
-    const size_t per_warp = size_t(wide_capacity(K)) * sizeof(unsigned long long);
-    P.tile = std::max(2, std::min(kWideTileMax, grid_nq / (g_num_sms * 128)));
+    const size_t per_warp = size_t(wide_capacity(K, slack)) * sizeof(unsigned long long);
+    P.tile = tile_req > 0 ? std::min(tile_req, kWideTileMax)
+                          : std::max(2, std::min(kWideTileMax, grid_nq / (g_num_sms * 128)));
     const int tiles = ceil_div(std::max(grid_nq, 1), P.tile);
     const int need = std::max(1, ceil_div(tiles, kWideWarps));
     P.smem = size_t(kWideWarps) * 1024;
@@ -1247,7 +1256,7 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
         LVRGB_LAUNCH_CHECK();
         return;
     }
-    const WidePlan P = plan_wide(grid_nq, A.K, ws);
+    const WidePlan P = plan_wide(grid_nq, A.K, ws, A.wide_tile_req, A.wide_slack);
     A.wide_tile = P.tile;
     A.gheap = P.gbuf;
     if (A.nprefix) {
@@ -1520,6 +1529,8 @@ void compute_normals(const Lbvh& T, const NormalsConfig& cfg, float4* normals, i
         A.bucket_scan = nullptr;
         A.nq_dev = nullptr;
         A.flip_target = cfg.flip_target;
+        A.wide_tile_req = cfg.wide_tile;
+        A.wide_slack = std::max(2, cfg.wide_slack);
         if (collapse) {
             A.nprefix = round - round0;
             A.round_prefix0 = round0;
@@ -1601,6 +1612,8 @@ void compute_normals_segmented(const Lbvh& T, const SegInfo* segs, const uint16_
         A.segs = segs;
         A.bucket_scan = bucket_scan;
         A.flip_target = nullptr;
+        A.wide_tile_req = cfg.wide_tile;
+        A.wide_slack = std::max(2, cfg.wide_slack);
         if (collapse) {
             // the list and count of the round the collapsed launch starts at
             A.list = lists[round0 & 1];

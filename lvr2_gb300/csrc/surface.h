@@ -14,6 +14,11 @@ struct NormalsConfig {
     float gap_threshold = 1e-3f;  // relative eigengap below which the eigensolve runs in FP64
     // Optional per point (Morton position, device): its own flip point when w != 0.
     const float4* flip_target = nullptr;
+    // Launch shape of the one-warp-per-query kernel (k > kSmemHeapMax):
+    // queries per warp tile (0: chosen from the query count) and the key
+    // buffer's size in units of k (wide_capacity).  Tuning knobs only.
+    int wide_tile = 0;
+    int wide_slack = 2;
 };
 
 // Device counters written by compute_normals (uint32[16]):

@@ -38,9 +38,10 @@ struct WideState {
     float tau;                 // d2 part of thr (box pruning bound)
 };
 
-// Buffer capacity for a wide search of K: room for K kept keys, K more before
-// each compaction, and one bucket of slack.
-__host__ __device__ inline int wide_capacity(int K) { return ((2 * K + 64) + 31) / 32 * 32; }
+// Buffer capacity for a wide search of K: room for K kept keys, (slack - 1) K
+// more before each compaction, and one bucket of slack (slack >= 2; a larger
+// buffer compacts less often but takes more memory per warp).
+__host__ __device__ inline int wide_capacity(int K, int slack = 2) { return ((slack * K + 64) + 31) / 32 * 32; }
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll

@@ -521,6 +521,12 @@ class Batch:
         check(_lib.load().lvrgb_batch_stats(self._h, _ptr(c), _ptr(ms)))
         return c, ms
 
+    def tuning(self):
+        """(bucket, seed radius, wide tile, wide buffer slack) in use."""
+        out = np.zeros(4, np.int32)
+        check(_lib.load().lvrgb_batch_tuning(self._h, _ptr(out)))
+        return tuple(int(x) for x in out)
+
     def round_times(self):
         """Device ms of each search round of the last eager run."""
         ms = np.zeros(5, np.float32)
