@@ -105,12 +105,10 @@ struct LaneHeap {
         top = kKeyEmpty;
     }
     __device__ __forceinline__ float tau() const { return key_d2(top); }
-    __device__ __forceinline__ void sift_down(int i, int end, unsigned long long key) {
-        while (true) {
-            const int c0 = kHeapArity * i + 1;
-            if (c0 >= end) break;
-            unsigned long long best = h[c0 * 32];
-            int bc = c0;
+    // Largest child of a node whose first child is c0 (< end).
+    __device__ __forceinline__ void max_child(int c0, int end, unsigned long long& best, int& bc) const {
+        best = h[c0 * 32];
+        bc = c0;
 #pragma unroll
             for (int t = 1; t < kHeapArity; t++) {
                 const int c = c0 + t;
@@ -122,6 +120,14 @@ struct LaneHeap {
                     }
                 }
             }
+    }
+    __device__ __forceinline__ void sift_down(int i, int end, unsigned long long key) {
+        while (true) {
+            const int c0 = kHeapArity * i + 1;
+            if (c0 >= end) break;
+            unsigned long long best;
+            int bc;
+            max_child(c0, end, best, bc);
             if (best <= key) break;
             h[i * 32] = best;
             i = bc;
@@ -139,8 +145,24 @@ struct LaneHeap {
             if (fill == K) heapify();
             return;
         }
-        sift_down(0, K, key);
-        top = h[0];
+        // the root's level is peeled so that the new maximum is known without
+        // reading it back
+        if (K == 1) {
+            h[0] = key;
+            top = key;
+            return;
+        }
+        unsigned long long best;
+        int bc;
+        max_child(1, K, best, bc);
+        if (best <= key) {
+            h[0] = key;
+            top = key;
+            return;
+        }
+        h[0] = best;
+        top = best;
+        sift_down(bc, K, key);
     }
     // Completes the heap when fewer than K keys were offered (sentinels).
     __device__ __forceinline__ void finish() {
