@@ -81,14 +81,15 @@ struct GradArgs {
     AdjointOut out;
     unsigned long long* gheap;
     int* err;
+    int* tiles = nullptr;  // tile counter of a persistent launch
 };
 
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_adjoint_kernel(GradArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
-    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
-         tile += gridDim.x * kWarpsPerBlock) {
+    for (int tile = first_tile<kWarpsPerBlock>(A.tiles); tile * 32 < A.nq;
+         tile = next_tile<kWarpsPerBlock>(A.tiles, tile)) {
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
@@ -147,6 +148,7 @@ struct ProjectArgs {
     float* out_normal;
     unsigned long long* gheap;
     int* err;
+    int* tiles = nullptr;  // tile counter of a persistent launch
 };
 
 // Newton steps toward the zero level: x <- x - d(x) nh(x), a new kd
@@ -155,8 +157,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) project_kernel(ProjectArg
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
-    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
-         tile += gridDim.x * kWarpsPerBlock) {
+    for (int tile = first_tile<kWarpsPerBlock>(A.tiles); tile * 32 < A.nq;
+         tile = next_tile<kWarpsPerBlock>(A.tiles, tile)) {
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
@@ -215,6 +217,7 @@ void distance_adjoint(const Lbvh& T, const float4* normals, int kd, const float4
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
     set_smem(sdf_adjoint_kernel, P.smem);
+    A.tiles = persistent_tiles(sdf_adjoint_kernel, P, ws, s);
     sdf_adjoint_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }
@@ -236,6 +239,7 @@ void project_to_surface(const Lbvh& T, const float4* normals, int kd, const floa
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
     set_smem(project_kernel, P.smem);
+    A.tiles = persistent_tiles(project_kernel, P, ws, s);
     project_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }

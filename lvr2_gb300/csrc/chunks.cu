@@ -99,14 +99,15 @@ struct ChunkSdfArgs {
     uint8_t* invalid;
     unsigned long long* gheap;
     int* err;
+    int* tiles = nullptr;  // tile counter of a persistent launch
 };
 
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) chunk_sdf_kernel(ChunkSdfArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
-    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
-         tile += gridDim.x * kWarpsPerBlock) {
+    for (int tile = first_tile<kWarpsPerBlock>(A.tiles); tile * 32 < A.nq;
+         tile = next_tile<kWarpsPerBlock>(A.tiles, tile)) {
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
@@ -218,6 +219,7 @@ void chunk_grid_distances(const SegTree& tree, const float4* normals, int kd, co
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
     set_smem(chunk_sdf_kernel, P.smem);
+    A.tiles = persistent_tiles(chunk_sdf_kernel, P, ws, s);
     chunk_sdf_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }

@@ -191,6 +191,7 @@ struct SdfArgs {
     const float4* qs;
     int nq;
     double limit;  // 1.75 * voxelsize
+    int* tiles = nullptr;  // tile counter of a persistent launch
     float* dist;
     float* eucl;
     uint8_t* invalid;
@@ -216,8 +217,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) 
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
-    for (int tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); tile * 32 < A.nq;
-         tile += gridDim.x * kWarpsPerBlock) {
+    for (int tile = first_tile<kWarpsPerBlock>(A.tiles); tile * 32 < A.nq;
+         tile = next_tile<kWarpsPerBlock>(A.tiles, tile)) {
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
@@ -611,6 +612,7 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
     set_smem(sdf_kernel, P.smem);
+    A.tiles = persistent_tiles(sdf_kernel, P, ws, s);
     sdf_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }

@@ -427,6 +427,25 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     knn_traverse(T, qx, qy, qz, active, heap, stage, err, st, seed);
 }
 
+// Tile order of the per-lane kNN kernels.  With a counter (zeroed before the
+// launch) a warp takes the next 32-query tile in ascending order whenever it
+// becomes free, so no warp idles until the other warps of its block finish
+// and the tiles in flight stay neighbours in Morton order; without one, warp
+// w of the grid takes tiles w, w + W, w + 2W, ... (W warps in the grid).
+__device__ __forceinline__ int take_tile(int* counter) {
+    int t = 0;
+    if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1);
+    return __shfl_sync(kFull, t, 0);
+}
+template <int kWarps>
+__device__ __forceinline__ int first_tile(int* counter) {
+    return counter ? take_tile(counter) : int(blockIdx.x) * kWarps + int(threadIdx.x >> 5);
+}
+template <int kWarps>
+__device__ __forceinline__ int next_tile(int* counter, int tile) {
+    return counter ? take_tile(counter) : tile + int(gridDim.x) * kWarps;
+}
+
 // Shared-memory carving of a kNN kernel block: kWarps candidate buffers of 64
 // float4, then (when gheap == nullptr) kWarps lane-interleaved heaps of K keys.
 // With a global heap buffer, each resident warp owns K*32 keys of it.

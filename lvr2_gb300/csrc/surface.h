@@ -1,5 +1,6 @@
 // surface.h -- host launchers of the point-surface kernels (surface.cu).
 #pragma once
+#include <algorithm>
 #include <atomic>
 #include "lbvh.cuh"
 #include "workspace.h"
@@ -115,5 +116,26 @@ struct HeapPlan {
     unsigned long long* gheap = nullptr;
 };
 HeapPlan plan_heap(int nq, int K, Workspace& ws);
+
+// Persistent form of a per-lane kNN launch (kernels whose tile loop takes
+// first_tile / next_tile): the grid is capped at the blocks that are resident
+// at once, and warps take their tiles from the returned counter, zeroed here
+// on the stream.  Lowers P.blocks in place.  The kernel's dynamic shared
+// memory attribute must already be set.
+template <typename Kernel>
+int* persistent_tiles(Kernel k, int threads, size_t smem, int& blocks, Workspace& ws, cudaStream_t s) {
+    int per_sm = 0, dev = 0, sms = 0;
+    LVRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+    LVRGB_CUDA(cudaGetDevice(&dev));
+    LVRGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (per_sm > 0 && sms > 0) blocks = std::min(blocks, per_sm * sms);
+    int* c = ws.get<int>("knn.tiles", 1);
+    LVRGB_CUDA(cudaMemsetAsync(c, 0, sizeof(int), s));
+    return c;
+}
+template <typename Kernel>
+int* persistent_tiles(Kernel k, HeapPlan& P, Workspace& ws, cudaStream_t s) {
+    return persistent_tiles(k, kWarpsPerBlock * 32, P.smem, P.blocks, ws, s);
+}
 
 }  // namespace lvrgb
