@@ -206,11 +206,22 @@ __device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, flo
     unsigned mask = 0;
     if (active) {
         const float tau = heap.tau();
+        const unsigned valid = W.count >= 32 ? kFull : (1u << W.count) - 1u;
+        if (tau == INFINITY) {
+            mask = valid;  // a heap still filling takes every entry
+        } else {
+            // d2 <= tau exactly when d2 - tau_up < 0, tau_up the float above
+            // tau (tau >= 0 is finite): the sign bit of the difference is
+            // the acceptance bit, shifted in from the top so that entry j
+            // ends at bit j.
+            const float tau_up = __uint_as_float(__float_as_uint(tau) + 1u);
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const float4 c = W.buf[j];
-            const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
-            mask |= (d2 <= tau ? 1u : 0u) << j;
+            for (int j = 31; j >= 0; j--) {
+                const float4 c = W.buf[j];
+                const float d2 = dist2(qx, qy, qz, c.x, c.y, c.z);
+                mask = __funnelshift_l(__float_as_uint(__fsub_rn(d2, tau_up)), mask, 1);
+            }
+            mask &= valid;
         }
     }
     st.rounds += __reduce_max_sync(kFull, unsigned(__popc(mask)));
