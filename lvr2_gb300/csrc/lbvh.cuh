@@ -83,14 +83,17 @@ struct TravStats {
 
 // Per-lane max-heap of uint64 keys, lane-interleaved (entry s of lane l at
 // base[s * 32 + l]) so that the 32 lanes of a warp hit distinct banks.  The
-// heap is kHeapArity-ary: a sift-down is a chain of dependent shared-memory
-// loads, one level per step, and the children of a level are independent
-// loads, so a wider node halves the chain (k = 40: 3 levels instead of 6).
-// The first K keys are stored without sifting and heapified once; until then
-// the bound is +inf.
+// heap is kA-ary: a sift-down is a chain of dependent shared-memory loads, one
+// level per step, and the children of a level are independent loads, so a
+// wider node shortens the chain (k = 40: 3 levels instead of 5 for a binary
+// heap).  kComplete: every internal node has all kA children, (K - 1) % kA ==
+// 0 (the launcher guarantees it), so replacements need no bounds tests; k = 40
+// is such a 3-ary heap (1 + 3 + 9 + 27 entries).  The first K keys are stored
+// without sifting and heapified once; until then the bound is +inf.
 constexpr int kHeapArity = 4;
 
-struct LaneHeap {
+template <int kA, bool kComplete>
+struct LaneHeapT {
     unsigned long long* h;
     int K;
     int fill;
@@ -105,29 +108,32 @@ struct LaneHeap {
         top = kKeyEmpty;
     }
     __device__ __forceinline__ float tau() const { return key_d2(top); }
-    // Largest child of a node whose first child is c0 (< end).
+    // Largest child of a node whose first child is c0 (< end); kChecked: some
+    // children may lie at or past end.
+    template <bool kChecked>
     __device__ __forceinline__ void max_child(int c0, int end, unsigned long long& best, int& bc) const {
         best = h[c0 * 32];
         bc = c0;
 #pragma unroll
-            for (int t = 1; t < kHeapArity; t++) {
-                const int c = c0 + t;
-                if (c < end) {
-                    const unsigned long long v = h[c * 32];
-                    if (v > best) {
-                        best = v;
-                        bc = c;
-                    }
+        for (int t = 1; t < kA; t++) {
+            const int c = c0 + t;
+            if (!kChecked || c < end) {
+                const unsigned long long v = h[c * 32];
+                if (v > best) {
+                    best = v;
+                    bc = c;
                 }
             }
+        }
     }
+    template <bool kChecked>
     __device__ __forceinline__ void sift_down(int i, int end, unsigned long long key) {
         while (true) {
-            const int c0 = kHeapArity * i + 1;
+            const int c0 = kA * i + 1;
             if (c0 >= end) break;
             unsigned long long best;
             int bc;
-            max_child(c0, end, best, bc);
+            max_child<kChecked>(c0, end, best, bc);
             if (best <= key) break;
             h[i * 32] = best;
             i = bc;
@@ -135,7 +141,7 @@ struct LaneHeap {
         h[i * 32] = key;
     }
     __device__ __forceinline__ void heapify() {
-        for (int i = (K - 2) / kHeapArity; i >= 0; i--) sift_down(i, K, h[i * 32]);
+        for (int i = (K - 2) / kA; i >= 0; i--) sift_down<true>(i, K, h[i * 32]);
         top = h[0];
     }
     // Replace the maximum by key (caller guarantees key < top).
@@ -147,14 +153,14 @@ struct LaneHeap {
         }
         // the root's level is peeled so that the new maximum is known without
         // reading it back
-        if (K == 1) {
+        if (!kComplete && K == 1) {
             h[0] = key;
             top = key;
             return;
         }
         unsigned long long best;
         int bc;
-        max_child(1, K, best, bc);
+        max_child<!kComplete>(1, K, best, bc);
         if (best <= key) {
             h[0] = key;
             top = key;
@@ -162,7 +168,7 @@ struct LaneHeap {
         }
         h[0] = best;
         top = best;
-        sift_down(bc, K, key);
+        sift_down<!kComplete>(bc, K, key);
     }
     // Completes the heap when fewer than K keys were offered (sentinels).
     __device__ __forceinline__ void finish() {
@@ -179,11 +185,15 @@ struct LaneHeap {
             unsigned long long mx = h[0];
             unsigned long long key = h[end * 32];
             h[end * 32] = mx;
-            sift_down(0, end, key);
+            sift_down<true>(0, end, key);
         }
     }
     __device__ __forceinline__ unsigned long long at(int s) const { return h[s * 32]; }
 };
+using LaneHeap = LaneHeapT<kHeapArity, false>;
+// k = 40 (the first adaptive round of kn = 20) as a complete 3-ary heap
+using LaneHeap3 = LaneHeapT<3, true>;
+__host__ __device__ constexpr bool complete_3ary(int K) { return K >= 4 && (K - 1) % 3 == 0; }
 
 // Per-warp candidate buffer (64 float4 in shared memory, NaN padded) and the
 // warp's query box.  Bucket points pass a cheap warp-level filter (one point
@@ -199,7 +209,8 @@ struct WarpCand {
 
 // Scans buf[0..32) for every lane (entries past `count` are NaN and never
 // accepted), pushes accepted candidates, and drops the scanned entries.
-__device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, float qz, bool active, LaneHeap& heap,
+template <class Heap>
+__device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, float qz, bool active, Heap& heap,
                                             TravStats& st) {
     const int lane = threadIdx.x & 31;
     st.chunks++;
@@ -247,8 +258,9 @@ __device__ __forceinline__ void flush_chunk(WarpCand& W, float qx, float qy, flo
 }
 
 // Adds the points of bucket b that may be within some lane's bound.
+template <class Heap>
 __device__ __forceinline__ void add_bucket(const Lbvh& T, int b, WarpCand& W, float qx, float qy, float qz,
-                                           bool active, LaneHeap& heap, TravStats& st) {
+                                           bool active, Heap& heap, TravStats& st) {
     const int lane = threadIdx.x & 31;
     st.buckets++;
     const int first = b * T.bucket;
@@ -292,8 +304,9 @@ __device__ __forceinline__ int seed_bucket_for(const Lbvh& T, float x, float y, 
 // warp-uniform seed bucket (and seed_radius buckets on each side, which are
 // Morton neighbours) are scanned first so that the k-th distance bound is
 // small before the tree walk; the walk skips them.
+template <class Heap>
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active_in,
-                                             LaneHeap& heap, float4* stage, int* err, TravStats& st,
+                                             Heap& heap, float4* stage, int* err, TravStats& st,
                                              int seed = -1, int root = 0, int blo = 0, int bhi = 0x7fffffff) {
     const int lane = threadIdx.x & 31;
     // A query with a non-finite coordinate has no neighbours (every distance
@@ -432,8 +445,9 @@ __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, 
     if (active_in) heap.finish();
 }
 
+template <class Heap>
 __device__ __forceinline__ void knn_traverse(const Lbvh& T, float qx, float qy, float qz, bool active,
-                                             LaneHeap& heap, float4* stage, int* err, int seed = -1) {
+                                             Heap& heap, float4* stage, int* err, int seed = -1) {
     TravStats st;
     knn_traverse(T, qx, qy, qz, active, heap, stage, err, st, seed);
 }

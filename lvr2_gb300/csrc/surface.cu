@@ -447,7 +447,7 @@ __global__ void list_normals_kernel(Lbvh T, const float* __restrict__ queries, i
 // (up to 102 registers) the kernel runs without spills; smaller heaps leave
 // room for more blocks: six (up to 85 registers) at k = 20 was 2.7% faster
 // on a 76M-point scan project than five without spills.
-template <int kNem, int kMinBlocks>
+template <int kNem, int kMinBlocks, class Heap = LaneHeap>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kernel(NormalsArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kMinBlocks) normals_kerne
         const float4 q = __ldg(A.T.pts + pos);
         // padding after each scan of a segmented tree is not a query
         if (A.segs && __float_as_uint(q.w) == 0xffffffffu) active = false;
-        LaneHeap heap;
+        Heap heap;
         heap.init(ctx.heap, A.K);
         float fx = A.fx, fy = A.fy, fz = A.fz;
         if (A.segs) {
@@ -1249,7 +1249,11 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
     if (A.K <= kSmemHeapMax) {
         HeapPlan P = plan_heap(grid_nq, A.K, ws);
         A.gheap = P.gheap;
-        if (A.K >= kFewBlocksK) {
+        if (A.K >= kFewBlocksK && complete_3ary(A.K)) {
+            set_smem(normals_kernel<kNem, 5, LaneHeap3>, P.smem);
+            A.tiles = persistent_tiles(normals_kernel<kNem, 5, LaneHeap3>, P, ws, s);
+            normals_kernel<kNem, 5, LaneHeap3><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+        } else if (A.K >= kFewBlocksK) {
             set_smem(normals_kernel<kNem, 5>, P.smem);
             A.tiles = persistent_tiles(normals_kernel<kNem, 5>, P, ws, s);
             normals_kernel<kNem, 5><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
