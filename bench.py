@@ -681,23 +681,28 @@ def run_gpu(args):
         cap_v, cap_f = 2 * int(info.vertices) + 1024, 2 * int(info.faces) + 1024
         h_v = torch.empty((cap_v, 3), dtype=torch.float32).pin_memory().numpy()
         h_f = torch.empty((cap_f, 3), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        # the normals are read back on a second stream while the grid, the
+        # distances and the mesh are computed
+        copy_stream = torch.cuda.Stream()
         for _ in range(1):
             s.set_points(pts_h)
             s.calculate_normals()
+            s.normals_async(h_norm, copy_stream)
             s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
             s.optimize_planar_faces(PLANAR_KC)
-            s.normals(out=h_norm)
             s.mesh(with_edges=False, out_vertices=h_v, out_faces=h_f)
+            copy_stream.synchronize()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         d2h = 0
         for _ in range(args.steps):
             s.set_points(pts_h)
             s.calculate_normals()
+            out_n = s.normals_async(h_norm, copy_stream)
             info = s.reconstruct(voxelsize=VOXELSIZE, decomposition="PMC")
             s.optimize_planar_faces(PLANAR_KC)
-            out_n = s.normals(out=h_norm)
             v, f, _ = s.mesh(with_edges=False, out_vertices=h_v, out_faces=h_f)
+            copy_stream.synchronize()
             d2h = out_n.nbytes + v.nbytes + f.nbytes
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps

@@ -145,6 +145,16 @@ lvrgb_status lvrgb_interpolate_normals(lvrgb_surface s, void* stream);
  * (CudaSurface.hpp:99); PointBuffer "normals" channel. */
 lvrgb_status lvrgb_get_normals(lvrgb_surface s, float* normals, int32_t on_device, void* stream);
 
+/* lvrgb_get_normals into host memory without waiting: the copy is ordered
+ * after the work issued so far on `stream` and runs on `copy_stream`, so it
+ * overlaps whatever the caller issues next on `stream` (lvrgb_reconstruct,
+ * lvrgb_optimize_planar_faces).  `normals` should be pinned host memory.  The
+ * caller synchronizes copy_stream before reading `normals`, and does not call
+ * lvrgb_surface_set_points, lvrgb_calculate_normals, lvrgb_set_normals,
+ * lvrgb_interpolate_normals or this function on the same surface until then.
+ * No lvr2 counterpart (lvr2 copies normals synchronously). */
+lvrgb_status lvrgb_get_normals_async(lvrgb_surface s, float* normals, void* stream, void* copy_stream);
+
 /* Normals before interpolation (n x 3), and the k of the search whose
  * neighbourhood fitted each plane (may be NULL). */
 lvrgb_status lvrgb_get_raw_normals(lvrgb_surface s, float* normals, int32_t* k_used, int32_t on_device,

@@ -47,9 +47,11 @@ struct lvrgb_surface_s {
     cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool ev_used[4] = {false, false, false, false};
     float grid_ms[4] = {0, 0, 0, 0};
+    cudaEvent_t copy_ev = nullptr;  // orders lvrgb_get_normals_async's copy stream
     ~lvrgb_surface_s() {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        if (copy_ev) cudaEventDestroy(copy_ev);
     }
 };
 
@@ -494,6 +496,25 @@ lvrgb_status lvrgb_get_normals(lvrgb_surface s, float* normals, int32_t on_devic
         }
         finish_out(normals, d, size_t(n) * 3, on_device, st);
         if (!on_device) LVRGB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+lvrgb_status lvrgb_get_normals_async(lvrgb_surface s, float* normals, void* stream, void* copy_stream) {
+    return guarded([&] {
+        require(s != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "surface is NULL");
+        require(s->has_normals, LVRGB_ERR_STATE, "no normals: call lvrgb_calculate_normals or lvrgb_set_normals");
+        require(normals != nullptr || s->T.n == 0, LVRGB_ERR_INVALID_ARGUMENT, "normals is NULL");
+        DeviceScope dev(s->device);
+        const int n = s->T.n;
+        if (n == 0) return;
+        cudaStream_t st = as_stream(stream), cs = as_stream(copy_stream);
+        float* d = s->ws.get<float>("api.normals_async", size_t(n) * 3);
+        if (!s->copy_ev) LVRGB_CUDA(cudaEventCreateWithFlags(&s->copy_ev, cudaEventDisableTiming));
+        LVRGB_CUDA(cudaEventRecord(s->copy_ev, st));
+        LVRGB_CUDA(cudaStreamWaitEvent(cs, s->copy_ev, 0));
+        morton_to_aos_kernel<<<ceil_div(n, 256), 256, 0, cs>>>(s->normals, s->T.pts, n, d);
+        LVRGB_LAUNCH_CHECK();
+        LVRGB_CUDA(cudaMemcpyAsync(normals, d, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, cs));
     });
 }
 

@@ -165,6 +165,20 @@ class Surface:
         check(_lib.load().lvrgb_get_normals(self._h, _ptr(res), 0, self._stream))
         return res
 
+    def normals_async(self, out, copy_stream):
+        """Starts the copy of the final normals into `out` (a C-contiguous
+        float32 (n, 3) host array, best over pinned memory) on copy_stream (a
+        torch.cuda.Stream or a raw stream handle), ordered after the work
+        issued so far and overlapping what comes next.  Synchronize
+        copy_stream before reading `out`; do not change the points or normals
+        until then."""
+        arr = np.asarray(out)
+        if arr.dtype != np.float32 or arr.shape != (self.n, 3) or not arr.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous float32 (%d, 3) array" % self.n)
+        cs = getattr(copy_stream, "cuda_stream", copy_stream)
+        check(_lib.load().lvrgb_get_normals_async(self._h, _ptr(arr), self._stream, ctypes.c_void_p(cs)))
+        return arr
+
     def raw_normals(self):
         res = np.empty((self.n, 3), np.float32)
         k = np.empty(self.n, np.int32)
