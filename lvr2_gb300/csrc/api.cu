@@ -145,7 +145,8 @@ void check_kernel_error(lvrgb_surface s, cudaStream_t st) {
         throw ApiError{LVRGB_ERR_KERNEL, (h[0] & kErrStack)  ? "kNN traversal exceeded its stack depth"
                                          : (h[0] & kErrWalk) ? "tree walk exceeded its bound (malformed tree)"
                                          : (h[0] & kErrTma)  ? "a TMA copy of marching cubes did not complete"
-                                                             : "a neighbour row was shorter than the RANSAC draws"};
+                                         : (h[0] & kErrTable) ? "the planar pass's edge table had no free slot"
+                                                              : "a neighbour row was shorter than the RANSAC draws"};
     }
 }
 

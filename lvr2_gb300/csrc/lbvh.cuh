@@ -74,6 +74,7 @@ constexpr int kErrStack = 1;   // traversal stack would overflow (never for dept
 constexpr int kErrWalk = 2;    // more node visits than a tree over nbuckets can have
 constexpr int kErrRows = 4;    // a neighbour row shorter than the RANSAC schedule reads
 constexpr int kErrTma = 8;     // a TMA tile copy did not complete within its wait bound
+constexpr int kErrTable = 16;  // a hash table had no free slot (sized to stay at most half full)
 
 // Traversal counters of one warp (nodes, buckets) and one lane (heap
 // insertions); kernels that do not report them let the compiler drop them.

@@ -1,9 +1,10 @@
 // planar.cu -- BilinearFastBox::optimizePlanarFaces (BilinearFastBox.tcc:140-212),
 // the post-pass FastReconstruction::getMesh runs on every cell with kc = 5 for
 // PMC (FastReconstruction.tcc:158-168), on the whole mesh at once:
-//   1. every face edge as an undirected key (min vertex, max vertex), packed
-//      into 2 x (bits of the vertex count) bits and sorted; an edge whose key
-//      occurs once belongs to one face: a border edge,
+//   1. every face edge as an undirected key (min vertex, max vertex) goes
+//      into an open-addressing table (linear probing, at most half full);
+//      the second insertion of a key marks its slot.  An edge whose slot is
+//      unmarked occurs once: it belongs to one face, a border edge,
 //   2. one thread per valid cell counts the border edges of its faces and,
 //      for 1 or 2, marks both end vertices of each,
 //   3. the marked vertices, compacted and Morton-sorted, take the centroid of
@@ -22,23 +23,59 @@ namespace lvrgb {
 
 namespace {
 
-__global__ void edge_keys_kernel(const uint32_t* __restrict__ faces, int nf, int vbits, uint64_t* __restrict__ keys,
-                                 uint32_t* __restrict__ vals) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 3 * nf) return;
-    const int f = i / 3, e = i - 3 * f;
-    const uint64_t a = faces[3 * size_t(f) + e], b = faces[3 * size_t(f) + (e == 2 ? 0 : e + 1)];
-    keys[i] = a < b ? (a << vbits) | b : (b << vbits) | a;
-    vals[i] = uint32_t(i);
+constexpr unsigned long long kSlotEmpty = ~0ull;
+constexpr unsigned long long kSlotTwice = 1ull << 63;  // set by a key's second insertion
+
+// Undirected key of edge e (0..2) of face f: (min vertex) << 32 | max vertex;
+// vertex ids are below 2^31, so bit 63 is free for kSlotTwice.
+__device__ __forceinline__ unsigned long long edge_key(const uint32_t* __restrict__ faces, int f, int e) {
+    const unsigned long long a = faces[3 * size_t(f) + e], b = faces[3 * size_t(f) + (e == 2 ? 0 : e + 1)];
+    return a < b ? (a << 32) | b : (b << 32) | a;
+}
+// 64-bit finaliser of splitmix64 (Steele, Lea, Flood 2014)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
 }
 
-__global__ void border_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, int m,
-                              uint8_t* __restrict__ border) {
+__global__ void edge_insert_kernel(const uint32_t* __restrict__ faces, int nf, unsigned long long* __restrict__ table,
+                                   unsigned long long slot_mask, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    const uint64_t k = keys[i];
-    const bool single = (i == 0 || keys[i - 1] != k) && (i == m - 1 || keys[i + 1] != k);
-    border[vals[i]] = single ? 1 : 0;
+    if (i >= 3 * nf) return;
+    const int f = i / 3;
+    const unsigned long long key = edge_key(faces, f, i - 3 * f);
+    unsigned long long h = mix64(key) & slot_mask;
+    for (unsigned long long probe = 0; probe <= slot_mask; probe++) {
+        const unsigned long long old = atomicCAS(table + h, kSlotEmpty, key);
+        if (old == kSlotEmpty) return;
+        if ((old & ~kSlotTwice) == key) {
+            if (!(old & kSlotTwice)) atomicOr(table + h, kSlotTwice);
+            return;
+        }
+        h = (h + 1) & slot_mask;
+    }
+    atomicOr(err, kErrTable);  // a full table: cannot happen at load <= 1/2
+}
+
+__global__ void border_kernel(const uint32_t* __restrict__ faces, int nf, const unsigned long long* __restrict__ table,
+                              unsigned long long slot_mask, uint8_t* __restrict__ border) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * nf) return;
+    const int f = i / 3;
+    const unsigned long long key = edge_key(faces, f, i - 3 * f);
+    unsigned long long h = mix64(key) & slot_mask;
+    uint8_t b = 1;
+    for (unsigned long long probe = 0; probe <= slot_mask; probe++) {
+        const unsigned long long v = table[h];
+        if ((v & ~kSlotTwice) == key) {
+            b = (v & kSlotTwice) ? 0 : 1;
+            break;
+        }
+        if (v == kSlotEmpty) break;
+        h = (h + 1) & slot_mask;
+    }
+    border[i] = b;
 }
 
 __global__ void mark_kernel(const uint32_t* __restrict__ faces, const uint8_t* __restrict__ border,
@@ -103,21 +140,14 @@ long long optimize_planar_faces(const Lbvh& T, const float* d_box, GridResult& R
     if (nf == 0 || nv == 0 || T.n == 0) return 0;
     const int m3 = 3 * nf;
     // 1. border edges
-    uint64_t* keys = ws.get<uint64_t>("planar.keys", size_t(m3));
-    uint64_t* keys2 = ws.get<uint64_t>("planar.keys2", size_t(m3));
-    uint32_t* vals = ws.get<uint32_t>("planar.vals", size_t(m3));
-    uint32_t* vals2 = ws.get<uint32_t>("planar.vals2", size_t(m3));
-    int vbits = 1;
-    while (vbits < 32 && (uint64_t(1) << vbits) < uint64_t(nv)) vbits++;
-    edge_keys_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(R.faces, nf, vbits, keys, vals);
+    size_t slots = 1024;
+    while (slots < 2 * size_t(m3)) slots *= 2;
+    unsigned long long* table = ws.get<unsigned long long>("planar.edges", slots);
+    LVRGB_CUDA(cudaMemsetAsync(table, 0xff, slots * sizeof(unsigned long long), s));
+    edge_insert_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(R.faces, nf, table, slots - 1, d_err);
     LVRGB_LAUNCH_CHECK();
-    void* tmp = ws.get<unsigned char>("planar.sorttmp", radix_sort_temp_bytes<uint64_t>(size_t(m3)));
-    if (radix_sort_pairs<uint64_t>(keys, vals, keys2, vals2, size_t(m3), 0, 2 * vbits, tmp, s)) {
-        std::swap(keys, keys2);
-        std::swap(vals, vals2);
-    }
     uint8_t* border = ws.get<uint8_t>("planar.border", size_t(m3));
-    border_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(keys, vals, m3, border);
+    border_kernel<<<ceil_div(m3, 256), 256, 0, s>>>(R.faces, nf, table, slots - 1, border);
     LVRGB_LAUNCH_CHECK();
     // 2. marked vertices
     uint32_t* vmark = ws.get<uint32_t>("planar.vmark", size_t(nv));
