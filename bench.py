@@ -625,8 +625,12 @@ def run_gpu(args):
     pts = workload(args.points)
     n = len(pts)
     d_pts = torch.from_numpy(pts).to(f"cuda:{local}")
+    # the surface works on a stream of its own, as a caller of the C ABI would
+    # give it (the legacy default stream serialises with every other stream)
+    work = torch.cuda.Stream(device=local)
+    torch.cuda.synchronize()  # d_pts was written on the default stream
     s = lvr2_gb300.Surface(d_pts, kn=KN, ki=KI, kd=KD, nem=NEM, adaptive=True, flip_point=None, device=local,
-                           bucket=args.bucket, seed_radius=args.seed_radius)
+                           bucket=args.bucket, seed_radius=args.seed_radius, stream=work)
 
     def step():
         s.set_points(d_pts)
@@ -648,13 +652,13 @@ def run_gpu(args):
         torch.cuda.synchronize()
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
-        t_start.record()
+        t_start.record(work)
         for _ in range(args.steps):
             info = step()
             stage += s.timings()
             stats_acc += s.normal_stats()
             infos.append((info.grid_vertices, info.cells_valid, info.faces, info.vertices))
-        t_end.record()
+        t_end.record(work)
         torch.cuda.synchronize()
     launches = (kernel_launches() - l0) // max(args.steps, 1)
     ms = t_start.elapsed_time(t_end) / args.steps
