@@ -650,6 +650,7 @@ def run_gpu(args):
     l0 = kernel_launches()
     stage = np.zeros(8)
     stats_acc = np.zeros(16)
+    sdf_acc = np.zeros(5)
     infos = []
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
@@ -660,6 +661,7 @@ def run_gpu(args):
             info = step()
             stage += s.timings()
             stats_acc += s.normal_stats()
+            sdf_acc += s.distance_stats()[:5].astype(np.float64)
             infos.append((info.grid_vertices, info.cells_valid, info.faces, info.vertices))
         t_end.record(work)
         torch.cuda.synchronize()
@@ -671,6 +673,7 @@ def run_gpu(args):
         ms = float(t.item())
     stage /= args.steps
     stats = stats_acc / args.steps
+    sdf_stats = sdf_acc / args.steps
     nq, ncv, nf, nv = infos[-1]
     value = world * n / (ms / 1000.0)
 
@@ -751,7 +754,12 @@ def run_gpu(args):
                    "normals_nodes_per_warp": float(stats[9]) / max(1.0, n / 32.0),
                    "normals_heap_pushes_per_query": float(stats[10]) / max(1.0, n),
                    "normals_chunks_per_warp": float(stats[11]) / max(1.0, n / 32.0),
-                   "normals_push_rounds_per_warp": float(stats[12]) / max(1.0, n / 32.0)},
+                   "normals_push_rounds_per_warp": float(stats[12]) / max(1.0, n / 32.0),
+                   "sdf_buckets_per_warp": float(sdf_stats[0]) / max(1.0, nq / 32.0),
+                   "sdf_nodes_per_warp": float(sdf_stats[1]) / max(1.0, nq / 32.0),
+                   "sdf_heap_pushes_per_query": float(sdf_stats[2]) / max(1.0, nq),
+                   "sdf_chunks_per_warp": float(sdf_stats[3]) / max(1.0, nq / 32.0),
+                   "sdf_push_rounds_per_warp": float(sdf_stats[4]) / max(1.0, nq / 32.0)},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": int(dom["bytes"]),

@@ -171,6 +171,13 @@ lvrgb_status lvrgb_set_normals(lvrgb_surface s, const float* normals, int32_t on
  * (per warp); other entries 0. */
 lvrgb_status lvrgb_normal_stats(lvrgb_surface s, uint32_t out[16]);
 
+/* Counters of the signed-distance searches of the last lvrgb_reconstruct
+ * (sums over its grid vertices): out[0] LBVH buckets scanned, out[1] tree
+ * nodes expanded (both per 32-query warp tile), out[2] heap insertions,
+ * out[3] 32-candidate chunks scanned, out[4] warp insertion rounds; other
+ * entries 0.  Diagnostics; no lvr2 counterpart. */
+lvrgb_status lvrgb_distance_stats(lvrgb_surface s, uint64_t out[8]);
+
 /* Batched k-nearest-neighbour search: SearchTree::kSearch / kSearchParallel
  * (include/lvr2/reconstruction/SearchTree.hpp:71, 101-125),
  * LBVHIndex::kSearch (LBVHIndex.hpp:135).  Rows of k, ascending; idx =

@@ -24,7 +24,7 @@ STATUS = {
 EXPORTS = [
     "lvrgb_surface_config_default", "lvrgb_surface_create", "lvrgb_surface_destroy", "lvrgb_surface_set_k",
     "lvrgb_surface_set_flip_point", "lvrgb_surface_set_method", "lvrgb_surface_bounding_box",
-    "lvrgb_surface_num_points", "lvrgb_calculate_normals", "lvrgb_get_normals", "lvrgb_get_normals_async", "lvrgb_get_raw_normals",
+    "lvrgb_surface_num_points", "lvrgb_calculate_normals", "lvrgb_get_normals", "lvrgb_get_normals_async", "lvrgb_get_raw_normals", "lvrgb_distance_stats",
     "lvrgb_set_normals", "lvrgb_interpolate_normals", "lvrgb_normal_stats", "lvrgb_knn", "lvrgb_distance",
     "lvrgb_distance_adjoint", "lvrgb_project_to_surface", "lvrgb_grid_distances",
     "lvrgb_interpolated_normal", "lvrgb_reconstruct", "lvrgb_optimize_planar_faces", "lvrgb_mesh_vertex_normals", "lvrgb_vertex_normals", "lvrgb_mesh_vertex_colors", "lvrgb_get_cell_tsdf", "lvrgb_reconstruct_cells", "lvrgb_radius_search", "lvrgb_normals_from_neighbors", "lvrgb_debug_fail_allocation", "lvrgb_debug_round_collapse", "lvrgb_mesh_halfedges", "lvrgb_halfedges", "lvrgb_surface_set_scan_poses", "lvrgb_get_mesh", "lvrgb_get_grid", "lvrgb_get_cells",
@@ -93,6 +93,7 @@ def load(path=None):
     L.lvrgb_calculate_normals.argtypes = [vp, vp]
     L.lvrgb_get_normals.argtypes = [vp, vp, i32, vp]
     L.lvrgb_get_normals_async.argtypes = [vp, vp, vp, vp]
+    L.lvrgb_distance_stats.argtypes = [vp, vp]
     L.lvrgb_get_raw_normals.argtypes = [vp, vp, vp, i32, vp]
     L.lvrgb_set_normals.argtypes = [vp, vp, i32, vp]
     L.lvrgb_interpolate_normals.argtypes = [vp, vp]

@@ -34,6 +34,7 @@ struct lvrgb_surface_s {
     float* d_box = nullptr;
     int* d_err = nullptr;
     uint32_t* d_stats = nullptr;
+    unsigned long long* d_sdf_stats = nullptr;  // signed-distance search counters of the last reconstruct
     float4* normals = nullptr;      // final normals, Morton order
     float4* raw_normals = nullptr;  // before interpolation
     int32_t* kused = nullptr;
@@ -519,6 +520,16 @@ lvrgb_status lvrgb_get_normals_async(lvrgb_surface s, float* normals, void* stre
     });
 }
 
+lvrgb_status lvrgb_distance_stats(lvrgb_surface s, uint64_t out[8]) {
+    return guarded([&] {
+        require(s != nullptr && out != nullptr, LVRGB_ERR_INVALID_ARGUMENT, "NULL argument");
+        DeviceScope dev(s->device);
+        for (int i = 0; i < 8; i++) out[i] = 0;
+        if (s->d_sdf_stats)
+            LVRGB_CUDA(cudaMemcpy(out, s->d_sdf_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    });
+}
+
 lvrgb_status lvrgb_get_raw_normals(lvrgb_surface s, float* normals, int32_t* k_used, int32_t on_device,
                                    void* stream) {
     return guarded([&] {
@@ -800,6 +811,9 @@ lvrgb_status lvrgb_reconstruct(lvrgb_surface s, const lvrgb_grid_config* g, lvrg
         c.extrude = g->extrude;
         c.kd = s->cfg.kd;
         c.decomposition = g->decomposition;
+        if (!s->d_sdf_stats) s->d_sdf_stats = s->ws.get<unsigned long long>("api.sdfstats", 8);
+        LVRGB_CUDA(cudaMemsetAsync(s->d_sdf_stats, 0, 8 * sizeof(unsigned long long), st));
+        c.sdf_stats = s->d_sdf_stats;
         GridTimings tm;
         s->has_grid = false;
         s->ev_used[3] = false;  // a new mesh has had no planar pass yet

@@ -192,6 +192,7 @@ struct SdfArgs {
     int nq;
     double limit;  // 1.75 * voxelsize
     int* tiles = nullptr;  // tile counter of a persistent launch
+    unsigned long long* stats = nullptr;  // optional search counters (GridConfig::sdf_stats)
     float* dist;
     float* eucl;
     uint8_t* invalid;
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) 
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const WarpCtx ctx = warp_ctx<kWarpsPerBlock>(smem, A.gheap, A.K);
+    TravStats st;
     for (int tile = first_tile<kWarpsPerBlock>(A.tiles); tile * 32 < A.nq;
          tile = next_tile<kWarpsPerBlock>(A.tiles, tile)) {
         const int qi = tile * 32 + lane;
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) 
         heap.init(ctx.heap, A.K);
         const float4 q0 = A.qs[tile * 32];
         const int seed = seed_bucket_for(A.T, q0.x, q0.y, q0.z);
-        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, seed);
+        knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, st, seed);
         if (active) {
             heap.sort_ascending();
             float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
@@ -256,6 +258,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) 
             A.dist[row] = proj;
             if (A.eucl) A.eucl[row] = eu;
             if (A.invalid) A.invalid[row] = double(eu) > A.limit ? 1 : 0;
+        }
+    }
+    if (A.stats) {
+        unsigned pushes = st.pushes;
+        for (int o = 16; o > 0; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
+        if (lane == 0 && st.nodes) {
+            atomicAdd(A.stats + 0, (unsigned long long)st.buckets);
+            atomicAdd(A.stats + 1, (unsigned long long)st.nodes);
+            atomicAdd(A.stats + 2, (unsigned long long)pushes);
+            atomicAdd(A.stats + 3, (unsigned long long)st.chunks);
+            atomicAdd(A.stats + 4, (unsigned long long)st.rounds);
         }
     }
 }
@@ -596,7 +609,8 @@ struct StageTimer {
 }  // namespace
 
 void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const float4* qs, int nq, float vs,
-                          float* dist, float* eucl, uint8_t* invalid, Workspace& ws, int* d_err, cudaStream_t s) {
+                          float* dist, float* eucl, uint8_t* invalid, Workspace& ws, int* d_err, cudaStream_t s,
+                          unsigned long long* stats) {
     if (nq == 0) return;
     SdfArgs A;
     A.T = T;
@@ -609,6 +623,7 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
     A.eucl = eucl;
     A.invalid = invalid;
     A.err = d_err;
+    A.stats = stats;
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
     set_smem(sdf_kernel, P.smem);
@@ -888,7 +903,8 @@ void grid_reconstruct(const Lbvh& T, const float4* normals, const float bb[6], c
     R.qp_dist = ws.get<float>("grid.qp_dist", nqp);
     R.qp_eucl = ws.get<float>("grid.qp_eucl", nqp);
     R.qp_invalid = ws.get<uint8_t>("grid.qp_invalid", nqp);
-    signed_distance_rows(T, normals, cfg.kd, qpos, int(nqp), vs, R.qp_dist, R.qp_eucl, R.qp_invalid, ws, d_err, s);
+    signed_distance_rows(T, normals, cfg.kd, qpos, int(nqp), vs, R.qp_dist, R.qp_eucl, R.qp_invalid, ws, d_err, s,
+                         cfg.sdf_stats);
     timer.mark(2, s);
     stage.emplace("lvrgb.culling");
 

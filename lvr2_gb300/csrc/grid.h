@@ -12,6 +12,10 @@ struct GridConfig {
     int extrude = 1;
     int kd = 5;
     int decomposition = 1;  // 0 = MC (FastBox), 1 = PMC (BilinearFastBox)
+    // optional device counters of the signed-distance searches (added to):
+    // buckets scanned, nodes expanded, heap insertions, candidate chunks,
+    // warp insertion rounds
+    unsigned long long* sdf_stats = nullptr;
 };
 
 // Device results of grid_reconstruct; pointers live in the workspace.
@@ -70,6 +74,7 @@ void cell_tsdf(const GridResult& R, float* centers, float* tsdf, cudaStream_t s)
 // row index bits), rows written to dist/eucl; invalid (optional) uses the
 // 1.75 * voxelsize rule of PointsetGrid::calcDistanceValues.
 void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const float4* qs, int nq, float vs,
-                          float* dist, float* eucl, uint8_t* invalid, Workspace& ws, int* d_err, cudaStream_t s);
+                          float* dist, float* eucl, uint8_t* invalid, Workspace& ws, int* d_err, cudaStream_t s,
+                          unsigned long long* stats = nullptr);
 
 }  // namespace lvrgb

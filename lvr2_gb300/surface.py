@@ -179,6 +179,14 @@ class Surface:
         check(_lib.load().lvrgb_get_normals_async(self._h, _ptr(arr), self._stream, ctypes.c_void_p(cs)))
         return arr
 
+    def distance_stats(self):
+        """Counters of the last reconstruct's signed-distance searches:
+        buckets scanned, nodes expanded, heap insertions, candidate chunks,
+        warp insertion rounds (sums; 8 entries)."""
+        out = np.zeros(8, np.uint64)
+        check(_lib.load().lvrgb_distance_stats(self._h, _ptr(out)))
+        return out
+
     def raw_normals(self):
         res = np.empty((self.n, 3), np.float32)
         k = np.empty(self.n, np.int32)
