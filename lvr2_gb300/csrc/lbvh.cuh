@@ -89,12 +89,16 @@ struct TravStats {
 // wider node shortens the chain (k = 40: 3 levels instead of 5 for a binary
 // heap).  kComplete: every internal node has all kA children, (K - 1) % kA ==
 // 0 (the launcher guarantees it), so replacements need no bounds tests; k = 40
-// is such a 3-ary heap (1 + 3 + 9 + 27 entries).  The first K keys are stored
-// without sifting and heapified once; until then the bound is +inf.
+// is such a 3-ary heap (1 + 3 + 9 + 27 entries).  kFixedK = 40 (the launcher
+// guarantees K == 40): the tree is perfect, so a replacement walks at most two
+// levels below the root's children with no leaf test (unrolled).  The first K
+// keys are stored without sifting and heapified once; until then the bound is
+// +inf.
 constexpr int kHeapArity = 4;
 
-template <int kA, bool kComplete>
+template <int kA, bool kComplete, int kFixedK = 0>
 struct LaneHeapT {
+    static constexpr int kLevelsBelow = (kA == 3 && kFixedK == 40) ? 2 : 0;
     unsigned long long* h;
     int K;
     int fill;
@@ -169,7 +173,21 @@ struct LaneHeapT {
         }
         h[0] = best;
         top = best;
-        sift_down<!kComplete>(bc, K, key);
+        if constexpr (kLevelsBelow > 0) {
+            int i = bc;
+#pragma unroll
+            for (int lev = 0; lev < kLevelsBelow; lev++) {
+                unsigned long long b2;
+                int c2;
+                max_child<false>(kA * i + 1, 0, b2, c2);
+                if (b2 <= key) break;
+                h[i * 32] = b2;
+                i = c2;
+            }
+            h[i * 32] = key;
+        } else {
+            sift_down<!kComplete>(bc, K, key);
+        }
     }
     // Completes the heap when fewer than K keys were offered (sentinels).
     __device__ __forceinline__ void finish() {
@@ -194,6 +212,7 @@ struct LaneHeapT {
 using LaneHeap = LaneHeapT<kHeapArity, false>;
 // k = 40 (the first adaptive round of kn = 20) as a complete 3-ary heap
 using LaneHeap3 = LaneHeapT<3, true>;
+using LaneHeap40 = LaneHeapT<3, true, 40>;
 __host__ __device__ constexpr bool complete_3ary(int K) { return K >= 4 && (K - 1) % 3 == 0; }
 
 // Per-warp candidate buffer (64 float4 in shared memory, NaN padded) and the

@@ -1249,7 +1249,11 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
     if (A.K <= kSmemHeapMax) {
         HeapPlan P = plan_heap(grid_nq, A.K, ws);
         A.gheap = P.gheap;
-        if (A.K >= kFewBlocksK && complete_3ary(A.K)) {
+        if (A.K == 40) {
+            set_smem(normals_kernel<kNem, 5, LaneHeap40>, P.smem);
+            A.tiles = persistent_tiles(normals_kernel<kNem, 5, LaneHeap40>, P, ws, s);
+            normals_kernel<kNem, 5, LaneHeap40><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+        } else if (A.K >= kFewBlocksK && complete_3ary(A.K)) {
             set_smem(normals_kernel<kNem, 5, LaneHeap3>, P.smem);
             A.tiles = persistent_tiles(normals_kernel<kNem, 5, LaneHeap3>, P, ws, s);
             normals_kernel<kNem, 5, LaneHeap3><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
