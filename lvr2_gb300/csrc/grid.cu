@@ -214,6 +214,7 @@ __device__ __forceinline__ void normalize_ieee(float& x, float& y, float& z) {
 // the invalid rule of PointsetGrid::calcDistanceValues (PointsetGrid.tcc:133-140).
 // Nine resident blocks is what the shared memory allows at kd = 20; at that
 // bound the kernel may use 56 registers.
+template <class Heap>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 9) sdf_kernel(SdfArgs A) 
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
-        LaneHeap heap;
+        Heap heap;
         heap.init(ctx.heap, A.K);
         const float4 q0 = A.qs[tile * 32];
         const int seed = seed_bucket_for(A.T, q0.x, q0.y, q0.z);
@@ -626,9 +627,15 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
     A.stats = stats;
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
-    set_smem(sdf_kernel, P.smem);
-    A.tiles = persistent_tiles(sdf_kernel, P, ws, s);
-    sdf_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    if (A.K == 20) {
+        set_smem(sdf_kernel<LaneHeap20>, P.smem);
+        A.tiles = persistent_tiles(sdf_kernel<LaneHeap20>, P, ws, s);
+        sdf_kernel<LaneHeap20><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else {
+        set_smem(sdf_kernel<LaneHeap>, P.smem);
+        A.tiles = persistent_tiles(sdf_kernel<LaneHeap>, P, ws, s);
+        sdf_kernel<LaneHeap><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    }
     LVRGB_LAUNCH_CHECK();
 }
 

@@ -98,7 +98,12 @@ constexpr int kHeapArity = 4;
 
 template <int kA, bool kComplete, int kFixedK = 0>
 struct LaneHeapT {
-    static constexpr int kLevelsBelow = (kA == 3 && kFixedK == 40) ? 2 : 0;
+    // levels below the root's children that a replacement can walk, for the
+    // fixed sizes: k = 40 as a perfect 3-ary tree (two, no leaf tests), k = 20
+    // as a 4-ary tree whose last internal node (4) lacks its fourth child
+    // (one, that child tested)
+    static constexpr int kLevelsBelow = (kA == 3 && kFixedK == 40) ? 2 : (kA == 4 && kFixedK == 20) ? 1 : 0;
+    static constexpr bool kPerfect = kA == 3 && kFixedK == 40;
     unsigned long long* h;
     int K;
     int fill;
@@ -158,14 +163,14 @@ struct LaneHeapT {
         }
         // the root's level is peeled so that the new maximum is known without
         // reading it back
-        if (!kComplete && K == 1) {
+        if (!kComplete && kFixedK == 0 && K == 1) {
             h[0] = key;
             top = key;
             return;
         }
         unsigned long long best;
         int bc;
-        max_child<!kComplete>(1, K, best, bc);
+        max_child<!(kComplete || kFixedK > kA)>(1, K, best, bc);
         if (best <= key) {
             h[0] = key;
             top = key;
@@ -177,9 +182,19 @@ struct LaneHeapT {
             int i = bc;
 #pragma unroll
             for (int lev = 0; lev < kLevelsBelow; lev++) {
-                unsigned long long b2;
-                int c2;
-                max_child<false>(kA * i + 1, 0, b2, c2);
+                const int c0 = kA * i + 1;
+                unsigned long long b2 = h[c0 * 32];
+                int c2 = c0;
+#pragma unroll
+                for (int t = 1; t < kA; t++) {
+                    if (kPerfect || t < kA - 1 || c0 + t < kFixedK) {
+                        const unsigned long long v = h[(c0 + t) * 32];
+                        if (v > b2) {
+                            b2 = v;
+                            c2 = c0 + t;
+                        }
+                    }
+                }
                 if (b2 <= key) break;
                 h[i * 32] = b2;
                 i = c2;
@@ -213,6 +228,7 @@ using LaneHeap = LaneHeapT<kHeapArity, false>;
 // k = 40 (the first adaptive round of kn = 20) as a complete 3-ary heap
 using LaneHeap3 = LaneHeapT<3, true>;
 using LaneHeap40 = LaneHeapT<3, true, 40>;
+using LaneHeap20 = LaneHeapT<4, false, 20>;
 __host__ __device__ constexpr bool complete_3ary(int K) { return K >= 4 && (K - 1) % 3 == 0; }
 
 // Per-warp candidate buffer (64 float4 in shared memory, NaN padded) and the

@@ -1265,8 +1265,13 @@ void launch_normals_nem(NormalsArgs& A, int grid_nq, Workspace& ws, cudaStream_t
             // Smaller heaps keep the one-tile-per-warp grid: the persistent
             // form was 2% slower for k = 20 on a 76.5M-point scan project
             // (and faster, 31.8 -> 29.0 ms, for k = 40 on 10M points).
-            set_smem(normals_kernel<kNem, 6>, P.smem);
-            normals_kernel<kNem, 6><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+            if (A.K == 20) {
+                set_smem(normals_kernel<kNem, 6, LaneHeap20>, P.smem);
+                normals_kernel<kNem, 6, LaneHeap20><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+            } else {
+                set_smem(normals_kernel<kNem, 6>, P.smem);
+                normals_kernel<kNem, 6><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+            }
         }
         A.tiles = nullptr;
         LVRGB_LAUNCH_CHECK();
