@@ -41,8 +41,8 @@ CPU_SAMPLE_FRACTION = 0.02
 # DRAM bytes (read + write) per unit of the two kNN kernels, from one ncu
 # capture of the 2M-point spheres-and-tori case; the normal kernel's traffic
 # is per-point I/O (the neighbour gathers hit L2), so it scales with the points.
-NCU_DRAM_BYTES_PER_NORMAL = (46.562816e6 + 153.217792e6) / 2e6
-NCU_DRAM_BYTES_PER_SDF_VERTEX = (151.707136e6 + 29.174528e6) / 4415248
+NCU_DRAM_BYTES_PER_NORMAL = (46.772224e6 + 155.092224e6) / 2e6
+NCU_DRAM_BYTES_PER_SDF_VERTEX = (150.843648e6 + 28.620544e6) / 4415248
 
 
 def parse():
