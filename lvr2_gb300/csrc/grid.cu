@@ -627,7 +627,11 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
     A.stats = stats;
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
-    if (A.K == 20) {
+    if (A.K == 5) {
+        set_smem(sdf_kernel<LaneHeap5>, P.smem);
+        A.tiles = persistent_tiles(sdf_kernel<LaneHeap5>, P, ws, s);
+        sdf_kernel<LaneHeap5><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else if (A.K == 20) {
         set_smem(sdf_kernel<LaneHeap20>, P.smem);
         A.tiles = persistent_tiles(sdf_kernel<LaneHeap20>, P, ws, s);
         sdf_kernel<LaneHeap20><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);

@@ -104,6 +104,8 @@ struct LaneHeapT {
     // (one, that child tested)
     static constexpr int kLevelsBelow = (kA == 3 && kFixedK == 40) ? 2 : (kA == 4 && kFixedK == 20) ? 1 : 0;
     static constexpr bool kPerfect = kA == 3 && kFixedK == 40;
+    // k = 5: the root's four children are leaves
+    static constexpr bool kFlat = kA == 4 && kFixedK == 5;
     unsigned long long* h;
     int K;
     int fill;
@@ -200,6 +202,8 @@ struct LaneHeapT {
                 i = c2;
             }
             h[i * 32] = key;
+        } else if constexpr (kFlat) {
+            h[bc * 32] = key;
         } else {
             sift_down<!kComplete>(bc, K, key);
         }
@@ -229,6 +233,7 @@ using LaneHeap = LaneHeapT<kHeapArity, false>;
 using LaneHeap3 = LaneHeapT<3, true>;
 using LaneHeap40 = LaneHeapT<3, true, 40>;
 using LaneHeap20 = LaneHeapT<4, false, 20>;
+using LaneHeap5 = LaneHeapT<4, true, 5>;
 __host__ __device__ constexpr bool complete_3ary(int K) { return K >= 4 && (K - 1) % 3 == 0; }
 
 // Per-warp candidate buffer (64 float4 in shared memory, NaN padded) and the

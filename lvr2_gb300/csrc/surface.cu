@@ -966,7 +966,8 @@ struct RowsArgs {
     int* tiles = nullptr;      // tile counter of a persistent launch
 };
 
-__device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, float4 q) {
+template <class Heap>
+__device__ __forceinline__ void emit_row(const RowsArgs& A, Heap& heap, float4 q) {
         heap.sort_ascending();
         const size_t row = __float_as_uint(q.w);
         if (A.normals) {
@@ -1006,6 +1007,7 @@ __device__ __forceinline__ void emit_row(const RowsArgs& A, LaneHeap& heap, floa
         }
 }
 
+template <class Heap>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -1015,7 +1017,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) rows_kernel(RowsArgs A) {
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
-        LaneHeap heap;
+        Heap heap;
         heap.init(ctx.heap, A.K);
         // radius search: keys below (radius2, index 0) are those with d2 < radius2
         if (A.radius2 < FLT_MAX) heap.top = make_key(A.radius2, 0u);
@@ -1732,9 +1734,15 @@ void knn_rows(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx, flo
     }
     HeapPlan P = plan_heap(nq, k, ws);
     A.gheap = P.gheap;
-    set_smem(rows_kernel, P.smem);
-    A.tiles = persistent_tiles(rows_kernel, P, ws, s);
-    rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    if (k == 5 && A.radius2 >= FLT_MAX) {
+        set_smem(rows_kernel<LaneHeap5>, P.smem);
+        A.tiles = persistent_tiles(rows_kernel<LaneHeap5>, P, ws, s);
+        rows_kernel<LaneHeap5><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else {
+        set_smem(rows_kernel<LaneHeap>, P.smem);
+        A.tiles = persistent_tiles(rows_kernel<LaneHeap>, P, ws, s);
+        rows_kernel<LaneHeap><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    }
     LVRGB_LAUNCH_CHECK();
 }
 
@@ -1758,8 +1766,8 @@ void knn_rows_smem(const Lbvh& T, const float4* qs, int nq, int k, uint32_t* idx
                         size_t(kWarpsPerBlock) * size_t(k) * 32 * sizeof(unsigned long long);
     const int tiles = (nq + 31) / 32;
     const int blocks = (tiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    set_smem(rows_kernel, smem);
-    rows_kernel<<<blocks, kWarpsPerBlock * 32, smem, s>>>(A);
+    set_smem(rows_kernel<LaneHeap>, smem);
+    rows_kernel<LaneHeap><<<blocks, kWarpsPerBlock * 32, smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }
 
@@ -1779,8 +1787,8 @@ void interpolated_normal_rows(const Lbvh& T, const float4* normals, int ki, cons
     A.err = d_err;
     HeapPlan P = plan_heap(nq, ki, ws);
     A.gheap = P.gheap;
-    set_smem(rows_kernel, P.smem);
-    rows_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    set_smem(rows_kernel<LaneHeap>, P.smem);
+    rows_kernel<LaneHeap><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     LVRGB_LAUNCH_CHECK();
 }
 
