@@ -89,11 +89,11 @@ struct TravStats {
 // wider node shortens the chain (k = 40: 3 levels instead of 5 for a binary
 // heap).  kComplete: every internal node has all kA children, (K - 1) % kA ==
 // 0 (the launcher guarantees it), so replacements need no bounds tests; k = 40
-// is such a 3-ary heap (1 + 3 + 9 + 27 entries).  kFixedK = 40 (the launcher
-// guarantees K == 40): the tree is perfect, so a replacement walks at most two
-// levels below the root's children with no leaf test (unrolled).  The first K
-// keys are stored without sifting and heapified once; until then the bound is
-// +inf.
+// is such a 3-ary heap (1 + 3 + 9 + 27 entries).  kFixedK: the launcher
+// guarantees K == kFixedK, and a replacement walks the levels below the root's
+// children unrolled, with only the bounds tests that size needs (k = 40, 20,
+// 5; see kLevelsBelow).  The first K keys are stored without sifting and
+// heapified once; until then the bound is +inf.
 constexpr int kHeapArity = 4;
 
 template <int kA, bool kComplete, int kFixedK = 0>
@@ -229,7 +229,9 @@ struct LaneHeapT {
     __device__ __forceinline__ unsigned long long at(int s) const { return h[s * 32]; }
 };
 using LaneHeap = LaneHeapT<kHeapArity, false>;
-// k = 40 (the first adaptive round of kn = 20) as a complete 3-ary heap
+// complete 3-ary heaps (K = 1 + 3m: 37, 43, ... with five resident blocks),
+// and the fixed sizes: k = 40 (kn = 20's first adaptive round), k = 20 (kd =
+// 20, kn = 10's first round), k = 5 (the planar pass, kd = 5)
 using LaneHeap3 = LaneHeapT<3, true>;
 using LaneHeap40 = LaneHeapT<3, true, 40>;
 using LaneHeap20 = LaneHeapT<4, false, 20>;
