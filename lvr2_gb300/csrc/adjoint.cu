@@ -40,7 +40,8 @@ struct SdfEval {
     float proj, eucl;
 };
 
-__device__ __forceinline__ SdfEval eval_sdf(const Lbvh& T, const float4* __restrict__ normals, const LaneHeap& heap,
+template <class Heap>
+__device__ __forceinline__ SdfEval eval_sdf(const Lbvh& T, const float4* __restrict__ normals, const Heap& heap,
                                             float qx, float qy, float qz) {
     SdfEval E;
     float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
@@ -84,6 +85,7 @@ struct GradArgs {
     int* tiles = nullptr;  // tile counter of a persistent launch
 };
 
+template <class Heap>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_adjoint_kernel(GradArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) sdf_adjoint_kernel(GradAr
         const int qi = tile * 32 + lane;
         const bool active = qi < A.nq;
         const float4 q = active ? A.qs[qi] : make_float4(0, 0, 0, 0);
-        LaneHeap heap;
+        Heap heap;
         heap.init(ctx.heap, A.K);
         const float4 q0 = A.qs[tile * 32];
         knn_traverse(A.T, q.x, q.y, q.z, active, heap, ctx.stage, A.err, seed_bucket_for(A.T, q0.x, q0.y, q0.z));
@@ -153,6 +155,7 @@ struct ProjectArgs {
 
 // Newton steps toward the zero level: x <- x - d(x) nh(x), a new kd
 // neighbourhood at every step.
+template <class Heap>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) project_kernel(ProjectArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) project_kernel(ProjectArg
         float x = q.x, y = q.y, z = q.z;
         float nh[3] = {0, 0, 0};
         for (int step = 0; step < A.steps; step++) {
-            LaneHeap heap;
+            Heap heap;
             heap.init(ctx.heap, A.K);
             const float sx = __shfl_sync(kFull, x, 0), sy = __shfl_sync(kFull, y, 0), sz = __shfl_sync(kFull, z, 0);
             knn_traverse(A.T, x, y, z, active, heap, ctx.stage, A.err, seed_bucket_for(A.T, sx, sy, sz));
@@ -216,9 +219,15 @@ void distance_adjoint(const Lbvh& T, const float4* normals, int kd, const float4
     A.err = d_err;
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
-    set_smem(sdf_adjoint_kernel, P.smem);
-    A.tiles = persistent_tiles(sdf_adjoint_kernel, P, ws, s);
-    sdf_adjoint_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    if (complete_3ary(A.K)) {
+        set_smem(sdf_adjoint_kernel<LaneHeap3>, P.smem);
+        A.tiles = persistent_tiles(sdf_adjoint_kernel<LaneHeap3>, P, ws, s);
+        sdf_adjoint_kernel<LaneHeap3><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else {
+        set_smem(sdf_adjoint_kernel<LaneHeap>, P.smem);
+        A.tiles = persistent_tiles(sdf_adjoint_kernel<LaneHeap>, P, ws, s);
+        sdf_adjoint_kernel<LaneHeap><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    }
     LVRGB_LAUNCH_CHECK();
 }
 
@@ -238,9 +247,15 @@ void project_to_surface(const Lbvh& T, const float4* normals, int kd, const floa
     A.err = d_err;
     HeapPlan P = plan_heap(nq, A.K, ws);
     A.gheap = P.gheap;
-    set_smem(project_kernel, P.smem);
-    A.tiles = persistent_tiles(project_kernel, P, ws, s);
-    project_kernel<<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    if (complete_3ary(A.K)) {
+        set_smem(project_kernel<LaneHeap3>, P.smem);
+        A.tiles = persistent_tiles(project_kernel<LaneHeap3>, P, ws, s);
+        project_kernel<LaneHeap3><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else {
+        set_smem(project_kernel<LaneHeap>, P.smem);
+        A.tiles = persistent_tiles(project_kernel<LaneHeap>, P, ws, s);
+        project_kernel<LaneHeap><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    }
     LVRGB_LAUNCH_CHECK();
 }
 

@@ -635,6 +635,10 @@ void signed_distance_rows(const Lbvh& T, const float4* normals, int kd, const fl
         set_smem(sdf_kernel<LaneHeap20>, P.smem);
         A.tiles = persistent_tiles(sdf_kernel<LaneHeap20>, P, ws, s);
         sdf_kernel<LaneHeap20><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
+    } else if (complete_3ary(A.K)) {
+        set_smem(sdf_kernel<LaneHeap3>, P.smem);
+        A.tiles = persistent_tiles(sdf_kernel<LaneHeap3>, P, ws, s);
+        sdf_kernel<LaneHeap3><<<P.blocks, kWarpsPerBlock * 32, P.smem, s>>>(A);
     } else {
         set_smem(sdf_kernel<LaneHeap>, P.smem);
         A.tiles = persistent_tiles(sdf_kernel<LaneHeap>, P, ws, s);
